@@ -1,0 +1,44 @@
+/*
+ * ref_shim_cpu3d.cpp -- host build of the reference CPU code's per-cell
+ * functions (CPU_3D/CPU_3D.cpp from bgk_collide up to main(), CPU:116-1209),
+ * staged by oracle/ref_recipe.py into oracle/_ref/cpu3d_body.inc.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Exposes bgk_collide, mrt_collide and the
+ * regularised lid boundary DirichletWest_Regularized on n cells (cell-major).
+ */
+#include <sys/time.h>
+
+#include <cmath>
+#include <cstdlib>
+#include <iostream>
+
+using namespace std;
+
+#include "cpu3d_body.inc"
+
+#define F19(g) g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7], g[8], g[9], g[10], g[11], g[12], g[13], g[14], g[15], g[16], g[17], g[18]
+
+extern "C" {
+
+void ref_cpu3d_bgk(float* f, int n, float omega) {
+    for (int i = 0; i < n; ++i) {
+        float* g = f + 19L * i;
+        bgk_collide(F19(g), omega);
+    }
+}
+
+void ref_cpu3d_mrt(float* f, int n, float omega) {
+    for (int i = 0; i < n; ++i) {
+        float* g = f + 19L * i;
+        mrt_collide(F19(g), omega);
+    }
+}
+
+void ref_cpu3d_lid_west(float* f, int n) {
+    for (int i = 0; i < n; ++i) {
+        float* g = f + 19L * i;
+        DirichletWest_Regularized(F19(g), 1, 1);
+    }
+}
+
+}  // extern "C"
