@@ -1,0 +1,149 @@
+/*
+ * lbm_gb300.h -- C ABI of the GB300 D3Q19 stream-collide engine.
+ *
+ * The reference (gladyslol/LBM_MultiGPU) has no library API: its programs are
+ * configured by #define blocks, record their parameters in a ".inputs" file,
+ * drive the kernels from main() and write tecplot/.force files.  This header
+ * replaces that boundary with functions a host program (or an FFI binding)
+ * calls; each entry point names the reference code it stands in for.
+ *
+ * Conventions: every function returns 0 (LBM_OK) or an LBM_ERR_* code and
+ * lbm_last_error() gives the message of the last failure on the calling
+ * thread.  A handle is driven by one host thread at a time and owns one CUDA
+ * stream.  Population arrays crossing the ABI are compact structure-of-arrays
+ * float[19][nz][ny][nx] in the reference's velocity order; fields are
+ * float[nz][ny][nx]; "velocity" is the momentum sum c_q f_q, as in the
+ * reference's output (LRTurbTest/LRMultiGPU7.cu:2368-2370).
+ * Level 0 is the base grid, level 1 the refinement patch.
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum lbm_status {
+    LBM_OK = 0,
+    LBM_ERR_ARG = 1,        /* bad argument or size */
+    LBM_ERR_CUDA = 2,       /* a CUDA call failed (message has the CUDA error) */
+    LBM_ERR_PARSE = 3,      /* malformed .inputs record */
+    LBM_ERR_CONFIG = 4,     /* inconsistent configuration (e.g. LRLEVEL vs LRFACTOR) */
+    LBM_ERR_NOMEM = 5,
+    LBM_ERR_STATE = 6       /* call not valid in the handle's state */
+};
+
+/* node types of the solid/boundary mask (the reference's ImageFcn codes in
+ * brackets, LRTurbTest/LRMultiGPU7.cu:88-127) */
+enum lbm_node {
+    LBM_FLUID = 0,          /* [0] */
+    LBM_WALL = 1,           /* [1]   full-way bounce-back */
+    LBM_BODY = 2,           /* [10]  full-way bounce-back + momentum-exchange force */
+    LBM_WEST_INLET = 3,     /* [400] West_Extrap, LR7:852-897 */
+    LBM_EAST_OUTLET = 4,    /* [300] East_Extrap, LR7:805-850 */
+    LBM_SOUTH_INLET = 5,    /* [200] South_Extrap, LR7:760-803 */
+    LBM_NORTH_OUTLET = 6,   /* [100] North_Extrap, LR7:713-758 */
+    LBM_LID = 7             /* [53 in CPU_3D] regularised moving lid, CPU_3D/CPU_3D.cpp:974-1054 */
+};
+
+typedef struct lbm_handle lbm_handle;
+
+const char* lbm_last_error(void);
+const char* lbm_version(void);
+
+/* ---- host-only helpers (no CUDA device needed) ---- */
+
+/* Parse a .inputs record and write it back in WriteInputs' format
+ * (LR7:2547-2573) with the derived omega / omegaLR lines recomputed
+ * (LR7:2607-2619).  Same length/capacity convention as lbm_write_inputs. */
+int lbm_inputs_normalize(const char* inputs_text, char* buf, size_t cap, size_t* len);
+/* Node mask a record describes (ImageFcn for level 0, ImageFcnLR for level
+ * 1, LR7:68-127), uint8[nz][ny][nx] of lbm_node values; *n = node count */
+int lbm_inputs_mask(const char* inputs_text, int level, uint8_t* mask, size_t cap, size_t* n);
+/* Tecplot POINT zone of one level in WriteResults' layout (LR7:2350-2442;
+ * WriteResultsLR, LR7:2444-2535, for level 1) from compact populations f and
+ * optional statistics stats4 (float[4][nz][ny][nx] or NULL for zeros).  The
+ * zone goes to buf, the slice rows (k == 1 on level 0, k == 3 on level 1) to
+ * slice; length/capacity convention as lbm_write_inputs for both. */
+int lbm_format_tecplot(const char* inputs_text, int level, const float* f, const float* stats4, char* buf,
+                       size_t cap, size_t* len, char* slice, size_t slice_cap, size_t* slice_len);
+
+/* ---- handle API: the reference program's main() (LR7:2575-3029) ---- */
+
+/* Parse a .inputs record (the text WriteInputs produces, LR7:2547-2573, plus
+ * the DPDY line of MRTtest/DynInlet3.cu and the extension keys listed in
+ * INTEGRATION.md), allocate both grid levels on the current CUDA device,
+ * build the node masks from the configured geometry (ImageFcn / ImageFcnLR)
+ * and initialise at equilibrium (initialize / initializeLR, LR7:1060-1125). */
+int lbm_create(const char* inputs_text, lbm_handle** out);
+int lbm_destroy(lbm_handle* h);
+
+/* nx, ny, nz of a level; nlevels is 2 with refinement, else 1 */
+int lbm_get_dims(const lbm_handle* h, int level, int* nx, int* ny, int* nz);
+int lbm_get_nlevels(const lbm_handle* h, int* nlevels);
+/* relaxation rates (LR7:2607-2619): omega, omegaLR, SF_cf, SF_fc */
+int lbm_get_params(const lbm_handle* h, float* omega4);
+/* steps taken so far */
+int lbm_get_time(const lbm_handle* h, int* t);
+
+/* node mask of a level, uint8[nz][ny][nx] of lbm_node values */
+int lbm_get_mask(const lbm_handle* h, int level, uint8_t* mask);
+int lbm_set_mask(lbm_handle* h, int level, const uint8_t* mask);
+
+/* equilibrium at rho = 1 and the configured initial velocity */
+int lbm_init_equilibrium(lbm_handle* h);
+int lbm_get_populations(lbm_handle* h, int level, float* f);
+int lbm_set_populations(lbm_handle* h, int level, const float* f);
+
+/* Advance n base-grid steps; with refinement every base step runs LRLEVEL
+ * patch sub-steps and the two interpolations (the loop of LR7:2849-2950). */
+int lbm_step(lbm_handle* h, int nsteps);
+/* Same, timed on the handle's stream with CUDA events; *ms = elapsed time */
+int lbm_step_timed(lbm_handle* h, int nsteps, float* ms);
+int lbm_synchronize(lbm_handle* h);
+
+/* density and momentum of a level (any pointer may be NULL) */
+int lbm_get_fields(lbm_handle* h, int level, float* rho, float* u, float* v, float* w);
+/* running statistics (velAv u/v, velFluc u/v: LR7:1018-1058), float[4][nz][ny][nx] */
+int lbm_get_stats(lbm_handle* h, int level, float* stats4);
+
+/* momentum-exchange force per step, FP64, fxyz[3*i + k] for step STARTF + i
+ * (the reference's FX/FY/FZ arrays, LR7:1607-1626); *n = entries written */
+int lbm_get_forces(lbm_handle* h, double* fxyz, int max_steps, int* n);
+
+/* FP64 mass and momentum of the non-solid nodes of a level: out4 = {M, Jx, Jy, Jz} */
+int lbm_audit(lbm_handle* h, int level, double* out4);
+
+/* ---- run record and outputs (LR7:2350-2573) ---- */
+
+/* the .inputs record of this handle (WriteInputs); returns the length in
+ * *len, writes at most cap bytes including the terminating NUL */
+int lbm_write_inputs(const lbm_handle* h, char* buf, size_t cap, size_t* len);
+/* CASENAME.dat (empty), CASENAME_part<n>.dat, CASENAME_slice.dat,
+ * CASENAME.force, CASENAME.inputs (WriteResults, WriteResultsLR,
+ * WriteForces, WriteInputs) */
+int lbm_write_outputs(lbm_handle* h, const char* casename);
+
+/* ---- kernel-level API on caller-owned device buffers ---- */
+
+/* One stream-collide step of a level from device buffer fA into fB: the work
+ * of update_inn/update_top/update_bot (LR7:1127-1628) over a single domain
+ * with periodic z.  Buffers are float[19][nz][ny][pitch] (pitch a multiple of
+ * 32, >= nx), mask uint8[nz][ny][pitch].  model: 0 MRT (LR7 mrt_collide),
+ * 1 MRT with bgk_meq (DynInlet3), 2 BGK, 3 CPU_3D MRT.  les != 0 folds the
+ * Smagorinsky eddy viscosity into tau (cs is the reference's CS).  When
+ * force_out != NULL the FP64 momentum-exchange force of this step is ADDED to
+ * force_out[0..2] (device memory); scratch must then hold
+ * lbm_force_scratch_doubles(nx, ny, nz, pitch) doubles of device memory. */
+int lbm_stream_collide_f32(const float* fA, float* fB, const uint8_t* mask, int nx, int ny, int nz, int pitch,
+                           int model, int les, float omega, float cs, float u_in, float rho_out, int t,
+                           double* force_out, double* scratch, void* cuda_stream);
+size_t lbm_force_scratch_doubles(int nx, int ny, int nz, int pitch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,321 @@
+"""GB300-native D3Q19 lattice-Boltzmann stream-collide engine.
+
+Python mirror of the C ABI in ``include/lbm_gb300.h`` (ctypes, no torch on the
+hot path).  The compute path is ``lbm_multigpu_gb300/_build/liblbm_gb300.so``,
+hand-written CUDA for sm_103a; importing this package never falls back to a
+CPU implementation: if the library is missing, :func:`library` raises.
+
+The reference (gladyslol/LBM_MultiGPU) is driven by ``#define`` blocks and
+records each run in a ``.inputs`` file (LRTurbTest/LRMultiGPU7.cu:2547-2573);
+:class:`Solver` takes that record as its configuration, and
+:func:`make_inputs` writes one from keyword arguments.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+__all__ = ["Solver", "LbmError", "library", "make_inputs", "normalize_inputs", "inputs_mask", "format_tecplot", "NODE", "MODELS"]
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "liblbm_gb300.so"
+
+NODE = dict(FLUID=0, WALL=1, BODY=2, WEST_INLET=3, EAST_OUTLET=4, SOUTH_INLET=5, NORTH_OUTLET=6, LID=7)
+MODELS = dict(MRT=0, MRT_DI3=1, BGK=2, MRT_CPU3D=3)
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_F = ctypes.c_float
+_SZ = ctypes.c_size_t
+
+# (name, restype, argtypes) for every function of include/lbm_gb300.h
+SIGNATURES = [
+    ("lbm_last_error", ctypes.c_char_p, []),
+    ("lbm_version", ctypes.c_char_p, []),
+    ("lbm_inputs_normalize", _I, [ctypes.c_char_p, ctypes.c_char_p, _SZ, ctypes.POINTER(_SZ)]),
+    ("lbm_inputs_mask", _I, [ctypes.c_char_p, _I, _P, _SZ, ctypes.POINTER(_SZ)]),
+    ("lbm_format_tecplot", _I, [ctypes.c_char_p, _I, _P, _P, ctypes.c_char_p, _SZ, ctypes.POINTER(_SZ),
+                                ctypes.c_char_p, _SZ, ctypes.POINTER(_SZ)]),
+    ("lbm_create", _I, [ctypes.c_char_p, ctypes.POINTER(_P)]),
+    ("lbm_destroy", _I, [_P]),
+    ("lbm_get_dims", _I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    ("lbm_get_nlevels", _I, [_P, ctypes.POINTER(_I)]),
+    ("lbm_get_params", _I, [_P, _P]),
+    ("lbm_get_time", _I, [_P, ctypes.POINTER(_I)]),
+    ("lbm_get_mask", _I, [_P, _I, _P]),
+    ("lbm_set_mask", _I, [_P, _I, _P]),
+    ("lbm_init_equilibrium", _I, [_P]),
+    ("lbm_get_populations", _I, [_P, _I, _P]),
+    ("lbm_set_populations", _I, [_P, _I, _P]),
+    ("lbm_step", _I, [_P, _I]),
+    ("lbm_step_timed", _I, [_P, _I, ctypes.POINTER(_F)]),
+    ("lbm_synchronize", _I, [_P]),
+    ("lbm_get_fields", _I, [_P, _I, _P, _P, _P, _P]),
+    ("lbm_get_stats", _I, [_P, _I, _P]),
+    ("lbm_get_forces", _I, [_P, _P, _I, ctypes.POINTER(_I)]),
+    ("lbm_audit", _I, [_P, _I, _P]),
+    ("lbm_write_inputs", _I, [_P, ctypes.c_char_p, _SZ, ctypes.POINTER(_SZ)]),
+    ("lbm_write_outputs", _I, [_P, ctypes.c_char_p]),
+    ("lbm_stream_collide_f32", _I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _F, _F, _F, _F, _I, _P, _P, _P]),
+    ("lbm_force_scratch_doubles", _SZ, [_I, _I, _I, _I]),
+]
+
+
+class LbmError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"lbm error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def library(path: str | os.PathLike | None = None) -> ctypes.CDLL:
+    """Load liblbm_gb300.so (built in-tree by lbm_multigpu_gb300.build)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: run `python -m lbm_multigpu_gb300.build` (or __graft_entry__.build())")
+    lib = ctypes.CDLL(str(p))
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise LbmError(rc, library().lbm_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray) -> ctypes.c_void_p:
+    return a.ctypes.data_as(_P)
+
+
+def _fmt(v) -> str:
+    # C++ ostream default formatting (6 significant digits) as WriteInputs uses
+    if isinstance(v, (int, np.integer)):
+        return str(int(v))
+    s = f"{float(np.float32(v)):.6g}"
+    if "e" in s:
+        m, e = s.split("e")
+        s = f"{m}e{int(e):+03d}"
+    return s
+
+
+def make_inputs(nx: int, ny: int, nz: int, *, obst1=(0.0, 0.0, 0.0), r1=1.0, obst2=(0.0, 0.0, 0.0), r2=0.0,
+                re=100.0, umax=0.05, tmax=1000, startf=0, start_velav=100000, start_velfluc=250000,
+                refinement=0, model="MRT", les=0, cs=0.02, lr_dims=(128, 80, 8), lr_factor=0.5,
+                lr_origin=(128.25, 64.25, -0.75), dpdy=None, **ext) -> str:
+    """A .inputs record in the reference's WriteInputs layout (LR7:2547-2573).
+
+    The derived ``omega`` lines are left for the library to recompute; extension
+    keys (geometry, precision, tau, lid, noise, ...) are passed as keyword
+    arguments named after the record keys: geometry="cavity", tau=0.6,
+    lid_velocity=(0.05, 0, 0), lid_face="+z", precision="fp16",
+    inlet_noise=0.01, seed=12345, velav=1, init=1, init_velocity=0.0.
+    """
+    def tup(t):
+        return "(" + ",".join(_fmt(v) for v in t) + ")"
+
+    lines = [
+        ("Base domain size", f"{nx}x{ny}x{nz}"),
+        ("Base blocksize:", "64x1x1"),
+        ("Obst1 location:", tup(obst1)),
+        ("Obst1 radius:", _fmt(r1)),
+        ("Obst2 location:", tup(obst2)),
+        ("Obst2 radius:", _fmt(r2)),
+        ("RE:", _fmt(re)),
+        ("UMAX:", _fmt(umax)),
+    ]
+    if dpdy is not None:
+        lines.append(("DPDY", ": " + _fmt(dpdy)))
+    lines += [
+        ("TMAX:", _fmt(tmax)),
+        ("STARTF:", _fmt(startf)),
+        ("START_VELAV:", _fmt(start_velav)),
+        ("START_VELFLUC:", _fmt(start_velfluc)),
+        ("REFINEMENT:", _fmt(refinement)),
+        ("MODEL:", model),
+        ("Smagorinsky LES:", _fmt(les)),
+        ("CS:", _fmt(cs)),
+        ("LR domain size", "x".join(str(int(v)) for v in lr_dims)),
+        ("LR factor", _fmt(lr_factor)),
+        ("LR location", "x".join(_fmt(v) for v in lr_origin)),
+        ("LR blocksize:", "64x1x1"),
+        ("GPUs per node", ": 1"),
+    ]
+    names = {"geometry": "GEOMETRY:", "precision": "PRECISION:", "tau": "TAU:", "lid_velocity": "LID velocity:",
+             "lid_face": "LID face:", "inlet_noise": "Inlet noise:", "seed": "Seed:", "velav": "VELAV:",
+             "init": "Init:", "init_velocity": "Init velocity:", "order": "ORDER:", "fc_top_zflip": "FC top zflip:"}
+    for k, v in ext.items():
+        if k not in names:
+            raise KeyError(f"unknown .inputs extension key {k!r}")
+        lines.append((names[k], tup(v) if isinstance(v, (tuple, list)) else (v if isinstance(v, str) else _fmt(v))))
+    return "".join(f"{k} \t{v}\n" for k, v in lines)
+
+
+def normalize_inputs(text: str) -> str:
+    """Parse a record and write it back in the reference's format (no GPU)."""
+    lib = library()
+    n = _SZ(0)
+    _check(lib.lbm_inputs_normalize(text.encode(), None, 0, ctypes.byref(n)))
+    buf = ctypes.create_string_buffer(n.value + 1)
+    _check(lib.lbm_inputs_normalize(text.encode(), buf, n.value + 1, ctypes.byref(n)))
+    return buf.value.decode()
+
+
+def inputs_mask(text: str, level: int = 0) -> np.ndarray:
+    """Node mask a record describes, uint8[nz][ny][nx] (no GPU)."""
+    lib = library()
+    n = _SZ(0)
+    _check(lib.lbm_inputs_mask(text.encode(), level, None, 0, ctypes.byref(n)))
+    m = np.zeros(n.value, np.uint8)
+    _check(lib.lbm_inputs_mask(text.encode(), level, _ptr(m), m.size, ctypes.byref(n)))
+    return m
+
+
+def format_tecplot(text: str, f: np.ndarray, level: int = 0, stats: np.ndarray | None = None) -> tuple[str, str]:
+    """(zone, slice) tecplot text of populations f in WriteResults' layout (no GPU)."""
+    lib = library()
+    f = np.ascontiguousarray(f, np.float32)
+    st = None if stats is None else np.ascontiguousarray(stats, np.float32)
+    n, m = _SZ(0), _SZ(0)
+    args = (text.encode(), level, _ptr(f), None if st is None else _ptr(st))
+    _check(lib.lbm_format_tecplot(*args, None, 0, ctypes.byref(n), None, 0, ctypes.byref(m)))
+    a, b = ctypes.create_string_buffer(n.value + 1), ctypes.create_string_buffer(m.value + 1)
+    _check(lib.lbm_format_tecplot(*args, a, n.value + 1, ctypes.byref(n), b, m.value + 1, ctypes.byref(m)))
+    return a.value.decode(), b.value.decode()
+
+
+class Solver:
+    """One simulation on the current CUDA device (``lbm_create`` ... ``lbm_destroy``)."""
+
+    def __init__(self, inputs_text: str):
+        self._lib = library()
+        h = _P()
+        _check(self._lib.lbm_create(inputs_text.encode(), ctypes.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.lbm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- shape and parameters --
+    @property
+    def nlevels(self) -> int:
+        n = _I()
+        _check(self._lib.lbm_get_nlevels(self._h, ctypes.byref(n)))
+        return n.value
+
+    def dims(self, level: int = 0) -> tuple[int, int, int]:
+        a, b, c = _I(), _I(), _I()
+        _check(self._lib.lbm_get_dims(self._h, level, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def params(self) -> dict:
+        o = np.zeros(4, np.float32)
+        _check(self._lib.lbm_get_params(self._h, _ptr(o)))
+        return dict(omega=float(o[0]), omega_lr=float(o[1]), sf_cf=float(o[2]), sf_fc=float(o[3]))
+
+    @property
+    def time(self) -> int:
+        t = _I()
+        _check(self._lib.lbm_get_time(self._h, ctypes.byref(t)))
+        return t.value
+
+    # -- state --
+    def mask(self, level: int = 0) -> np.ndarray:
+        nx, ny, nz = self.dims(level)
+        m = np.zeros((nz, ny, nx), np.uint8)
+        _check(self._lib.lbm_get_mask(self._h, level, _ptr(m)))
+        return m
+
+    def set_mask(self, mask: np.ndarray, level: int = 0) -> None:
+        nx, ny, nz = self.dims(level)
+        m = np.ascontiguousarray(mask, np.uint8).reshape(nz, ny, nx)
+        _check(self._lib.lbm_set_mask(self._h, level, _ptr(m)))
+
+    def init_equilibrium(self) -> None:
+        _check(self._lib.lbm_init_equilibrium(self._h))
+
+    def populations(self, level: int = 0) -> np.ndarray:
+        nx, ny, nz = self.dims(level)
+        f = np.zeros((19, nz, ny, nx), np.float32)
+        _check(self._lib.lbm_get_populations(self._h, level, _ptr(f)))
+        return f
+
+    def set_populations(self, f: np.ndarray, level: int = 0) -> None:
+        nx, ny, nz = self.dims(level)
+        g = np.ascontiguousarray(f, np.float32).reshape(19, nz, ny, nx)
+        _check(self._lib.lbm_set_populations(self._h, level, _ptr(g)))
+
+    # -- time stepping --
+    def step(self, n: int = 1) -> None:
+        _check(self._lib.lbm_step(self._h, n))
+
+    def step_timed(self, n: int) -> float:
+        ms = _F()
+        _check(self._lib.lbm_step_timed(self._h, n, ctypes.byref(ms)))
+        return float(ms.value)
+
+    def synchronize(self) -> None:
+        _check(self._lib.lbm_synchronize(self._h))
+
+    # -- outputs --
+    def fields(self, level: int = 0) -> tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray]:
+        nx, ny, nz = self.dims(level)
+        out = [np.zeros((nz, ny, nx), np.float32) for _ in range(4)]
+        _check(self._lib.lbm_get_fields(self._h, level, *(_ptr(a) for a in out)))
+        return tuple(out)
+
+    def stats(self, level: int = 0) -> np.ndarray:
+        nx, ny, nz = self.dims(level)
+        s = np.zeros((4, nz, ny, nx), np.float32)
+        _check(self._lib.lbm_get_stats(self._h, level, _ptr(s)))
+        return s
+
+    def forces(self, max_steps: int | None = None) -> np.ndarray:
+        n = max(self.time, 1) if max_steps is None else max_steps
+        f = np.zeros((n, 3), np.float64)
+        got = _I()
+        _check(self._lib.lbm_get_forces(self._h, _ptr(f), n, ctypes.byref(got)))
+        return f[: got.value]
+
+    def audit(self, level: int = 0) -> np.ndarray:
+        o = np.zeros(4, np.float64)
+        _check(self._lib.lbm_audit(self._h, level, _ptr(o)))
+        return o
+
+    def inputs_text(self) -> str:
+        n = _SZ(0)
+        _check(self._lib.lbm_write_inputs(self._h, None, 0, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value + 1)
+        _check(self._lib.lbm_write_inputs(self._h, buf, n.value + 1, ctypes.byref(n)))
+        return buf.value.decode()
+
+    def write_outputs(self, casename: str) -> None:
+        _check(self._lib.lbm_write_outputs(self._h, casename.encode()))

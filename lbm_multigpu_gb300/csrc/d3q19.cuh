@@ -1,0 +1,446 @@
+/*
+ * d3q19.cuh -- per-cell D3Q19 operators of the stream-collide path (device code).
+ *
+ * Velocity ordering, moment basis and relaxation follow the reference
+ * (LRTurbTest/LRMultiGPU7.cu, "LR7"):
+ *   moments / basis          LR7:258-279
+ *   mrt_collide (+ LES)      LR7:583-711
+ *   *_Extrap rebuilds        LR7:713-897
+ *   DynInlet3 MRT / BGK      MRTtest/DynInlet3.cu:599-832
+ *   CPU_3D MRT               CPU_3D/CPU_3D.cpp:164-409
+ * The arithmetic is organised for the GPU: populations are handled in
+ * opposite-velocity pairs (even and odd parts), which halves the work of both
+ * the forward moment transform and its inverse, and the Smagorinsky stress
+ * |Pi_neq| is taken from the non-equilibrium moments the collision already has
+ * instead of from 19 separately built equilibria (the two are the same linear
+ * map: Pi_neq = sum c c f - rho/3 I - j j for every equilibrium used here).
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lbm_kernels.cuh"
+
+namespace lbm {
+
+__host__ __device__ constexpr int cx(int q) {
+    return (q == 1 || q == 5 || q == 8 || q == 10 || q == 15) ? 1 : (q == 3 || q == 6 || q == 7 || q == 12 || q == 17) ? -1 : 0;
+}
+__host__ __device__ constexpr int cy(int q) {
+    return (q == 2 || q == 5 || q == 6 || q == 11 || q == 16) ? 1 : (q == 4 || q == 7 || q == 8 || q == 13 || q == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int cz(int q) { return (q >= 9 && q <= 13) ? 1 : (q >= 14) ? -1 : 0; }
+__host__ __device__ constexpr int opp(int q) {
+    return q == 0 ? 0 : q <= 4 ? ((q + 1) % 4 + 1) : q <= 8 ? ((q - 5 + 2) % 4 + 5) : q == 9 ? 14 : q == 14 ? 9 :
+           q == 10 ? 17 : q == 17 ? 10 : q == 11 ? 18 : q == 18 ? 11 : q == 12 ? 15 : q == 15 ? 12 : q == 13 ? 16 : 13;
+}
+/* lattice weights (the equilibrium at rest), used for the offset storage f - w */
+__host__ __device__ constexpr float wq(int q) {
+    return q == 0 ? 1.f / 3.f : (q <= 4 || q == 9 || q == 14) ? 1.f / 18.f : 1.f / 36.f;
+}
+
+/* Smagorinsky relaxation (LR7:683-685): tau = tau0/2 + sqrt(tau0^2 + 18 sqrt2 CS Q)/2.
+ * The reference's CS enters where the textbook formula has Cs^2. */
+template <class T> __host__ __device__ __forceinline__ T smag_omega(T omega, T cs, T qn) {
+    T tau0 = T(1) / omega;
+    T tau = T(0.5) * tau0 + T(0.5) * sqrt(tau0 * tau0 + T(18) * cs * T(1.4142135623730951) * qn);
+    return T(1) / tau;
+}
+
+/* Moment-space collision shared by the three MRT flavours.
+ * VAR: MRT (LR7), MRT_DI3 (bgk_meq equilibria, then AddForce) or MRT_CPU3D
+ * (CPU_3D's meq2 sign and rate-1 m13/m14). */
+template <int VAR, class T>
+__host__ __device__ __forceinline__ void collide_mrt(T f[19], T omega, bool les, T cs, T dpdy) {
+    /* even / odd parts of the opposite pairs */
+    const T sx = f[1] + f[3], dx = f[1] - f[3];
+    const T sy = f[2] + f[4], dy = f[2] - f[4];
+    const T sz = f[9] + f[14], dz = f[9] - f[14];
+    const T a5 = f[5] + f[7], b5 = f[5] - f[7];
+    const T a6 = f[6] + f[8], b6 = f[6] - f[8];
+    const T a10 = f[10] + f[17], b10 = f[10] - f[17];
+    const T a12 = f[12] + f[15], b12 = f[12] - f[15];
+    const T a11 = f[11] + f[18], b11 = f[11] - f[18];
+    const T a13 = f[13] + f[16], b13 = f[13] - f[16];
+
+    const T axy = a5 + a6, axz = a10 + a12, ayz = a11 + a13;
+    const T sax = sx + sy + sz, sdi = axy + axz + ayz;
+    const T rho = f[0] + sax + sdi;
+    const T Dx = b5 - b6 + b10 - b12, Dy = b5 + b6 + b11 - b13, Dz = b10 + b12 + b11 + b13;
+    const T jx = dx + Dx, jy = dy + Dy, jz = dz + Dz;
+    const T jxx = jx * jx, jyy = jy * jy, jzz = jz * jz;
+    const T usq = jxx + jyy + jzz;
+
+    /* non-equilibrium moments n_k = m_k - meq_k */
+    T n1 = T(19) * ((sax + T(2) * sdi) - rho - usq);
+    T n2 = T(12) * f[0] - T(4) * sax + sdi;
+    T n9 = T(2) * sx - sy - sz + axy + axz - T(2) * ayz;
+    T n10 = T(-4) * sx + T(2) * sy + T(2) * sz + axy + axz - T(2) * ayz;
+    T n11 = sy - sz + axy - axz;
+    T n12 = T(-2) * sy + T(2) * sz + axy - axz;
+    const T m9eq = T(2) * jxx - (jyy + jzz), m11eq = jyy - jzz;
+    if (VAR == MRT_DI3) {
+        n2 -= T(3) * rho - T(5.5) * usq;
+        n10 -= T(-0.5) * m9eq * T(0.333333333333);
+        n12 -= T(-0.5) * m11eq;
+    } else if (VAR == MRT_CPU3D) {
+        n2 += T(7.53968254) * usq;
+    } else {
+        n2 -= T(7.53968254) * usq;
+    }
+    n9 -= m9eq;
+    n11 -= m11eq;
+    T n13 = (a5 - a6) - jx * jy;
+    T n14 = (a11 - a13) - jy * jz;
+    T n15 = (a10 - a12) - jx * jz;
+    const T two3 = T(0.666666667);
+    const T n4 = T(-4) * dx + Dx + two3 * jx;
+    const T n6 = T(-4) * dy + Dy + two3 * jy;
+    const T n8 = T(-4) * dz + Dz + two3 * jz;
+    const T n16 = b5 - b6 - b10 + b12;
+    const T n17 = -b5 - b6 + b11 - b13;
+    const T n18 = b10 + b12 - b11 - b13;
+
+    if (les) {
+        /* Pi_neq from the stress moments: Pi_xx = n1/57 + n9/3,
+         * Pi_yy + Pi_zz = n1/19 - Pi_xx, Pi_yy - Pi_zz = n11 */
+        const T tr = n1 * T(1.0 / 19.0);
+        const T pxx = n1 * T(1.0 / 57.0) + n9 * T(1.0 / 3.0);
+        const T pyy = T(0.5) * (tr - pxx + n11), pzz = T(0.5) * (tr - pxx - n11);
+        const T qn = sqrt(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (n13 * n13 + n14 * n14 + n15 * n15));
+        omega = smag_omega(omega, cs, qn);
+    }
+    /* relaxation: stress moments with omega, the rest to equilibrium */
+    n9 *= omega;
+    n11 *= omega;
+    n15 *= omega;
+    if (VAR == MRT_CPU3D) {
+        /* CPU_3D relaxes m13 and m14 at rate 1 (CPU:246-248) */
+    } else {
+        n13 *= omega;
+        n14 *= omega;
+    }
+    /* scaled by the row norms of the basis: f -= M^T diag(1/|M_k|^2) dm */
+    const T g1 = n1 * T(1.0 / 2394.0), g2 = n2 * T(1.0 / 252.0);
+    const T g4 = n4 * T(0.025), g6 = n6 * T(0.025), g8 = n8 * T(0.025);
+    const T g9 = n9 * T(1.0 / 36.0), g10 = n10 * T(1.0 / 72.0);
+    const T g11 = n11 * T(1.0 / 12.0), g12 = n12 * T(1.0 / 24.0);
+    const T g13 = n13 * T(0.25), g14 = n14 * T(0.25), g15 = n15 * T(0.25);
+    const T g16 = n16 * T(0.125), g17 = n17 * T(0.125), g18 = n18 * T(0.125);
+
+    const T axis = T(-11) * g1 - T(4) * g2;
+    const T diag = T(8) * g1 + g2;
+    const T p9 = g9 - T(2) * g10;   /* -(9,10) combination on y/z axes */
+    f[0] -= T(-30) * g1 + T(12) * g2;
+    {   /* x axis pair (1,3) */
+        const T e = axis + T(2) * g9 - T(4) * g10, o = T(-4) * g4;
+        f[1] -= e + o;
+        f[3] -= e - o;
+    }
+    {   /* y axis pair (2,4) */
+        const T e = axis - p9 + g11 - T(2) * g12, o = T(-4) * g6;
+        f[2] -= e + o;
+        f[4] -= e - o;
+    }
+    {   /* z axis pair (9,14) */
+        const T e = axis - p9 - g11 + T(2) * g12, o = T(-4) * g8;
+        f[9] -= e + o;
+        f[14] -= e - o;
+    }
+    const T dxy = diag + g9 + g10 + g11 + g12;
+    const T dxz = diag + g9 + g10 - g11 - g12;
+    const T dyz = diag - T(2) * g9 - T(2) * g10;
+    {   /* (5,7): c = (1,1,0) */
+        const T e = dxy + g13, o = g4 + g6 + g16 - g17;
+        f[5] -= e + o;
+        f[7] -= e - o;
+    }
+    {   /* (6,8): c = (-1,1,0) */
+        const T e = dxy - g13, o = -g4 + g6 - g16 - g17;
+        f[6] -= e + o;
+        f[8] -= e - o;
+    }
+    {   /* (10,17): c = (1,0,1) */
+        const T e = dxz + g15, o = g4 + g8 - g16 + g18;
+        f[10] -= e + o;
+        f[17] -= e - o;
+    }
+    {   /* (12,15): c = (-1,0,1) */
+        const T e = dxz - g15, o = -g4 + g8 + g16 + g18;
+        f[12] -= e + o;
+        f[15] -= e - o;
+    }
+    {   /* (11,18): c = (0,1,1) */
+        const T e = dyz + g14, o = g6 + g8 + g17 - g18;
+        f[11] -= e + o;
+        f[18] -= e - o;
+    }
+    {   /* (13,16): c = (0,-1,1) */
+        const T e = dyz - g14, o = -g6 + g8 - g17 - g18;
+        f[13] -= e + o;
+        f[16] -= e - o;
+    }
+    if (VAR == MRT_DI3 && dpdy != T(0)) {
+        /* AddForce (DI3:229-252) */
+        const T a = T(0.0555555556) * T(3) * dpdy, b = T(0.0277777778) * T(3) * dpdy;
+        f[2] -= a;
+        f[4] += a;
+        f[5] -= b;
+        f[6] -= b;
+        f[7] += b;
+        f[8] += b;
+        f[11] -= b;
+        f[13] += b;
+        f[16] -= b;
+        f[18] += b;
+    }
+}
+
+/* BGK with the incompressible equilibrium w (rho + 3 c.j + 4.5 (c.j)^2 - 1.5 j^2)
+ * (DI3:806-827, CPU:116-162), optional Smagorinsky and AddForce (DI3:830). */
+template <class T> __host__ __device__ __forceinline__ void collide_bgk(T f[19], T omega, bool les, T cs, T dpdy) {
+    T rho = 0, jx = 0, jy = 0, jz = 0;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        rho += f[q];
+        if (cx(q)) jx += T(cx(q)) * f[q];
+        if (cy(q)) jy += T(cy(q)) * f[q];
+        if (cz(q)) jz += T(cz(q)) * f[q];
+    }
+    const T usq = jx * jx + jy * jy + jz * jz;
+    if (les) {
+        T pxx = 0, pyy = 0, pzz = 0, pxy = 0, pyz = 0, pxz = 0;
+#pragma unroll
+        for (int q = 1; q < 19; ++q) {
+            if (cx(q)) pxx += f[q];
+            if (cy(q)) pyy += f[q];
+            if (cz(q)) pzz += f[q];
+            if (cx(q) * cy(q)) pxy += T(cx(q) * cy(q)) * f[q];
+            if (cy(q) * cz(q)) pyz += T(cy(q) * cz(q)) * f[q];
+            if (cx(q) * cz(q)) pxz += T(cx(q) * cz(q)) * f[q];
+        }
+        const T third = rho * T(1.0 / 3.0);
+        pxx -= third + jx * jx;
+        pyy -= third + jy * jy;
+        pzz -= third + jz * jz;
+        pxy -= jx * jy;
+        pyz -= jy * jz;
+        pxz -= jx * jz;
+        const T qn = sqrt(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (pxy * pxy + pyz * pyz + pxz * pxz));
+        omega = smag_omega(omega, cs, qn);
+    }
+    const T base = rho - T(1.5) * usq;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const T cu = T(cx(q)) * jx + T(cy(q)) * jy + T(cz(q)) * jz;
+        const T feq = T(wq(q)) * (base + T(3) * cu + T(4.5) * cu * cu);
+        f[q] -= omega * (f[q] - feq);
+    }
+    if (dpdy != T(0)) {
+        const T a = T(0.0555555556) * T(3) * dpdy, b = T(0.0277777778) * T(3) * dpdy;
+        f[2] -= a;
+        f[4] += a;
+        f[5] -= b;
+        f[6] -= b;
+        f[7] += b;
+        f[8] += b;
+        f[11] -= b;
+        f[13] += b;
+        f[16] -= b;
+        f[18] += b;
+    }
+}
+
+template <class T>
+__host__ __device__ __forceinline__ void collide(int model, T f[19], T omega, bool les, T cs, T dpdy) {
+    switch (model) {
+        case MRT: collide_mrt<MRT>(f, omega, les, cs, dpdy); break;
+        case MRT_DI3: collide_mrt<MRT_DI3>(f, omega, les, cs, dpdy); break;
+        case MRT_CPU3D: collide_mrt<MRT_CPU3D>(f, omega, les, cs, dpdy); break;
+        default: collide_bgk(f, omega, les, cs, dpdy); break;
+    }
+}
+
+/* *_Extrap rebuild (LR7:713-897): keep every moment of the neighbour's
+ * populations except density (outlets) or momentum (inlets); as a linear map
+ *   f_q += (rho_new - rho)/19 + c_q.(j_new - j)/10 */
+template <class T> __host__ __device__ __forceinline__ void extrap(int type, T f[19], T rho_bc, T u_in) {
+    T rho = 0, jx = 0, jy = 0, jz = 0;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        rho += f[q];
+        if (cx(q)) jx += T(cx(q)) * f[q];
+        if (cy(q)) jy += T(cy(q)) * f[q];
+        if (cz(q)) jz += T(cz(q)) * f[q];
+    }
+    T drho = 0, djx = 0, djy = 0, djz = 0;
+    if (type == EAST_OUTLET || type == NORTH_OUTLET) {
+        drho = rho_bc - rho;
+    } else if (type == WEST_INLET) {
+        djx = u_in - jx;
+        djy = -jy;
+        djz = -jz;
+    } else if (type == SOUTH_INLET) {
+        djx = -jx;
+        djy = u_in - jy;
+        djz = -jz;
+    }
+    const T r = drho * T(1.0 / 19.0);
+    djx *= T(0.1);
+    djy *= T(0.1);
+    djz *= T(0.1);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) f[q] += r + T(cx(q)) * djx + T(cy(q)) * djy + T(cz(q)) * djz;
+}
+
+/* Regularised velocity boundary for a moving lid on any face (the reference's
+ * DirichletWest_Regularized, CPU:974-1054, written per face): density from the
+ * known populations, unknowns by non-equilibrium bounce-back, then
+ * f = feq + 4.5 w_q (c_q c_q - I/3) : Pi_neq. */
+template <class T> __host__ __device__ __forceinline__ void lid(T f[19], int face, T ux, T uy, T uz) {
+    const int axis = face >> 1;
+    const int sgn = (face & 1) ? -1 : 1;
+    T s0 = 0, s1 = 0;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const int cn = (axis == 0 ? cx(q) : axis == 1 ? cy(q) : cz(q)) * sgn;
+        if (cn == 0) s0 += f[q];
+        else if (cn < 0) s1 += f[q];
+    }
+    const T un = (axis == 0 ? ux : axis == 1 ? uy : uz) * T(sgn);
+    const T rho = un + (s0 + T(2) * s1);
+    const T usq = ux * ux + uy * uy + uz * uz;
+    T feq[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const T cu = T(cx(q)) * ux + T(cy(q)) * uy + T(cz(q)) * uz;
+        feq[q] = T(wq(q)) * (rho + T(3) * cu + T(4.5) * cu * cu - T(1.5) * usq);
+    }
+    T g[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) g[q] = f[q] - feq[q];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const int cn = (axis == 0 ? cx(q) : axis == 1 ? cy(q) : cz(q)) * sgn;
+        if (cn > 0) g[q] = g[opp(q)];
+    }
+    T P[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int q = 1; q < 19; ++q) {
+        P[0] += T(cx(q) * cx(q)) * g[q];
+        P[1] += T(cy(q) * cy(q)) * g[q];
+        P[2] += T(cz(q) * cz(q)) * g[q];
+        P[3] += T(cx(q) * cy(q)) * g[q];
+        P[4] += T(cy(q) * cz(q)) * g[q];
+        P[5] += T(cx(q) * cz(q)) * g[q];
+    }
+    const T tr = (P[0] + P[1] + P[2]) * T(1.0 / 3.0);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const T s = T(cx(q) * cx(q)) * P[0] + T(cy(q) * cy(q)) * P[1] + T(cz(q) * cz(q)) * P[2] +
+                    T(2 * cx(q) * cy(q)) * P[3] + T(2 * cy(q) * cz(q)) * P[4] + T(2 * cx(q) * cz(q)) * P[5] - tr;
+        f[q] = feq[q] + T(wq(q)) * T(4.5) * s;
+    }
+}
+
+/* PhysicalMoments (LR7:380-391): rho, j, m9, m11, m13, m14, m15 */
+template <class T> __host__ __device__ __forceinline__ void physical_moments(const T f[19], T mom[9]) {
+    const T sx = f[1] + f[3], sy = f[2] + f[4], sz = f[9] + f[14];
+    const T a5 = f[5] + f[7], a6 = f[6] + f[8], a10 = f[10] + f[17], a12 = f[12] + f[15];
+    const T a11 = f[11] + f[18], a13 = f[13] + f[16];
+    const T b5 = f[5] - f[7], b6 = f[6] - f[8], b10 = f[10] - f[17], b12 = f[12] - f[15];
+    const T b11 = f[11] - f[18], b13 = f[13] - f[16];
+    const T axy = a5 + a6, axz = a10 + a12, ayz = a11 + a13;
+    mom[0] = f[0] + sx + sy + sz + axy + axz + ayz;
+    mom[1] = (f[1] - f[3]) + b5 - b6 + b10 - b12;
+    mom[2] = (f[2] - f[4]) + b5 + b6 + b11 - b13;
+    mom[3] = (f[9] - f[14]) + b10 + b12 + b11 + b13;
+    mom[4] = T(2) * sx - sy - sz + axy + axz - T(2) * ayz;
+    mom[5] = sy - sz + axy - axz;
+    mom[6] = a5 - a6;
+    mom[7] = a11 - a13;
+    mom[8] = a10 - a12;
+}
+
+/* StrainRate (LR7:351-377) with the reference's omega = 1, m1 = 0, dx = 1 */
+template <class T> __host__ __device__ __forceinline__ void strain_rate(const T mom[9], T S[6]) {
+    const T u = mom[1], v = mom[2], w = mom[3];
+    const T n9 = mom[4] - (T(2) * u * u - (v * v + w * w));
+    const T n11 = mom[5] - (v * v - w * w);
+    S[0] = T(-0.5) * n9;
+    S[1] = T(0.25) * (n9 - T(3) * n11);
+    S[2] = T(0.25) * (n9 + T(3) * n11);
+    S[3] = T(-1.5) * (mom[6] - u * v);
+    S[4] = T(-1.5) * (mom[7] - v * w);
+    S[5] = T(-1.5) * (mom[8] - u * w);
+}
+
+template <class T> __host__ __device__ __forceinline__ T strain_mag(const T S[6]) {
+    return sqrt(T(2) * (S[0] * S[0] + S[1] * S[1] + S[2] * S[2] + T(2) * (S[3] * S[3] + S[4] * S[4] + S[5] * S[5])));
+}
+
+/* equilibrium moments with the non-equilibrium stress scaled by SF, back to
+ * populations (InvertPhysicalMoments, LR7:421-465) */
+template <class T> __host__ __device__ __forceinline__ void invert_scaled(const T mom[9], T SF, T f[19]) {
+    const T rho = mom[0], u = mom[1], v = mom[2], w = mom[3];
+    const T usq = u * u + v * v + w * w;
+    const T one = T(1) - SF;
+    const T m1 = T(-11) * rho + T(19) * usq, m2 = T(7.53968254) * usq;
+    const T m4 = T(-0.666666667) * u, m6 = T(-0.666666667) * v, m8 = T(-0.666666667) * w;
+    const T m9 = mom[4] * SF + one * (T(2) * u * u - (v * v + w * w));
+    const T m11 = mom[5] * SF + one * (v * v - w * w);
+    const T m13 = mom[6] * SF + one * u * v;
+    const T m14 = mom[7] * SF + one * v * w;
+    const T m15 = mom[8] * SF + one * u * w;
+    const T g0 = rho * T(1.0 / 19.0), g1 = m1 * T(1.0 / 2394.0), g2 = m2 * T(1.0 / 252.0);
+    const T gu = u * T(0.1), gv = v * T(0.1), gw = w * T(0.1);
+    const T g4 = m4 * T(0.025), g6 = m6 * T(0.025), g8 = m8 * T(0.025);
+    const T g9 = m9 * T(1.0 / 36.0), g11 = m11 * T(1.0 / 12.0);
+    const T g13 = m13 * T(0.25), g14 = m14 * T(0.25), g15 = m15 * T(0.25);
+    const T axis = g0 + T(-11) * g1 - T(4) * g2;
+    const T diag = g0 + T(8) * g1 + g2;
+    f[0] = g0 + T(-30) * g1 + T(12) * g2;
+    f[1] = axis + T(2) * g9 + (gu - T(4) * g4);
+    f[3] = axis + T(2) * g9 - (gu - T(4) * g4);
+    f[2] = axis - g9 + g11 + (gv - T(4) * g6);
+    f[4] = axis - g9 + g11 - (gv - T(4) * g6);
+    f[9] = axis - g9 - g11 + (gw - T(4) * g8);
+    f[14] = axis - g9 - g11 - (gw - T(4) * g8);
+    const T dxy = diag + g9 + g11, dxz = diag + g9 - g11, dyz = diag - T(2) * g9;
+    f[5] = dxy + g13 + (gu + gv + g4 + g6);
+    f[7] = dxy + g13 - (gu + gv + g4 + g6);
+    f[6] = dxy - g13 + (-gu + gv - g4 + g6);
+    f[8] = dxy - g13 - (-gu + gv - g4 + g6);
+    f[10] = dxz + g15 + (gu + gw + g4 + g8);
+    f[17] = dxz + g15 - (gu + gw + g4 + g8);
+    f[12] = dxz - g15 + (-gu + gw - g4 + g8);
+    f[15] = dxz - g15 - (-gu + gw - g4 + g8);
+    f[11] = dyz + g14 + (gv + gw + g6 + g8);
+    f[18] = dyz + g14 - (gv + gw + g6 + g8);
+    f[13] = dyz - g14 + (-gv + gw - g6 + g8);
+    f[16] = dyz - g14 - (-gv + gw - g6 + g8);
+}
+
+/* Philox4x32-10 (Salmon et al., SC'11): counter (cell, step, 0, 0), key
+ * (seed, 0); returns a uniform float in [0, 1) from the first output word.
+ * Used for the seeded inlet noise, an extension the reference does not have. */
+__host__ __device__ __forceinline__ float philox_uniform(uint32_t seed, uint32_t cell, uint32_t step) {
+    uint32_t c0 = cell, c1 = step, c2 = 0u, c3 = 0u, k0 = seed, k1 = 0u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = uint64_t(0xD2511F53u) * c0;
+        const uint64_t p1 = uint64_t(0xCD9E8D57u) * c2;
+        const uint32_t hi0 = uint32_t(p0 >> 32), lo0 = uint32_t(p0);
+        const uint32_t hi1 = uint32_t(p1 >> 32), lo1 = uint32_t(p1);
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return float(c0 >> 8) * (1.0f / 16777216.0f);
+}
+
+}  // namespace lbm

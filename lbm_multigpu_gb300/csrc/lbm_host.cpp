@@ -1,0 +1,1067 @@
+/*
+ * lbm_host.cpp -- host side of the GB300 D3Q19 engine behind the C ABI of
+ * include/lbm_gb300.h.
+ *
+ * It replaces the reference program's main() (LRTurbTest/LRMultiGPU7.cu,
+ * "LR7", lines 2575-3029): the .inputs run record becomes the runtime
+ * configuration (parsed here, written back byte-compatibly by WriteInputs'
+ * format, LR7:2547-2573), ImageFcn/ImageFcnLR (LR7:68-127) build a one-byte
+ * node mask per level on the host, and the time loop (LR7:2849-2950) becomes
+ * a sequence of launches on one CUDA stream with no host synchronisation
+ * between steps.  The reference's z-slab decomposition over GPUs with peer
+ * copies of halo planes is replaced by one domain per level with periodic z.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/lbm_gb300.h"
+#include "lbm_kernels.cuh"
+
+using namespace lbm;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CUDA_TRY(call)                                                                      \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) return fail(LBM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+/* ------------------------------------------------------------------------ */
+/* configuration: the .inputs record                                          */
+/* ------------------------------------------------------------------------ */
+
+struct Config {
+    int nx = 0, ny = 0, nz = 0;
+    int bs[3] = {64, 1, 1};
+    float ob1[3] = {0, 0, 0}, r1 = 0;
+    float ob2[3] = {0, 0, 0}, r2 = 0;
+    float re = 100.f, umax = 0.05f;
+    float omega_rec = 0;            /* the recorded omega line (informative) */
+    bool has_dpdy = false;
+    float dpdy = 0;
+    int tmax = 1000, startf = 0, start_av = 100000, start_fluc = 250000;
+    int refinement = 0;
+    std::string model = "MRT";
+    int les = 0;
+    float cs = 0.02f;
+    int lrx = 128, lry = 80, lrz = 8;
+    float lrfactor = 0.5f;
+    float lrx0 = 128.25f, lry0 = 64.25f, lrz0 = -0.75f;
+    int lbs[3] = {64, 1, 1};
+    float omega_lr_rec = 0;
+    int gpus = 1;
+    /* extension keys (not in the reference record) */
+    std::string geometry = "channel_square";
+    std::string precision = "fp32";
+    float tau = 0;                  /* > 0: tau0 given directly instead of RE */
+    float lid_u[3] = {0, 0, 0};
+    bool lid_u_set = false;
+    int lid_face = 5;               /* +z */
+    float noise = 0;
+    uint32_t seed = 12345u;
+    int velav = 0;
+    int init = -1;                  /* 0: MRT equilibrium, 1: BGK equilibrium; -1: by model */
+    float init_u = -1e30f;          /* default: UMAX (channel), 0 (cavity / periodic) */
+    int order = 2;
+    int fc_zflip = 1;
+    /* older records spell the LES line "Smagorinski LES: YES/NO"; DynInlet
+     * records add "KP" (the inlet P-control gain, MRTtest/DynInlet3.cu:26) */
+    bool les_yesno = false;
+    float kp = 0;
+    /* the parsed record's lines: label and separator as written, canonical key */
+    struct Line {
+        std::string label, sep, key;
+    };
+    std::vector<Line> layout;
+};
+
+std::string trim(const std::string& s) {
+    size_t a = s.find_first_not_of(" \t\r\n"), b = s.find_last_not_of(" \t\r\n");
+    return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+}
+
+bool parse_xyz_int(const std::string& v, int out[3]) {
+    return sscanf(v.c_str(), "%dx%dx%d", &out[0], &out[1], &out[2]) == 3;
+}
+bool parse_xyz_float_x(const std::string& v, float out[3]) {
+    return sscanf(v.c_str(), "%fx%fx%f", &out[0], &out[1], &out[2]) == 3;
+}
+bool parse_tuple(const std::string& v, float out[3]) {
+    return sscanf(v.c_str(), " (%f , %f , %f )", &out[0], &out[1], &out[2]) == 3;
+}
+
+int parse_inputs(const char* text, Config& c) {
+    std::istringstream in(text ? text : "");
+    std::string line;
+    int lineno = 0;
+    bool have_dims = false;
+    while (std::getline(in, line)) {
+        ++lineno;
+        if (trim(line).empty() || trim(line)[0] == '#') continue;
+        size_t tab = line.find('\t');
+        if (tab == std::string::npos) return fail(LBM_ERR_PARSE, ".inputs line %d has no TAB separator: '%s'", lineno, line.c_str());
+        std::string key = trim(line.substr(0, tab));
+        while (!key.empty() && key.back() == ':') key = trim(key.substr(0, key.size() - 1));
+        std::string rest = line.substr(tab + 1);
+        std::string val = trim(rest);
+        std::string sep;
+        if (!val.empty() && val[0] == ':') {
+            sep = rest.substr(0, rest.find(':') + 1);
+            size_t v0 = rest.find_first_not_of(' ', sep.size());
+            sep = rest.substr(0, v0 == std::string::npos ? rest.size() : v0);
+            val = trim(val.substr(1));
+        }
+        if (key == "Smagorinski LES") {
+            c.les_yesno = true;
+            val = (val == "YES" || val == "1") ? "1" : "0";
+        }
+        bool ok = true;
+        auto F = [&](float& dst) { ok = sscanf(val.c_str(), "%f", &dst) == 1; };
+        auto I = [&](int& dst) { ok = sscanf(val.c_str(), "%d", &dst) == 1; };
+        if (key == "Base domain size") { int d[3]; ok = parse_xyz_int(val, d); c.nx = d[0]; c.ny = d[1]; c.nz = d[2]; have_dims = ok; }
+        else if (key == "Base blocksize") ok = parse_xyz_int(val, c.bs);
+        else if (key == "Obst1 location") ok = parse_tuple(val, c.ob1);
+        else if (key == "Obst1 radius") F(c.r1);
+        else if (key == "Obst2 location") ok = parse_tuple(val, c.ob2);
+        else if (key == "Obst2 radius") F(c.r2);
+        else if (key == "RE") F(c.re);
+        else if (key == "UMAX") F(c.umax);
+        else if (key == "omega") F(c.omega_rec);
+        else if (key == "DPDY") { F(c.dpdy); c.has_dpdy = true; }
+        else if (key == "TMAX") I(c.tmax);
+        else if (key == "STARTF") I(c.startf);
+        else if (key == "START_VELAV") I(c.start_av);
+        else if (key == "START_VELFLUC") I(c.start_fluc);
+        else if (key == "REFINEMENT") I(c.refinement);
+        else if (key == "MODEL") c.model = val;
+        else if (key == "Smagorinsky LES") I(c.les);
+        else if (key == "CS") F(c.cs);
+        else if (key == "LR domain size") { int d[3]; ok = parse_xyz_int(val, d); c.lrx = d[0]; c.lry = d[1]; c.lrz = d[2]; }
+        else if (key == "LR factor") F(c.lrfactor);
+        else if (key == "LR location") { float d[3]; ok = parse_xyz_float_x(val, d); c.lrx0 = d[0]; c.lry0 = d[1]; c.lrz0 = d[2]; }
+        else if (key == "LR blocksize") ok = parse_xyz_int(val, c.lbs);
+        else if (key == "omega in LR") F(c.omega_lr_rec);
+        else if (key == "GPUs per node") I(c.gpus);
+        else if (key == "Smagorinski LES") I(c.les);
+        else if (key == "KP") F(c.kp);
+        /* extension keys */
+        else if (key == "GEOMETRY") c.geometry = val;
+        else if (key == "PRECISION") c.precision = val;
+        else if (key == "TAU") F(c.tau);
+        else if (key == "LID velocity") { ok = parse_tuple(val, c.lid_u); c.lid_u_set = true; }
+        else if (key == "LID face") {
+            static const char* faces[6] = {"-x", "+x", "-y", "+y", "-z", "+z"};
+            ok = false;
+            for (int i = 0; i < 6; ++i) if (val == faces[i]) { c.lid_face = i; ok = true; }
+        }
+        else if (key == "Inlet noise") F(c.noise);
+        else if (key == "Seed") { unsigned long s = 0; ok = sscanf(val.c_str(), "%lu", &s) == 1; c.seed = uint32_t(s); }
+        else if (key == "VELAV") I(c.velav);
+        else if (key == "Init") I(c.init);
+        else if (key == "Init velocity") F(c.init_u);
+        else if (key == "ORDER") I(c.order);
+        else if (key == "FC top zflip") I(c.fc_zflip);
+        else return fail(LBM_ERR_PARSE, ".inputs line %d: unknown key '%s'", lineno, key.c_str());
+        if (!ok) return fail(LBM_ERR_PARSE, ".inputs line %d: cannot read value '%s' of '%s'", lineno, val.c_str(), key.c_str());
+        c.layout.push_back({line.substr(0, tab), sep, key});
+    }
+    if (!have_dims) return fail(LBM_ERR_PARSE, ".inputs record has no 'Base domain size' line");
+    if (c.nx < 3 || c.ny < 3 || c.nz < 1) return fail(LBM_ERR_CONFIG, "domain %dx%dx%d is too small", c.nx, c.ny, c.nz);
+    return LBM_OK;
+}
+
+int model_id(const std::string& m) {
+    if (m == "MRT") return MRT;
+    if (m == "MRT_DI3") return MRT_DI3;
+    if (m == "BGK") return BGK;
+    if (m == "MRT_CPU3D") return MRT_CPU3D;
+    return -1;
+}
+
+int storage_id(const std::string& p) {
+    if (p == "fp32") return STORE_F32;
+    if (p == "fp16") return STORE_F16;
+    if (p == "bf16") return STORE_BF16;
+    if (p == "fp64") return STORE_F64;
+    return -1;
+}
+
+size_t storage_bytes(int s) { return s == STORE_F64 ? 8 : (s == STORE_F32 ? 4 : 2); }
+
+/* relaxation rates, LR7:2607-2619 */
+void relaxation(const Config& c, float& omega, float& omegaLR, float& sf_cf, float& sf_fc) {
+    if (c.tau > 0.f) omega = 1.0f / c.tau;
+    else {
+        float CharLength = c.r1 * 2.f;
+        omega = 1.0f / (3.0f * (c.umax * CharLength / c.re) + 0.5f);
+    }
+    omegaLR = 2.0f / (1.0f + 2.0f * (2.0f / omega - 1.0f));
+    if (c.lrfactor == 0.25f) omegaLR = 2.0f / (1.0f + 2.0f * (2.0f / omegaLR - 1.0f));
+    if (c.lrfactor == 0.125f) {
+        omegaLR = 2.0f / (1.0f + 2.0f * (2.0f / omegaLR - 1.0f));
+        omegaLR = 2.0f / (1.0f + 2.0f * (2.0f / omegaLR - 1.0f));
+    }
+    sf_cf = omega * (1.0f - omegaLR) / ((1.0f - omega) * omegaLR / c.lrfactor);
+    sf_fc = 1.f / sf_cf;
+}
+
+/* the record, in WriteInputs' order and format (LR7:2547-2573); extension
+ * keys follow only when they differ from their defaults */
+std::string value_of(const Config& c, const std::string& key, float omega, float omegaLR) {
+    std::ostringstream o;
+    static const char* faces[6] = {"-x", "+x", "-y", "+y", "-z", "+z"};
+    if (key == "Base domain size") o << c.nx << "x" << c.ny << "x" << c.nz;
+    else if (key == "Base blocksize") o << c.bs[0] << "x" << c.bs[1] << "x" << c.bs[2];
+    else if (key == "Obst1 location") o << "(" << c.ob1[0] << "," << c.ob1[1] << "," << c.ob1[2] << ")";
+    else if (key == "Obst1 radius") o << c.r1;
+    else if (key == "Obst2 location") o << "(" << c.ob2[0] << "," << c.ob2[1] << "," << c.ob2[2] << ")";
+    else if (key == "Obst2 radius") o << c.r2;
+    else if (key == "RE") o << c.re;
+    else if (key == "UMAX") o << c.umax;
+    else if (key == "omega") o << omega;
+    else if (key == "DPDY") o << c.dpdy;
+    else if (key == "TMAX") o << c.tmax;
+    else if (key == "STARTF") o << c.startf;
+    else if (key == "START_VELAV") o << c.start_av;
+    else if (key == "START_VELFLUC") o << c.start_fluc;
+    else if (key == "REFINEMENT") o << c.refinement;
+    else if (key == "MODEL") o << c.model;
+    else if (key == "Smagorinsky LES") o << c.les;
+    else if (key == "Smagorinski LES") o << (c.les ? "YES" : "NO");
+    else if (key == "CS") o << c.cs;
+    else if (key == "KP") o << c.kp;
+    else if (key == "LR domain size") o << c.lrx << "x" << c.lry << "x" << c.lrz;
+    else if (key == "LR factor") o << c.lrfactor;
+    else if (key == "LR location") o << c.lrx0 << "x" << c.lry0 << "x" << c.lrz0;
+    else if (key == "LR blocksize") o << c.lbs[0] << "x" << c.lbs[1] << "x" << c.lbs[2];
+    else if (key == "omega in LR") o << omegaLR;
+    else if (key == "GPUs per node") o << c.gpus;
+    else if (key == "GEOMETRY") o << c.geometry;
+    else if (key == "PRECISION") o << c.precision;
+    else if (key == "TAU") o << c.tau;
+    else if (key == "LID velocity") o << "(" << c.lid_u[0] << "," << c.lid_u[1] << "," << c.lid_u[2] << ")";
+    else if (key == "LID face") o << faces[c.lid_face];
+    else if (key == "Inlet noise") o << c.noise;
+    else if (key == "Seed") o << c.seed;
+    else if (key == "VELAV") o << c.velav;
+    else if (key == "Init") o << c.init;
+    else if (key == "Init velocity") o << c.init_u;
+    else if (key == "ORDER") o << c.order;
+    else if (key == "FC top zflip") o << c.fc_zflip;
+    return o.str();
+}
+
+/* The run record.  A parsed record is written back line by line with its own
+ * labels (values from the configuration, the omega lines recomputed); a new
+ * one follows WriteInputs (LR7:2547-2573), extension keys after it when they
+ * differ from their defaults. */
+std::string write_inputs(const Config& c, float omega, float omegaLR) {
+    std::ostringstream o;
+    if (!c.layout.empty()) {
+        for (const auto& l : c.layout) o << l.label << "\t" << l.sep << value_of(c, l.key, omega, omegaLR) << std::endl;
+        return o.str();
+    }
+    auto line = [&](const char* label, const char* key, const char* sep = "") {
+        o << label << "\t" << sep << value_of(c, key, omega, omegaLR) << std::endl;
+    };
+    line("Base domain size ", "Base domain size");
+    line("Base blocksize: ", "Base blocksize");
+    line("Obst1 location: ", "Obst1 location");
+    line("Obst1 radius: ", "Obst1 radius");
+    line("Obst2 location: ", "Obst2 location");
+    line("Obst2 radius: ", "Obst2 radius");
+    line("RE: ", "RE");
+    line("UMAX: ", "UMAX");
+    line("omega ", "omega", ": ");
+    if (c.has_dpdy) line("DPDY ", "DPDY", ": ");
+    line("TMAX: ", "TMAX");
+    line("STARTF: ", "STARTF");
+    line("START_VELAV: ", "START_VELAV");
+    line("START_VELFLUC: ", "START_VELFLUC");
+    line("REFINEMENT: ", "REFINEMENT");
+    line("MODEL: ", "MODEL");
+    line("Smagorinsky LES: ", "Smagorinsky LES");
+    line("CS: ", "CS");
+    line("LR domain size ", "LR domain size");
+    line("LR factor ", "LR factor");
+    line("LR location ", "LR location");
+    line("LR blocksize: ", "LR blocksize");
+    line("omega in LR ", "omega in LR", ": ");
+    line("GPUs per node ", "GPUs per node", ": ");
+    Config d;
+    if (c.geometry != d.geometry) line("GEOMETRY: ", "GEOMETRY");
+    if (c.precision != d.precision) line("PRECISION: ", "PRECISION");
+    if (c.tau > 0.f) line("TAU: ", "TAU");
+    if (c.lid_u_set) line("LID velocity: ", "LID velocity");
+    if (c.lid_face != d.lid_face) line("LID face: ", "LID face");
+    if (c.noise != 0.f) line("Inlet noise: ", "Inlet noise");
+    if (c.seed != d.seed) line("Seed: ", "Seed");
+    if (c.velav) line("VELAV: ", "VELAV");
+    if (c.init >= 0) line("Init: ", "Init");
+    if (c.init_u > -1e29f) line("Init velocity: ", "Init velocity");
+    if (c.order != d.order) line("ORDER: ", "ORDER");
+    if (c.fc_zflip != d.fc_zflip) line("FC top zflip: ", "FC top zflip");
+    return o.str();
+}
+
+/* ------------------------------------------------------------------------ */
+/* geometry: ImageFcn / ImageFcnLR                                            */
+/* ------------------------------------------------------------------------ */
+
+int body_shape(const std::string& g) {
+    if (g == "channel_square") return 1;
+    if (g == "channel_circle") return 2;
+    return 0;
+}
+
+/* channel programs (LR7:88-127): body, then walls y = 0 / ny-1, inlet x = 0,
+ * outlet x = nx-1 (walls override inlet/outlet, both override the body) */
+void mask_base(const Config& c, std::vector<uint8_t>& m) {
+    const int nx = c.nx, ny = c.ny, nz = c.nz;
+    m.assign(size_t(nx) * ny * nz, FLUID);
+    const int shape = body_shape(c.geometry);
+    const bool channel = c.geometry.rfind("channel", 0) == 0;
+    const bool cavity = c.geometry == "cavity";
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                uint8_t v = FLUID;
+                if (shape == 1) {
+                    if (std::fabs(float(x) - c.ob1[0]) < c.r1 && std::fabs(float(y) - c.ob1[1]) < c.r1) v = BODY;
+                } else if (shape == 2) {
+                    float dx = float(x) - c.ob1[0], dy = float(y) - c.ob1[1];
+                    if (dx * dx + dy * dy < c.r1 * c.r1) v = BODY;
+                }
+                if (channel) {
+                    if (y == 0 || y == ny - 1) v = WALL;
+                    else if (x == 0) v = WEST_INLET;
+                    else if (x == nx - 1) v = EAST_OUTLET;
+                } else if (cavity) {
+                    int p[3] = {x, y, z}, n[3] = {nx, ny, nz};
+                    int a = c.lid_face / 2;
+                    bool on_lid = (c.lid_face % 2 == 0) ? p[a] == 0 : p[a] == n[a] - 1;
+                    if (on_lid) v = LID;
+                    else if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || z == 0 || z == nz - 1) v = WALL;
+                }
+                m[(size_t(z) * ny + y) * nx + x] = v;
+            }
+}
+
+/* ImageFcnLR (LR7:68-86) at fine-node coordinates */
+void mask_fine(const Config& c, std::vector<uint8_t>& m) {
+    const int nx = c.lrx, ny = c.lry, nz = c.lrz;
+    m.assign(size_t(nx) * ny * nz, FLUID);
+    const int shape = body_shape(c.geometry);
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                float xc = c.lrx0 + float(x) * c.lrfactor, yc = c.lry0 + float(y) * c.lrfactor;
+                uint8_t v = FLUID;
+                if (shape == 1) {
+                    if (std::fabs(xc - c.ob1[0]) < c.r1 && std::fabs(yc - c.ob1[1]) < c.r1) v = BODY;
+                } else if (shape == 2) {
+                    float dx = xc - c.ob1[0], dy = yc - c.ob1[1];
+                    if (dx * dx + dy * dy < c.r1 * c.r1) v = BODY;
+                }
+                m[(size_t(z) * ny + y) * nx + x] = v;
+            }
+}
+
+/* ------------------------------------------------------------------------ */
+/* handle                                                                     */
+/* ------------------------------------------------------------------------ */
+
+struct LevelState {
+    Level L{};
+    void* f[2] = {nullptr, nullptr};
+    int cur = 0;
+    uint8_t* mask = nullptr;        /* device, pitched */
+    std::vector<uint8_t> hmask;     /* host, compact */
+    float* stats = nullptr;         /* device, 4 x qstride */
+    double* fpart = nullptr;        /* per-block force partials */
+    int nblocks = 0;
+};
+
+}  // namespace
+
+struct lbm_handle {
+    Config cfg;
+    int storage = STORE_F32;
+    int model = MRT;
+    cudaStream_t stream = nullptr;
+    LevelState lv[2];
+    int nlevels = 1;
+    float omega = 0, omegaLR = 0, sf_cf = 0, sf_fc = 0;
+    int t = 0;
+    double* force_hist = nullptr;   /* device, 3 doubles per recorded step */
+    int force_cap = 0;
+    float* mom = nullptr;           /* coarse moment export, [9][nz][eny][enx] */
+    int enx = 0, eny = 0;
+    double* audit_part = nullptr;
+    double* audit_out = nullptr;
+    RefineParams rp{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+void free_level(LevelState& s) {
+    cudaFree(s.f[0]);
+    cudaFree(s.f[1]);
+    cudaFree(s.mask);
+    cudaFree(s.stats);
+    cudaFree(s.fpart);
+    s = LevelState();
+}
+
+int alloc_level(LevelState& s, int nx, int ny, int nz, int storage, bool stats) {
+    Level& L = s.L;
+    L.nx = nx;
+    L.ny = ny;
+    L.nz = nz;
+    L.pitch = (nx + 31) / 32 * 32;
+    L.plane = (long long)L.pitch * ny;
+    L.qstride = L.plane * nz;
+    L.storage = storage;
+    if (L.qstride * 19 > (1LL << 40)) return fail(LBM_ERR_CONFIG, "level %dx%dx%d too large", nx, ny, nz);
+    const size_t bytes = size_t(L.qstride) * 19 * storage_bytes(storage);
+    for (int i = 0; i < 2; ++i) {
+        CUDA_TRY(cudaMalloc(&s.f[i], bytes));
+        CUDA_TRY(cudaMemset(s.f[i], 0, bytes));
+    }
+    CUDA_TRY(cudaMalloc(&s.mask, size_t(L.qstride)));
+    CUDA_TRY(cudaMemset(s.mask, WALL, size_t(L.qstride)));
+    if (stats) {
+        CUDA_TRY(cudaMalloc(&s.stats, size_t(L.qstride) * 4 * sizeof(float)));
+        CUDA_TRY(cudaMemset(s.stats, 0, size_t(L.qstride) * 4 * sizeof(float)));
+    }
+    s.nblocks = sc_blocks(L);
+    CUDA_TRY(cudaMalloc(&s.fpart, size_t(s.nblocks) * 3 * sizeof(double)));
+    return LBM_OK;
+}
+
+int upload_mask(lbm_handle* h, int level) {
+    LevelState& s = h->lv[level];
+    const Level& L = s.L;
+    std::vector<uint8_t> pitched(size_t(L.qstride), WALL);
+    for (int z = 0; z < L.nz; ++z)
+        for (int y = 0; y < L.ny; ++y)
+            memcpy(&pitched[size_t(z) * L.plane + size_t(y) * L.pitch], &s.hmask[(size_t(z) * L.ny + y) * L.nx], L.nx);
+    CUDA_TRY(cudaMemcpyAsync(s.mask, pitched.data(), pitched.size(), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return LBM_OK;
+}
+
+int ensure_force_cap(lbm_handle* h, int n) {
+    if (n <= h->force_cap) return LBM_OK;
+    int cap = std::max(n, std::max(2 * h->force_cap, 1024));
+    double* nh = nullptr;
+    CUDA_TRY(cudaMalloc(&nh, size_t(cap) * 3 * sizeof(double)));
+    CUDA_TRY(cudaMemsetAsync(nh, 0, size_t(cap) * 3 * sizeof(double), h->stream));
+    if (h->force_hist) {
+        CUDA_TRY(cudaMemcpyAsync(nh, h->force_hist, size_t(h->force_cap) * 3 * sizeof(double), cudaMemcpyDeviceToDevice,
+                                 h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        cudaFree(h->force_hist);
+    }
+    h->force_hist = nh;
+    h->force_cap = cap;
+    return LBM_OK;
+}
+
+StepParams base_params(const lbm_handle* h, int level) {
+    const Config& c = h->cfg;
+    StepParams p{};
+    p.model = h->model;
+    p.les = c.les;
+    p.omega = level == 0 ? h->omega : h->omegaLR;
+    p.cs = c.cs;
+    p.dpdy = c.dpdy;
+    p.u_in = c.umax;          /* PoisProf3D returns UMAX (LR7:135-143) */
+    p.rho_out = 1.0f;
+    const bool lid_default = !c.lid_u_set;
+    p.lid_u[0] = lid_default ? c.umax : c.lid_u[0];
+    p.lid_u[1] = lid_default ? 0.f : c.lid_u[1];
+    p.lid_u[2] = lid_default ? 0.f : c.lid_u[2];
+    p.lid_face = c.lid_face;
+    p.stats_on = c.velav;
+    p.start_av = c.start_av;
+    p.start_fluc = c.start_fluc;
+    p.stats_weight = level == 0 ? 1.f : c.lrfactor;
+    p.noise_amp = level == 0 ? c.noise : 0.f;
+    p.noise_seed = c.seed;
+    return p;
+}
+
+int do_init(lbm_handle* h) {
+    const Config& c = h->cfg;
+    int kind = c.init >= 0 ? c.init : (h->model == BGK ? 1 : 0);
+    float u0 = c.init_u > -1e29f ? c.init_u : (c.geometry == "cavity" || c.geometry == "periodic" ? 0.f : c.umax);
+    for (int l = 0; l < h->nlevels; ++l) {
+        LevelState& s = h->lv[l];
+        for (int i = 0; i < 2; ++i) CUDA_TRY(launch_init(s.L, s.mask, s.f[i], kind, u0, h->stream));
+        s.cur = 0;
+        if (s.stats) CUDA_TRY(cudaMemsetAsync(s.stats, 0, size_t(s.L.qstride) * 4 * sizeof(float), h->stream));
+    }
+    if (h->force_hist) CUDA_TRY(cudaMemsetAsync(h->force_hist, 0, size_t(h->force_cap) * 3 * sizeof(double), h->stream));
+    h->t = 0;
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return LBM_OK;
+}
+
+/* one base step and, with refinement, the patch sub-steps and the two
+ * interpolations; the order of LR7:2849-2950 */
+int one_step(lbm_handle* h) {
+    const Config& c = h->cfg;
+    const int t = h->t;
+    LevelState& C = h->lv[0];
+    StepParams p = base_params(h, 0);
+    p.t = t;
+    p.force_on = (!c.refinement && t > c.startf) ? 1 : 0;
+    if (c.refinement) {
+        p.exp_x0 = int(c.lrx0);
+        p.exp_y0 = int(c.lry0);
+        p.exp_nx = h->enx;
+        p.exp_ny = h->eny;
+    }
+    const int fidx = t - c.startf;
+    if (p.force_on) {
+        int rc = ensure_force_cap(h, fidx + 1);
+        if (rc) return rc;
+    }
+    CUDA_TRY(launch_stream_collide(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.fpart, C.stats, h->mom, h->stream));
+    if (p.force_on) CUDA_TRY(launch_reduce_force(C.fpart, C.nblocks, h->force_hist + 3LL * fidx, h->stream));
+    C.cur = 1 - C.cur;
+    if (c.refinement) {
+        LevelState& Fn = h->lv[1];
+        const int L = int(std::lround(1.0 / c.lrfactor));
+        for (int i = 0; i < L; ++i) {
+            StepParams pf = base_params(h, 1);
+            pf.t = t;
+            pf.force_on = (t > c.startf && i == 0) ? 1 : 0;
+            if (pf.force_on) {
+                int rc = ensure_force_cap(h, fidx + 1);
+                if (rc) return rc;
+            }
+            CUDA_TRY(launch_stream_collide(Fn.L, pf, Fn.f[Fn.cur], Fn.f[1 - Fn.cur], Fn.mask, Fn.fpart, Fn.stats,
+                                           nullptr, h->stream));
+            if (pf.force_on) CUDA_TRY(launch_reduce_force(Fn.fpart, Fn.nblocks, h->force_hist + 3LL * fidx, h->stream));
+            Fn.cur = 1 - Fn.cur;
+        }
+        CUDA_TRY(launch_interp_cf(h->rp, Fn.L, h->mom, Fn.f[Fn.cur], Fn.mask, h->stream));
+        CUDA_TRY(launch_interp_fc(h->rp, C.L, Fn.L, Fn.f[Fn.cur], C.f[C.cur], C.mask, h->stream));
+    }
+    h->t = t + 1;
+    return LBM_OK;
+}
+
+int check_level(const lbm_handle* h, int level) {
+    if (!h) return fail(LBM_ERR_ARG, "null handle");
+    if (level < 0 || level >= h->nlevels) return fail(LBM_ERR_ARG, "level %d does not exist", level);
+    return LBM_OK;
+}
+
+}  // namespace
+
+/* ------------------------------------------------------------------------ */
+/* C ABI                                                                       */
+/* ------------------------------------------------------------------------ */
+
+extern "C" {
+
+const char* lbm_last_error(void) { return g_err.c_str(); }
+const char* lbm_version(void) { return "lbm_gb300 0.1 (sm_103a)"; }
+
+int lbm_inputs_normalize(const char* inputs_text, char* buf, size_t cap, size_t* len) {
+    Config c;
+    if (int rc = parse_inputs(inputs_text, c)) return rc;
+    float om, omlr, a, b;
+    relaxation(c, om, omlr, a, b);
+    std::string s = write_inputs(c, om, omlr);
+    if (len) *len = s.size();
+    if (buf && cap > 0) {
+        size_t k = std::min(cap - 1, s.size());
+        memcpy(buf, s.data(), k);
+        buf[k] = 0;
+        if (k < s.size()) return fail(LBM_ERR_ARG, "buffer of %zu bytes too small for %zu", cap, s.size() + 1);
+    }
+    return LBM_OK;
+}
+
+int lbm_inputs_mask(const char* inputs_text, int level, uint8_t* mask, size_t cap, size_t* n) {
+    Config c;
+    if (int rc = parse_inputs(inputs_text, c)) return rc;
+    if (level < 0 || level > 1 || (level == 1 && !c.refinement)) return fail(LBM_ERR_ARG, "level %d does not exist", level);
+    std::vector<uint8_t> m;
+    if (level == 0) mask_base(c, m);
+    else mask_fine(c, m);
+    if (n) *n = m.size();
+    if (mask) {
+        if (cap < m.size()) return fail(LBM_ERR_ARG, "mask buffer of %zu bytes too small for %zu", cap, m.size());
+        memcpy(mask, m.data(), m.size());
+    }
+    return LBM_OK;
+}
+
+static void write_level(std::ostream& out, std::ostream* slice, const Config& c, int level, const std::vector<float>& f,
+                        const std::vector<float>& st, int nx, int ny, int nz);
+
+static int copy_out(const std::string& s, char* buf, size_t cap, size_t* len) {
+    if (len) *len = s.size();
+    if (buf && cap > 0) {
+        size_t k = std::min(cap - 1, s.size());
+        memcpy(buf, s.data(), k);
+        buf[k] = 0;
+        if (k < s.size()) return fail(LBM_ERR_ARG, "buffer of %zu bytes too small for %zu", cap, s.size() + 1);
+    }
+    return LBM_OK;
+}
+
+int lbm_format_tecplot(const char* inputs_text, int level, const float* f, const float* stats4, char* buf, size_t cap,
+                       size_t* len, char* slice, size_t slice_cap, size_t* slice_len) {
+    Config c;
+    if (int rc = parse_inputs(inputs_text, c)) return rc;
+    if (!f) return fail(LBM_ERR_ARG, "f is null");
+    if (level < 0 || level > 1 || (level == 1 && !c.refinement)) return fail(LBM_ERR_ARG, "level %d does not exist", level);
+    const int nx = level ? c.lrx : c.nx, ny = level ? c.lry : c.ny, nz = level ? c.lrz : c.nz;
+    const size_t N = size_t(nx) * ny * nz;
+    std::vector<float> fv(f, f + 19 * N), st;
+    if (stats4) st.assign(stats4, stats4 + 4 * N);
+    std::ostringstream zone, sl;
+    write_level(zone, &sl, c, level, fv, st, nx, ny, nz);
+    if (int rc = copy_out(zone.str(), buf, cap, len)) return rc;
+    return copy_out(sl.str(), slice, slice_cap, slice_len);
+}
+
+int lbm_create(const char* inputs_text, lbm_handle** out) {
+    if (!out) return fail(LBM_ERR_ARG, "out is null");
+    *out = nullptr;
+    Config c;
+    int rc = parse_inputs(inputs_text, c);
+    if (rc) return rc;
+    const int model = model_id(c.model);
+    if (model < 0) return fail(LBM_ERR_CONFIG, "MODEL '%s' is not one of MRT, MRT_DI3, BGK, MRT_CPU3D", c.model.c_str());
+    const int storage = storage_id(c.precision);
+    if (storage < 0) return fail(LBM_ERR_CONFIG, "PRECISION '%s' is not one of fp32, fp16, bf16, fp64", c.precision.c_str());
+    static const char* geoms[] = {"channel_square", "channel_circle", "channel", "cavity", "periodic"};
+    if (std::find(std::begin(geoms), std::end(geoms), c.geometry) == std::end(geoms))
+        return fail(LBM_ERR_CONFIG, "GEOMETRY '%s' is not supported", c.geometry.c_str());
+    if (c.refinement) {
+        /* LR7:2624-2627 */
+        const int lev = int(std::lround(1.0 / c.lrfactor));
+        if (std::fabs(c.lrfactor - 1.f / lev) > 0.001f || lev < 2)
+            return fail(LBM_ERR_CONFIG, "LR factor %g is not 1/LRLEVEL", c.lrfactor);
+        if (c.lrz != lev * c.nz)
+            return fail(LBM_ERR_CONFIG, "the refinement patch must span the periodic z extent: LR nz %d != %d * %d", c.lrz,
+                        lev, c.nz);
+        if (std::fabs((c.lrx0 - std::floor(c.lrx0)) - 0.5f * c.lrfactor) > 1e-6f ||
+            std::fabs((c.lry0 - std::floor(c.lry0)) - 0.5f * c.lrfactor) > 1e-6f ||
+            std::fabs(c.lrz0 + (1.f - 0.5f * c.lrfactor)) > 1e-6f)
+            return fail(LBM_ERR_CONFIG, "LR location must sit at half a fine spacing past a coarse node (z at %g)",
+                        -(1.f - 0.5f * c.lrfactor));
+        const int ex = int(c.lrx * c.lrfactor) + 1, ey = int(c.lry * c.lrfactor) + 1;
+        if (int(c.lrx0) < 0 || int(c.lry0) < 0 || int(c.lrx0) + ex > c.nx || int(c.lry0) + ey > c.ny)
+            return fail(LBM_ERR_CONFIG, "refinement patch does not fit in the base grid");
+        if (c.lrx < 2 * lev + 2 || c.lry < 2 * lev + 2) return fail(LBM_ERR_CONFIG, "refinement patch too small");
+    }
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    lbm_handle* h = new lbm_handle();
+    h->cfg = c;
+    h->model = model;
+    h->storage = storage;
+    relaxation(c, h->omega, h->omegaLR, h->sf_cf, h->sf_fc);
+    h->nlevels = c.refinement ? 2 : 1;
+    auto bail = [&](int code) {
+        lbm_destroy(h);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(LBM_ERR_CUDA, "cannot create a CUDA stream"));
+    cudaEventCreate(&h->ev0);
+    cudaEventCreate(&h->ev1);
+    if ((rc = alloc_level(h->lv[0], c.nx, c.ny, c.nz, storage, c.velav != 0))) return bail(rc);
+    mask_base(c, h->lv[0].hmask);
+    if ((rc = upload_mask(h, 0))) return bail(rc);
+    if (c.refinement) {
+        if ((rc = alloc_level(h->lv[1], c.lrx, c.lry, c.lrz, storage, c.velav != 0))) return bail(rc);
+        mask_fine(c, h->lv[1].hmask);
+        if ((rc = upload_mask(h, 1))) return bail(rc);
+        h->enx = int(c.lrx * c.lrfactor) + 1;
+        h->eny = int(c.lry * c.lrfactor) + 1;
+        if (cudaMalloc(&h->mom, size_t(9) * h->enx * h->eny * c.nz * sizeof(float)) != cudaSuccess)
+            return bail(fail(LBM_ERR_NOMEM, "cannot allocate the moment export"));
+        cudaMemset(h->mom, 0, size_t(9) * h->enx * h->eny * c.nz * sizeof(float));
+        RefineParams& r = h->rp;
+        r.cnx = c.nx; r.cny = c.ny; r.cnz = c.nz;
+        r.fnx = c.lrx; r.fny = c.lry; r.fnz = c.lrz;
+        r.lrx0 = c.lrx0; r.lry0 = c.lry0; r.lrz0 = c.lrz0;
+        r.lrfactor = c.lrfactor;
+        r.lrlevel = int(std::lround(1.0 / c.lrfactor));
+        r.order = c.order;
+        r.cs = c.cs;
+        r.omega_c = h->omega;
+        r.omega_f = h->omegaLR;
+        r.quirk_fc_top_zflip = c.fc_zflip;
+        r.enx = h->enx;
+        r.eny = h->eny;
+    }
+    if (cudaMalloc(&h->audit_part, size_t(audit_partials(h->lv[0].L)) * 4 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&h->audit_out, 4 * sizeof(double)) != cudaSuccess)
+        return bail(fail(LBM_ERR_NOMEM, "cannot allocate audit scratch"));
+    if ((rc = ensure_force_cap(h, std::max(1, c.tmax - c.startf)))) return bail(rc);
+    if ((rc = do_init(h))) return bail(rc);
+    *out = h;
+    return LBM_OK;
+}
+
+int lbm_destroy(lbm_handle* h) {
+    if (!h) return LBM_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (auto& s : h->lv) free_level(s);
+    cudaFree(h->force_hist);
+    cudaFree(h->mom);
+    cudaFree(h->audit_part);
+    cudaFree(h->audit_out);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return LBM_OK;
+}
+
+int lbm_get_dims(const lbm_handle* h, int level, int* nx, int* ny, int* nz) {
+    if (int rc = check_level(h, level)) return rc;
+    const Level& L = h->lv[level].L;
+    if (nx) *nx = L.nx;
+    if (ny) *ny = L.ny;
+    if (nz) *nz = L.nz;
+    return LBM_OK;
+}
+
+int lbm_get_nlevels(const lbm_handle* h, int* n) {
+    if (!h || !n) return fail(LBM_ERR_ARG, "null argument");
+    *n = h->nlevels;
+    return LBM_OK;
+}
+
+int lbm_get_params(const lbm_handle* h, float* o) {
+    if (!h || !o) return fail(LBM_ERR_ARG, "null argument");
+    o[0] = h->omega;
+    o[1] = h->omegaLR;
+    o[2] = h->sf_cf;
+    o[3] = h->sf_fc;
+    return LBM_OK;
+}
+
+int lbm_get_time(const lbm_handle* h, int* t) {
+    if (!h || !t) return fail(LBM_ERR_ARG, "null argument");
+    *t = h->t;
+    return LBM_OK;
+}
+
+int lbm_get_mask(const lbm_handle* h, int level, uint8_t* mask) {
+    if (int rc = check_level(h, level)) return rc;
+    if (!mask) return fail(LBM_ERR_ARG, "mask is null");
+    memcpy(mask, h->lv[level].hmask.data(), h->lv[level].hmask.size());
+    return LBM_OK;
+}
+
+int lbm_set_mask(lbm_handle* h, int level, const uint8_t* mask) {
+    if (int rc = check_level(h, level)) return rc;
+    if (!mask) return fail(LBM_ERR_ARG, "mask is null");
+    for (size_t i = 0; i < h->lv[level].hmask.size(); ++i)
+        if (mask[i] > LID) return fail(LBM_ERR_ARG, "mask value %d at %zu is not a node type", int(mask[i]), i);
+    memcpy(h->lv[level].hmask.data(), mask, h->lv[level].hmask.size());
+    return upload_mask(h, level);
+}
+
+int lbm_init_equilibrium(lbm_handle* h) {
+    if (!h) return fail(LBM_ERR_ARG, "null handle");
+    return do_init(h);
+}
+
+int lbm_get_populations(lbm_handle* h, int level, float* f) {
+    if (int rc = check_level(h, level)) return rc;
+    if (!f) return fail(LBM_ERR_ARG, "f is null");
+    LevelState& s = h->lv[level];
+    const size_t n = size_t(s.L.nx) * s.L.ny * s.L.nz * 19;
+    float* d = nullptr;
+    CUDA_TRY(cudaMallocAsync((void**)&d, n * sizeof(float), h->stream));
+    cudaError_t e = launch_pack(s.L, s.f[s.cur], d, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(f, d, n * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+    cudaFreeAsync(d, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "get_populations: %s", cudaGetErrorString(e));
+    return LBM_OK;
+}
+
+int lbm_set_populations(lbm_handle* h, int level, const float* f) {
+    if (int rc = check_level(h, level)) return rc;
+    if (!f) return fail(LBM_ERR_ARG, "f is null");
+    LevelState& s = h->lv[level];
+    const size_t n = size_t(s.L.nx) * s.L.ny * s.L.nz * 19;
+    float* d = nullptr;
+    CUDA_TRY(cudaMallocAsync((void**)&d, n * sizeof(float), h->stream));
+    cudaError_t e = cudaMemcpyAsync(d, f, n * sizeof(float), cudaMemcpyHostToDevice, h->stream);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = launch_unpack(s.L, d, s.f[i], h->stream);
+    cudaFreeAsync(d, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "set_populations: %s", cudaGetErrorString(e));
+    return LBM_OK;
+}
+
+int lbm_step(lbm_handle* h, int nsteps) {
+    if (!h) return fail(LBM_ERR_ARG, "null handle");
+    if (nsteps < 0) return fail(LBM_ERR_ARG, "nsteps %d < 0", nsteps);
+    for (int i = 0; i < nsteps; ++i)
+        if (int rc = one_step(h)) return rc;
+    return LBM_OK;
+}
+
+int lbm_step_timed(lbm_handle* h, int nsteps, float* ms) {
+    if (!h || !ms) return fail(LBM_ERR_ARG, "null argument");
+    CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+    if (int rc = lbm_step(h, nsteps)) return rc;
+    CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
+    CUDA_TRY(cudaEventSynchronize(h->ev1));
+    CUDA_TRY(cudaEventElapsedTime(ms, h->ev0, h->ev1));
+    return LBM_OK;
+}
+
+int lbm_synchronize(lbm_handle* h) {
+    if (!h) return fail(LBM_ERR_ARG, "null handle");
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return LBM_OK;
+}
+
+int lbm_get_fields(lbm_handle* h, int level, float* rho, float* u, float* v, float* w) {
+    if (int rc = check_level(h, level)) return rc;
+    LevelState& s = h->lv[level];
+    const size_t n = size_t(s.L.nx) * s.L.ny * s.L.nz;
+    float* d = nullptr;
+    CUDA_TRY(cudaMallocAsync((void**)&d, 4 * n * sizeof(float), h->stream));
+    cudaError_t e = launch_fields(s.L, s.f[s.cur], d, d + n, d + 2 * n, d + 3 * n, h->stream);
+    float* outs[4] = {rho, u, v, w};
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+        if (outs[i]) e = cudaMemcpyAsync(outs[i], d + i * n, n * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+    cudaFreeAsync(d, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "get_fields: %s", cudaGetErrorString(e));
+    return LBM_OK;
+}
+
+int lbm_get_stats(lbm_handle* h, int level, float* stats4) {
+    if (int rc = check_level(h, level)) return rc;
+    LevelState& s = h->lv[level];
+    if (!s.stats) return fail(LBM_ERR_STATE, "statistics are off (VELAV: 0)");
+    const Level& L = s.L;
+    const size_t n = size_t(L.nx) * L.ny * L.nz;
+    std::vector<float> tmp(size_t(L.qstride) * 4);
+    CUDA_TRY(cudaMemcpyAsync(tmp.data(), s.stats, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < 4; ++k)
+        for (int z = 0; z < L.nz; ++z)
+            for (int y = 0; y < L.ny; ++y)
+                memcpy(stats4 + k * n + (size_t(z) * L.ny + y) * L.nx,
+                       tmp.data() + k * L.qstride + size_t(z) * L.plane + size_t(y) * L.pitch, L.nx * sizeof(float));
+    return LBM_OK;
+}
+
+int lbm_get_forces(lbm_handle* h, double* fxyz, int max_steps, int* n) {
+    if (!h || !fxyz || max_steps < 0) return fail(LBM_ERR_ARG, "bad argument");
+    const int avail = std::max(0, std::min(h->t - h->cfg.startf, h->force_cap));
+    const int k = std::min(avail, max_steps);
+    if (k > 0) {
+        CUDA_TRY(cudaMemcpyAsync(fxyz, h->force_hist, size_t(k) * 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+    }
+    if (n) *n = k;
+    return LBM_OK;
+}
+
+int lbm_audit(lbm_handle* h, int level, double* out4) {
+    if (int rc = check_level(h, level)) return rc;
+    if (!out4) return fail(LBM_ERR_ARG, "out4 is null");
+    LevelState& s = h->lv[level];
+    CUDA_TRY(launch_audit(s.L, s.f[s.cur], s.mask, h->audit_part, audit_partials(s.L), h->audit_out, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(out4, h->audit_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return LBM_OK;
+}
+
+int lbm_write_inputs(const lbm_handle* h, char* buf, size_t cap, size_t* len) {
+    if (!h) return fail(LBM_ERR_ARG, "null handle");
+    std::string s = write_inputs(h->cfg, h->omega, h->omegaLR);
+    if (len) *len = s.size();
+    if (buf && cap > 0) {
+        size_t k = std::min(cap - 1, s.size());
+        memcpy(buf, s.data(), k);
+        buf[k] = 0;
+        if (k < s.size()) return fail(LBM_ERR_ARG, "buffer of %zu bytes too small for %zu", cap, s.size() + 1);
+    }
+    return LBM_OK;
+}
+
+/* tecplot POINT zones in WriteResults' layout (LR7:2350-2442, 2444-2535) */
+static void write_level(std::ostream& out, std::ostream* slice, const Config& c, int level, const std::vector<float>& f,
+                        const std::vector<float>& st, int nx, int ny, int nz) {
+    const size_t N = size_t(nx) * ny * nz;
+    out << "VARIABLES = \"X\",\"Y\",\"Z\",\"u\",\"v\",\"w\",\"rho\",\"velAv[0]\",\"velAv[1]\",\"ufluc\",\"vfluc\",\"Smag\"\n";
+    out << "ZONE F=POINT, I=" << nx << ", J=" << ny << ", K=" << nz << "\n";
+    if (slice) {
+        *slice << "VARIABLES = \"X\",\"Y\",\"Z\",\"u\",\"v\",\"w\",\"rho\",\"velAv[0]\",\"velAv[1]\",\"ufluc\",\"vfluc\",\"Smag\"\n";
+        *slice << "ZONE F=POINT, I=" << nx << ", J=" << ny << ", K=" << 1 << "\n";
+    }
+    const int slice_k = level == 0 ? 1 : 3;
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const size_t o = (size_t(k) * ny + j) * nx + i;
+                float g[19];
+                float rho = 0;
+                for (int l = 0; l < 19; ++l) {
+                    g[l] = f[l * N + o];
+                    rho += g[l];
+                }
+                float u = g[1] - g[3] + g[5] - g[6] - g[7] + g[8] + g[10] - g[12] + g[15] - g[17];
+                float v = g[2] - g[4] + g[5] + g[6] - g[7] - g[8] + g[11] - g[13] + g[16] - g[18];
+                float w = g[9] + g[10] + g[11] + g[12] + g[13] - g[14] - g[15] - g[16] - g[17] - g[18];
+                float smag = 0.f;
+                const bool interior = k > 0 && k < nz - 1;
+                if (interior) {
+                    /* strain magnitude from the non-equilibrium stress moments
+                     * (LR7:2386-2407; divided by LRFACTOR on the fine level) */
+                    float m9 = 2.f * g[1] + -g[2] + 2.f * g[3] + -g[4] + g[5] + g[6] + g[7] + g[8] + -g[9] + g[10] +
+                               -2.f * g[11] + g[12] + -2.f * g[13] + -g[14] + g[15] + -2.f * g[16] + g[17] + -2.f * g[18];
+                    float m11 = g[2] + g[4] + g[5] + g[6] + g[7] + g[8] + -g[9] + -g[10] + -g[12] + -g[14] + -g[15] + -g[17];
+                    float m13 = g[5] + -g[6] + g[7] + -g[8];
+                    float m14 = g[11] + -g[13] + -g[16] + g[18];
+                    float m15 = g[10] + -g[12] + -g[15] + g[17];
+                    m9 -= 2.f * u * u - (v * v + w * w);
+                    m11 -= v * v - w * w;
+                    m13 -= u * v;
+                    m14 -= v * w;
+                    m15 -= u * w;
+                    float P11 = -0.5f * (m9), P22 = -(-38.f * m9 - 3.0f * m11) / 76.f,
+                          P33 = -(-38.f * m9 + 3.0f * m11) / 76.f;
+                    float P12 = -1.5f * m13, P23 = -1.5f * m14, P13 = -1.5f * m15;
+                    smag = std::sqrt(2.f * (P11 * P11 + P22 * P22 + P33 * P33 + 2.f * P12 * P12 + 2.f * P23 * P23 +
+                                            2.f * P13 * P13));
+                    if (level == 1) smag /= c.lrfactor;
+                }
+                float s0 = st.empty() ? 0.f : st[o], s1 = st.empty() ? 0.f : st[N + o];
+                float s2 = st.empty() ? 0.f : st[2 * N + o], s3 = st.empty() ? 0.f : st[3 * N + o];
+                std::ostringstream line;
+                if (level == 0) line << i << ", " << j << ", " << k << ", ";
+                else
+                    line << (c.lrx0 + c.lrfactor * i) << ", " << (c.lry0 + c.lrfactor * j) << ", "
+                         << (c.lrz0 + c.lrfactor * k) << ", ";
+                line << u << "," << v << "," << w << "," << rho << "," << s0 << "," << s1 << ", " << s2 << "," << s3 << ",";
+                if (interior) line << smag;
+                else line << 0;
+                out << line.str() << std::endl;
+                if (slice && k == slice_k) *slice << line.str() << std::endl;
+            }
+}
+
+int lbm_write_outputs(lbm_handle* h, const char* casename) {
+    if (!h || !casename) return fail(LBM_ERR_ARG, "null argument");
+    const Config& c = h->cfg;
+    std::string base(casename);
+    std::ofstream dat(base + ".dat"), force(base + ".force"), inputs(base + ".inputs"), slice(base + "_slice.dat");
+    if (!dat || !force || !inputs || !slice) return fail(LBM_ERR_ARG, "cannot open output files for '%s'", casename);
+    inputs << write_inputs(c, h->omega, h->omegaLR);
+    for (int l = 0; l < h->nlevels; ++l) {
+        LevelState& s = h->lv[l];
+        const size_t N = size_t(s.L.nx) * s.L.ny * s.L.nz;
+        std::vector<float> f(N * 19), st;
+        if (int rc = lbm_get_populations(h, l, f.data())) return rc;
+        if (s.stats) {
+            st.resize(4 * N);
+            if (int rc = lbm_get_stats(h, l, st.data())) return rc;
+        }
+        /* WriteResults / WriteResultsLR append their slice to one file */
+        std::ofstream part(base + "_part" + std::to_string(l) + ".dat");
+        write_level(part, &slice, c, l, f, st, s.L.nx, s.L.ny, s.L.nz);
+        part << std::endl;
+    }
+    /* WriteForces (LR7:2537-2545): t, F/ref with ref = UMAX^2 ZDIM OBSTR1 (x LRLEVEL^2) */
+    const int nf = std::max(0, c.tmax - c.startf);
+    std::vector<double> F(size_t(std::max(nf, 1)) * 3, 0.0);
+    int got = 0;
+    if (int rc = lbm_get_forces(h, F.data(), nf, &got)) return rc;
+    float ref = c.umax * c.umax * c.nz * c.r1;
+    if (c.refinement) ref *= std::lround(1.0 / c.lrfactor) * std::lround(1.0 / c.lrfactor);
+    for (int i = 0; i < nf; ++i)
+        force << i + c.startf << ", " << float(F[3 * i]) / ref << ", " << float(F[3 * i + 1]) / ref << ", "
+              << float(F[3 * i + 2]) / ref << std::endl;
+    return LBM_OK;
+}
+
+/* ---- kernel-level API ---- */
+
+size_t lbm_force_scratch_doubles(int nx, int ny, int nz, int pitch) {
+    Level L{};
+    L.nx = nx;
+    L.ny = ny;
+    L.nz = nz;
+    L.pitch = pitch;
+    return size_t(sc_blocks(L)) * 3;
+}
+
+int lbm_stream_collide_f32(const float* fA, float* fB, const uint8_t* mask, int nx, int ny, int nz, int pitch, int model,
+                           int les, float omega, float cs, float u_in, float rho_out, int t, double* force_out,
+                           double* scratch, void* cuda_stream) {
+    if (!fA || !fB || !mask || fA == fB) return fail(LBM_ERR_ARG, "bad buffer pointers");
+    if (nx < 1 || ny < 1 || nz < 1 || pitch < nx || pitch % 32) return fail(LBM_ERR_ARG, "bad dimensions or pitch");
+    if (model < 0 || model > 3) return fail(LBM_ERR_ARG, "model %d unknown", model);
+    if (force_out && !scratch) return fail(LBM_ERR_ARG, "force_out needs scratch");
+    Level L{};
+    L.nx = nx;
+    L.ny = ny;
+    L.nz = nz;
+    L.pitch = pitch;
+    L.plane = (long long)pitch * ny;
+    L.qstride = L.plane * nz;
+    L.storage = STORE_F32;
+    StepParams p{};
+    p.model = model;
+    p.les = les;
+    p.omega = omega;
+    p.cs = cs;
+    p.u_in = u_in;
+    p.rho_out = rho_out;
+    p.t = t;
+    p.force_on = force_out ? 1 : 0;
+    p.stats_weight = 1.f;
+    cudaStream_t s = (cudaStream_t)cuda_stream;
+    CUDA_TRY(launch_stream_collide(L, p, fA, fB, mask, scratch, nullptr, nullptr, s));
+    if (force_out) CUDA_TRY(launch_reduce_force(scratch, sc_blocks(L), force_out, s));
+    return LBM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,614 @@
+/*
+ * lbm_kernels.cu -- CUDA kernels of the D3Q19 stream-collide path for sm_103a.
+ *
+ * k_stream_collide is the hot kernel: one thread per lattice node, a warp
+ * spans 32 consecutive x of one row, so every population load and store of a
+ * warp touches one 128-byte line (x-shifted pulls straddle two, the neighbour
+ * warp's line is then an L2 hit).  It fuses, per node and per step, what the
+ * reference spreads over update_inn/update_top/update_bot (LR7:1127-1628):
+ *   pull streaming (LR7:1445-1491) with the z halo planes replaced by a
+ *   periodic index wrap inside one domain,
+ *   full-way bounce-back + momentum exchange (LR7:1493-1526, 1607-1626),
+ *   inlet/outlet rebuilds (LR7:1531-1561), the moving lid,
+ *   MRT/BGK collision with Smagorinsky (LR7:583-711, DI3:599-832),
+ *   running statistics (LR7:1567-1584),
+ *   the coarse-moment export for the refinement (LR7:1590-1605).
+ * Forces are reduced per block in FP64 (warp shuffles, then shared memory)
+ * into a scratch array and summed by a second, deterministic kernel.
+ */
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "d3q19.cuh"
+#include "lbm_kernels.cuh"
+
+namespace lbm {
+
+/* ---- storage formats: FP32, FP16/BF16 offset (f - w) with FP32 math, FP64 ---- */
+template <class S> struct Fmt;
+template <> struct Fmt<float> {
+    using T = float;
+    static __device__ __forceinline__ float ld(const float* p, int) { return __ldg(p); }
+    static __device__ __forceinline__ void st(float* p, float v, int) { *p = v; }
+};
+template <> struct Fmt<double> {
+    using T = double;
+    static __device__ __forceinline__ double ld(const double* p, int) { return __ldg(p); }
+    static __device__ __forceinline__ void st(double* p, double v, int) { *p = v; }
+};
+template <> struct Fmt<__half> {
+    using T = float;
+    static __device__ __forceinline__ float ld(const __half* p, int q) { return __half2float(__ldg(p)) + wq(q); }
+    static __device__ __forceinline__ void st(__half* p, float v, int q) { *p = __float2half_rn(v - wq(q)); }
+};
+template <> struct Fmt<__nv_bfloat16> {
+    using T = float;
+    static __device__ __forceinline__ float ld(const __nv_bfloat16* p, int q) {
+        return __bfloat162float(__ldg(p)) + wq(q);
+    }
+    static __device__ __forceinline__ void st(__nv_bfloat16* p, float v, int q) { *p = __float2bfloat16_rn(v - wq(q)); }
+};
+
+template <class S>
+__global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, const StepParams p,
+                                                                  const S* __restrict__ fA, S* __restrict__ fB,
+                                                                  const uint8_t* __restrict__ mask,
+                                                                  double* __restrict__ fpart,
+                                                                  float* __restrict__ stats,
+                                                                  float* __restrict__ mom_export) {
+    using F = Fmt<S>;
+    using T = typename F::T;
+    const int x = blockIdx.x * SC_BX + threadIdx.x;
+    const int y = blockIdx.y * SC_BY + threadIdx.y;
+    const int z = blockIdx.z;
+    const bool active = (x < L.nx) && (y < L.ny);
+    double fsx = 0.0, fsy = 0.0, fsz = 0.0;
+
+    if (active) {
+        const long long qs = L.qstride;
+        const long long c = z * L.plane + (long long)y * L.pitch + x;
+        const int type = mask[c];
+        /* periodic neighbours; only boundary nodes, whose pulled values the
+         * reference discards or bounces, ever wrap in x or y */
+        const int xm = (x == 0) ? L.nx - 1 : x - 1;
+        const int xp = (x == L.nx - 1) ? 0 : x + 1;
+        const int ym = (y == 0) ? L.ny - 1 : y - 1;
+        const int yp = (y == L.ny - 1) ? 0 : y + 1;
+        const int zm = (z == 0) ? L.nz - 1 : z - 1;
+        const int zp = (z == L.nz - 1) ? 0 : z + 1;
+        const long long zb[3] = {zm * L.plane, z * L.plane, zp * L.plane};
+        const long long yb[3] = {(long long)ym * L.pitch, (long long)y * L.pitch, (long long)yp * L.pitch};
+        const int xs[3] = {xm, x, xp};
+
+        T f[19];
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            /* pull: the value arriving from x - c_q */
+            const long long src = zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)];
+            f[q] = F::ld(fA + q * qs + src, q);
+        }
+
+        if (type == WALL || type == BODY) {
+            if (type == BODY && p.force_on) {
+#pragma unroll
+                for (int q = 1; q < 19; ++q) {
+                    const double v = 2.0 * double(f[q]);
+                    if (cx(q)) fsx += cx(q) * v;
+                    if (cy(q)) fsy += cy(q) * v;
+                    if (cz(q)) fsz += cz(q) * v;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 19; ++q) F::st(fB + q * qs + c, f[opp(q)], q);
+        } else {
+            if (type >= WEST_INLET && type <= NORTH_OUTLET) {
+                /* rebuild from the neighbour's stored post-collision state */
+                long long nb = c;
+                if (type == WEST_INLET) nb = zb[1] + yb[1] + xp;
+                else if (type == EAST_OUTLET) nb = zb[1] + yb[1] + xm;
+                else if (type == SOUTH_INLET) nb = zb[1] + yb[2] + x;
+                else nb = zb[1] + yb[0] + x;
+#pragma unroll
+                for (int q = 0; q < 19; ++q) f[q] = F::ld(fA + q * qs + nb, q);
+                T uin = T(p.u_in);
+                if (p.noise_amp != 0.f) {
+                    const uint32_t cell = uint32_t((z * L.ny + y) * L.nx + x);
+                    const float xi = philox_uniform(p.noise_seed, cell, uint32_t(p.t));
+                    uin = uin + T(p.u_in) * T(p.noise_amp) * (T(2) * T(xi) - T(1));
+                }
+                extrap<T>(type, f, T(p.rho_out), uin);
+            } else if (type == LID) {
+                lid<T>(f, p.lid_face, T(p.lid_u[0]), T(p.lid_u[1]), T(p.lid_u[2]));
+            }
+            collide<T>(p.model, f, T(p.omega), p.les != 0, T(p.cs), T(p.dpdy));
+
+            if (p.stats_on && p.t >= p.start_av) {
+                /* vel_av / vel_fluc (LR7:1018-1058): running mean, then variance */
+                T u = 0, v = 0;
+#pragma unroll
+                for (int q = 0; q < 19; ++q) {
+                    if (cx(q)) u += T(cx(q)) * f[q];
+                    if (cy(q)) v += T(cy(q)) * f[q];
+                }
+                const long long ns = L.qstride;
+                float* au = stats;
+                float* av = stats + ns;
+                const float w = p.stats_weight;
+                if (p.t < p.start_fluc) {
+                    const float n = float(p.t - p.start_av);
+                    au[c] = (au[c] * n + float(u) * w) / (n + w);
+                    av[c] = (av[c] * n + float(v) * w) / (n + w);
+                } else {
+                    float* fu = stats + 2 * ns;
+                    float* fv = stats + 3 * ns;
+                    const float n = float(p.t - p.start_fluc);
+                    const float du = (float(u) - au[c]) * (float(u) - au[c]);
+                    const float dv = (float(v) - av[c]) * (float(v) - av[c]);
+                    fu[c] = (fu[c] * n + du * w) / (n + w);
+                    fv[c] = (fv[c] * n + dv * w) / (n + w);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 19; ++q) F::st(fB + q * qs + c, f[q], q);
+        }
+
+        if (p.exp_nx > 0) {
+            const int ex = x - p.exp_x0, ey = y - p.exp_y0;
+            if (ex >= 0 && ex < p.exp_nx && ey >= 0 && ey < p.exp_ny) {
+                float ff[19], mom[9];
+#pragma unroll
+                for (int q = 0; q < 19; ++q) ff[q] = float(f[q]);
+                physical_moments<float>(ff, mom);
+                const long long ne = (long long)p.exp_nx * p.exp_ny * L.nz;
+                const long long ce = ((long long)z * p.exp_ny + ey) * p.exp_nx + ex;
+#pragma unroll
+                for (int i = 0; i < 9; ++i) mom_export[i * ne + ce] = mom[i];
+            }
+        }
+    }
+
+    if (p.force_on) {
+        /* deterministic block sum in FP64: warp shuffles, then one warp */
+        __shared__ double red[SC_BY][3];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            fsx += __shfl_down_sync(0xffffffffu, fsx, o);
+            fsy += __shfl_down_sync(0xffffffffu, fsy, o);
+            fsz += __shfl_down_sync(0xffffffffu, fsz, o);
+        }
+        if (threadIdx.x == 0) {
+            red[threadIdx.y][0] = fsx;
+            red[threadIdx.y][1] = fsy;
+            red[threadIdx.y][2] = fsz;
+        }
+        __syncthreads();
+        if (threadIdx.y == 0 && threadIdx.x < 3) {
+            double s = 0.0;
+#pragma unroll
+            for (int w = 0; w < SC_BY; ++w) s += red[w][threadIdx.x];
+            const long long b = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+            fpart[b * 3 + threadIdx.x] = s;
+        }
+    }
+}
+
+/* sum n block partials (3 doubles each) in a fixed order; one block */
+__global__ void k_reduce3(const double* __restrict__ part, int n, double* __restrict__ out) {
+    __shared__ double red[3][32];
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        s[0] += part[3LL * i];
+        s[1] += part[3LL * i + 1];
+        s[2] += part[3LL * i + 2];
+    }
+    for (int k = 0; k < 3; ++k) {
+        double v = s[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double v = 0.0;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) v += red[threadIdx.x][w];
+        out[threadIdx.x] += v;
+    }
+}
+
+/* initialize / initializeLR (LR7:1060-1125): rest state at rho = 1 with the
+ * x velocity u0 (zero at bounce-back nodes).  kind 0: the MRT equilibrium
+ * moments (mrt_meq + InvertMoments); kind 1: the BGK equilibrium. */
+template <class S>
+__global__ void k_init(const Level L, const uint8_t* __restrict__ mask, S* __restrict__ f, int kind, float u0) {
+    using F = Fmt<S>;
+    using T = typename F::T;
+    const int x = blockIdx.x * SC_BX + threadIdx.x, y = blockIdx.y * SC_BY + threadIdx.y, z = blockIdx.z;
+    if (x >= L.nx || y >= L.ny) return;
+    const long long c = z * L.plane + (long long)y * L.pitch + x;
+    const int type = mask[c];
+    const T u = (type == WALL || type == BODY) ? T(0) : T(u0);
+    T g[19];
+    if (kind == 0) {
+        const T mom[9] = {T(1), u, T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+        invert_scaled<T>(mom, T(0), g);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            const T cu = T(cx(q)) * u;
+            g[q] = T(wq(q)) * (T(1) + T(3) * cu + T(4.5) * cu * cu - T(1.5) * u * u);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 19; ++q) F::st(f + q * L.qstride + c, g[q], q);
+}
+
+/* density and momentum (the reference's u, v, w are momenta) into compact arrays */
+template <class S>
+__global__ void k_fields(const Level L, const S* __restrict__ f, float* rho, float* u, float* v, float* w) {
+    using F = Fmt<S>;
+    using T = typename F::T;
+    const int x = blockIdx.x * SC_BX + threadIdx.x, y = blockIdx.y * SC_BY + threadIdx.y, z = blockIdx.z;
+    if (x >= L.nx || y >= L.ny) return;
+    const long long c = z * L.plane + (long long)y * L.pitch + x;
+    T r = 0, a = 0, b = 0, d = 0;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const T g = F::ld(f + q * L.qstride + c, q);
+        r += g;
+        if (cx(q)) a += T(cx(q)) * g;
+        if (cy(q)) b += T(cy(q)) * g;
+        if (cz(q)) d += T(cz(q)) * g;
+    }
+    const long long o = ((long long)z * L.ny + y) * L.nx + x;
+    if (rho) rho[o] = float(r);
+    if (u) u[o] = float(a);
+    if (v) v[o] = float(b);
+    if (w) w[o] = float(d);
+}
+
+template <class S> __global__ void k_pack(const Level L, const S* __restrict__ f, float* __restrict__ out) {
+    using F = Fmt<S>;
+    const int x = blockIdx.x * SC_BX + threadIdx.x, y = blockIdx.y * SC_BY + threadIdx.y, z = blockIdx.z;
+    if (x >= L.nx || y >= L.ny) return;
+    const long long c = z * L.plane + (long long)y * L.pitch + x;
+    const long long n = (long long)L.nx * L.ny * L.nz, o = ((long long)z * L.ny + y) * L.nx + x;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) out[q * n + o] = float(F::ld(f + q * L.qstride + c, q));
+}
+
+template <class S> __global__ void k_unpack(const Level L, const float* __restrict__ in, S* __restrict__ f) {
+    using F = Fmt<S>;
+    const int x = blockIdx.x * SC_BX + threadIdx.x, y = blockIdx.y * SC_BY + threadIdx.y, z = blockIdx.z;
+    if (x >= L.nx || y >= L.ny) return;
+    const long long c = z * L.plane + (long long)y * L.pitch + x;
+    const long long n = (long long)L.nx * L.ny * L.nz, o = ((long long)z * L.ny + y) * L.nx + x;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) F::st(f + q * L.qstride + c, in[q * n + o], q);
+}
+
+/* FP64 mass and momentum of the non-solid nodes; grid-stride over rows so the
+ * number of block partials is fixed (audit_partials) */
+constexpr int AUDIT_BLOCKS = 1216; /* 8 blocks per SM on a 152-SM GB300 */
+template <class S>
+__global__ void __launch_bounds__(256) k_audit(const Level L, const S* __restrict__ f, const uint8_t* __restrict__ mask,
+                                               double* __restrict__ part) {
+    using F = Fmt<S>;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    const long long rows = (long long)L.ny * L.nz;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (long long r = (long long)blockIdx.x * 8 + warp; r < rows; r += (long long)gridDim.x * 8) {
+        const int y = int(r % L.ny), z = int(r / L.ny);
+        for (int x = lane; x < L.nx; x += 32) {
+            const long long c = z * L.plane + (long long)y * L.pitch + x;
+            const int t = mask[c];
+            if (t == WALL || t == BODY) continue;
+#pragma unroll
+            for (int q = 0; q < 19; ++q) {
+                const double g = double(F::ld(f + q * L.qstride + c, q));
+                acc[0] += g;
+                if (cx(q)) acc[1] += cx(q) * g;
+                if (cy(q)) acc[2] += cy(q) * g;
+                if (cz(q)) acc[3] += cz(q) * g;
+            }
+        }
+    }
+    __shared__ double red[4][8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        double v = acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double v = 0.0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) v += red[threadIdx.x][w];
+        part[4LL * blockIdx.x + threadIdx.x] = v;
+    }
+}
+
+__global__ void k_audit_final(const double* __restrict__ part, int n, double* __restrict__ out) {
+    __shared__ double red[4][8];
+    double s[4] = {0, 0, 0, 0};
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        for (int k = 0; k < 4; ++k) s[k] += part[4LL * i + k];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = 0; k < 4; ++k) {
+        double v = s[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double v = 0.0;
+        for (int w = 0; w < 8; ++w) v += red[threadIdx.x][w];
+        out[threadIdx.x] = v;
+    }
+}
+
+/* ---- refinement exchange ---- */
+
+template <class S>
+__device__ __forceinline__ void load19(const Level& L, const S* f, long long c, float g[19]) {
+#pragma unroll
+    for (int q = 0; q < 19; ++q) g[q] = float(Fmt<S>::ld(f + q * L.qstride + c, q));
+}
+
+/* second-order correction of the interpolated momentum from the 8 corner
+ * strain rates and momenta (LR7:2101-2144, 2270-2316); corner i = x + 2y + 4z */
+__device__ __forceinline__ void second_order(const float mc[8][9], const float S[8][6], float a[9]) {
+#pragma unroll
+    for (int j = 0; j < 9; ++j) a[j] = 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const float sx = (i & 1) ? 1.f : -1.f, sy = (i & 2) ? 1.f : -1.f, sz = (i & 4) ? 1.f : -1.f;
+        a[0] += sx * S[i][0];
+        a[1] += sy * S[i][3] - sx * sy * mc[i][2];
+        a[2] += sz * S[i][5] - sx * sz * mc[i][3];
+        a[3] += sx * S[i][3] - sx * sy * mc[i][1];
+        a[4] += sy * S[i][1];
+        a[5] += sz * S[i][4] - sy * sz * mc[i][3];
+        a[6] += sx * S[i][5] - sx * sz * mc[i][1];
+        a[7] += sy * S[i][4] - sy * sz * mc[i][2];
+        a[8] += sz * S[i][2];
+    }
+#pragma unroll
+    for (int j = 0; j < 9; ++j) a[j] *= (j % 4 == 0) ? -0.03125f : -0.0625f;
+}
+
+/* InterpCF (LR7:1991-2170): fine nodes of the LRLEVEL-wide x/y band get the
+ * coarse moments interpolated (trilinear + second-order velocity correction)
+ * and rebuilt with the LES-aware non-equilibrium rescale (LR7:524-579).  One
+ * thread per band node; mom_c is [9][cnz][eny][enx] (coarse footprint). */
+template <class S>
+__global__ void k_interp_cf(const RefineParams r, const Level F, const float* __restrict__ mom_c, S* __restrict__ f_f,
+                            const uint8_t* __restrict__ mask_f) {
+    const int L = r.lrlevel;
+    const int nb_x = r.fny * 2 * L;                /* x-band nodes per plane */
+    const int nb_y = (r.fnx - 2 * L) * 2 * L;      /* y-band nodes per plane (x-band excluded) */
+    const int per_plane = nb_x + nb_y;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)per_plane * r.fnz) return;
+    const int k = int(idx / per_plane);
+    int i = int(idx % per_plane), xf, yf;
+    if (i < nb_x) {
+        yf = i / (2 * L);
+        const int b = i % (2 * L);
+        xf = b < L ? b : r.fnx - 2 * L + b;
+    } else {
+        i -= nb_x;
+        xf = L + i / (2 * L);
+        const int b = i % (2 * L);
+        yf = b < L ? b : r.fny - 2 * L + b;
+    }
+    const long long cf = k * F.plane + (long long)yf * F.pitch + xf;
+    const int t = mask_f[cf];
+    if (t == WALL || t == BODY) return;
+    const float xr = xf * r.lrfactor + r.lrfactor * 0.5f, yr = yf * r.lrfactor + r.lrfactor * 0.5f;
+    const int xm = int(xr), ym = int(yr);
+    const float fx = xr - xm, fy = yr - ym;
+    int zb = k / L - 1;
+    const float fz = (k % L) * r.lrfactor + r.lrfactor * 0.5f;
+    const long long ne = (long long)r.enx * r.eny * r.cnz;
+    float mc[8][9], Sc[8][6];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        int zc = zb + ((c >> 2) & 1);
+        zc = zc < 0 ? zc + r.cnz : (zc >= r.cnz ? zc - r.cnz : zc);
+        const long long ce = ((long long)zc * r.eny + (ym + ((c >> 1) & 1))) * r.enx + (xm + (c & 1));
+#pragma unroll
+        for (int m = 0; m < 9; ++m) mc[c][m] = __ldg(mom_c + m * ne + ce);
+        strain_rate<float>(mc[c], Sc[c]);
+    }
+    float mom[9];
+#pragma unroll
+    for (int m = 0; m < 9; ++m)
+        mom[m] = mc[0][m] * (1.f - fx) * (1.f - fy) * (1.f - fz) + mc[1][m] * fx * (1.f - fy) * (1.f - fz) +
+                 mc[2][m] * (1.f - fx) * fy * (1.f - fz) + mc[3][m] * fx * fy * (1.f - fz) +
+                 mc[4][m] * (1.f - fx) * (1.f - fy) * fz + mc[5][m] * fx * (1.f - fy) * fz +
+                 mc[6][m] * (1.f - fx) * fy * fz + mc[7][m] * fx * fy * fz;
+    if (r.order == 2) {
+        float a[9];
+        second_order(mc, Sc, a);
+        const float wx = 1.f - (4.f * fx * fx - 4.f * fx + 1.f);
+        const float wy = 1.f - (4.f * fy * fy - 4.f * fy + 1.f);
+        const float wz = 1.f - (4.f * fz * fz - 4.f * fz + 1.f);
+        mom[1] += a[0] * wx + a[1] * wy + a[2] * wz;
+        mom[2] += a[3] * wx + a[4] * wy + a[5] * wz;
+        mom[3] += a[6] * wx + a[7] * wy + a[8] * wz;
+    }
+    /* InvertPhysicalMoments_LES_cf: rescale factor from the local eddy viscosity */
+    float Sm[6];
+    strain_rate<float>(mom, Sm);
+    const float smag = strain_mag<float>(Sm);
+    float tau_c = 1.f / r.omega_c;
+    const float tau_f = 2.f * tau_c - 0.5f + 1.5f * smag * r.cs;
+    const float omega_f = 1.f / tau_f;
+    tau_c = tau_c + smag * r.cs;
+    const float omega_c = 1.f / tau_c;
+    const float SF = (r.lrfactor * omega_c * (1.f - omega_f)) / ((1.f - omega_c) * omega_f);
+    float g[19];
+    invert_scaled<float>(mom, SF, g);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) Fmt<S>::st(f_f + q * F.qstride + cf, g[q], q);
+}
+
+/* InterpFC (LR7:2172-2348): coarse nodes strictly inside the patch (2-node
+ * margin) are replaced by the restriction of their 8 fine children. */
+template <class S>
+__global__ void k_interp_fc(const RefineParams r, const Level C, const Level F, const S* __restrict__ f_f,
+                            S* __restrict__ f_c, const uint8_t* __restrict__ mask_c, int x0, int y0, int nxi, int nyi) {
+    const int xi = blockIdx.x * blockDim.x + threadIdx.x, yi = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
+    if (xi >= nxi || yi >= nyi) return;
+    const int x = x0 + xi, y = y0 + yi;
+    const long long cc = z * C.plane + (long long)y * C.pitch + x;
+    const int t = mask_c[cc];
+    if (t == WALL || t == BODY) return;
+    const int L = r.lrlevel;
+    const int xm = int(L * (x - r.lrx0)), ym = int(L * (y - r.lry0));
+    int kl = int(L * (z - r.lrz0)), kh = kl + 1;
+    const bool top = kh >= r.fnz;
+    kl = kl >= r.fnz ? kl - r.fnz : kl;
+    kh = kh >= r.fnz ? kh - r.fnz : kh;
+    int k0 = kl, k1 = kh;
+    if (top && r.quirk_fc_top_zflip) {
+        /* the reference reads the top plane's corners upper plane first */
+        k0 = kh;
+        k1 = kl;
+    }
+    float mc[8][9], Sc[8][6];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int kk = (c & 4) ? k1 : k0;
+        const long long cf = kk * F.plane + (long long)(ym + ((c >> 1) & 1)) * F.pitch + (xm + (c & 1));
+        float g[19];
+        load19<S>(F, f_f, cf, g);
+        physical_moments<float>(g, mc[c]);
+        strain_rate<float>(mc[c], Sc[c]);
+    }
+    float mom[9];
+#pragma unroll
+    for (int m = 0; m < 9; ++m) {
+        float s = 0.f;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) s += mc[c][m];
+        mom[m] = 0.125f * s;
+    }
+    if (r.order == 2) {
+        float a[9];
+        second_order(mc, Sc, a);
+        mom[1] += a[0] + a[1] + a[2];
+        mom[2] += a[3] + a[4] + a[5];
+        mom[3] += a[6] + a[7] + a[8];
+    }
+    /* InvertPhysicalMoments_LES_fc */
+    float Sm[6];
+    strain_rate<float>(mom, Sm);
+    const float smag = strain_mag<float>(Sm);
+    float tau_f = 1.f / r.omega_f;
+    float tau_c = tau_f + 0.5f + 12.f * smag * r.cs;
+    tau_c *= 0.5f;
+    const float omega_c = 1.f / tau_c;
+    tau_f = tau_f + smag * r.cs;
+    const float omega_f = 1.f / tau_f;
+    const float SF = (1.f - omega_c) * omega_f / (r.lrfactor * omega_c * (1.f - omega_f));
+    float g[19];
+    invert_scaled<float>(mom, SF, g);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) Fmt<S>::st(f_c + q * C.qstride + cc, g[q], q);
+}
+
+/* ---- launchers ---- */
+
+#define LBM_DISPATCH(storage, KERNEL_CALL)                   \
+    switch (storage) {                                        \
+        case STORE_F32: { using S = float; KERNEL_CALL; } break;            \
+        case STORE_F16: { using S = __half; KERNEL_CALL; } break;           \
+        case STORE_BF16: { using S = __nv_bfloat16; KERNEL_CALL; } break;   \
+        case STORE_F64: { using S = double; KERNEL_CALL; } break;           \
+        default: return cudaErrorInvalidValue;                \
+    }
+
+cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const void* fA, void* fB, const uint8_t* mask,
+                                  double* force_partials, float* stats, float* mom_export, cudaStream_t s) {
+    const dim3 block(SC_BX, SC_BY), grid = sc_grid(L);
+    LBM_DISPATCH(L.storage, (k_stream_collide<S><<<grid, block, 0, s>>>(L, p, (const S*)fA, (S*)fB, mask,
+                                                                         force_partials, stats, mom_export)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_force(const double* partials, int n, double* out3, cudaStream_t s) {
+    k_reduce3<<<1, 1024, 0, s>>>(partials, n, out3);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init(const Level& L, const uint8_t* mask, void* f, int kind, float u0, cudaStream_t s) {
+    const dim3 block(SC_BX, SC_BY), grid = sc_grid(L);
+    LBM_DISPATCH(L.storage, (k_init<S><<<grid, block, 0, s>>>(L, mask, (S*)f, kind, u0)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fields(const Level& L, const void* f, float* rho, float* u, float* v, float* w, cudaStream_t s) {
+    const dim3 block(SC_BX, SC_BY), grid = sc_grid(L);
+    LBM_DISPATCH(L.storage, (k_fields<S><<<grid, block, 0, s>>>(L, (const S*)f, rho, u, v, w)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack(const Level& L, const void* f, float* compact, cudaStream_t s) {
+    const dim3 block(SC_BX, SC_BY), grid = sc_grid(L);
+    LBM_DISPATCH(L.storage, (k_pack<S><<<grid, block, 0, s>>>(L, (const S*)f, compact)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack(const Level& L, const float* compact, void* f, cudaStream_t s) {
+    const dim3 block(SC_BX, SC_BY), grid = sc_grid(L);
+    LBM_DISPATCH(L.storage, (k_unpack<S><<<grid, block, 0, s>>>(L, compact, (S*)f)));
+    return cudaGetLastError();
+}
+
+int audit_partials(const Level&) { return AUDIT_BLOCKS; }
+
+cudaError_t launch_audit(const Level& L, const void* f, const uint8_t* mask, double* partials, int npart, double* out4,
+                         cudaStream_t s) {
+    if (npart < AUDIT_BLOCKS) return cudaErrorInvalidValue;
+    LBM_DISPATCH(L.storage, (k_audit<S><<<AUDIT_BLOCKS, 256, 0, s>>>(L, (const S*)f, mask, partials)));
+    k_audit_final<<<1, 256, 0, s>>>(partials, AUDIT_BLOCKS, out4);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_interp_cf(const RefineParams& r, const Level& F, const float* mom_c, void* f_f,
+                             const uint8_t* mask_f, cudaStream_t s) {
+    const int L = r.lrlevel;
+    const long long n = (long long)(r.fny * 2 * L + (r.fnx - 2 * L) * 2 * L) * r.fnz;
+    const int threads = 128;
+    const unsigned blocks = unsigned((n + threads - 1) / threads);
+    LBM_DISPATCH(F.storage, (k_interp_cf<S><<<blocks, threads, 0, s>>>(r, F, mom_c, (S*)f_f, mask_f)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_interp_fc(const RefineParams& r, const Level& C, const Level& F, const void* f_f, void* f_c,
+                             const uint8_t* mask_c, cudaStream_t s) {
+    /* coarse x with x > lrx0 + 1 and x < lrx0 + fnx*lrfactor - 2 (same for y) */
+    int x0 = 0, x1 = -1, y0 = 0, y1 = -1;
+    for (int x = 0; x < C.nx; ++x)
+        if (x > r.lrx0 + 1 && x < r.lrx0 + r.fnx * r.lrfactor - 2) {
+            if (x1 < x0) x0 = x;
+            x1 = x;
+        }
+    for (int y = 0; y < C.ny; ++y)
+        if (y > r.lry0 + 1 && y < r.lry0 + r.fny * r.lrfactor - 2) {
+            if (y1 < y0) y0 = y;
+            y1 = y;
+        }
+    const int nxi = x1 - x0 + 1, nyi = y1 - y0 + 1;
+    if (nxi <= 0 || nyi <= 0) return cudaSuccess;
+    const dim3 block(32, 4), grid((nxi + 31) / 32, (nyi + 3) / 4, C.nz);
+    LBM_DISPATCH(C.storage, (k_interp_fc<S><<<grid, block, 0, s>>>(r, C, F, (const S*)f_f, (S*)f_c, mask_c, x0, y0,
+                                                                    nxi, nyi)));
+    return cudaGetLastError();
+}
+
+}  // namespace lbm

@@ -1,0 +1,97 @@
+/*
+ * lbm_kernels.cuh -- level descriptor and kernel launchers shared by the host
+ * library and the kernels (one compilation unit: lbm_kernels.cu).
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lbm {
+
+/* node types of the one-byte mask; numbering shared with include/lbm_gb300.h */
+enum NodeType : uint8_t {
+    FLUID = 0,
+    WALL = 1,
+    BODY = 2,
+    WEST_INLET = 3,
+    EAST_OUTLET = 4,
+    SOUTH_INLET = 5,
+    NORTH_OUTLET = 6,
+    LID = 7
+};
+
+/* collision models: LR7 mrt_collide, DynInlet3's MRT (bgk_meq + AddForce),
+ * BGK, CPU_3D's MRT */
+enum Model : int { MRT = 0, MRT_DI3 = 1, BGK = 2, MRT_CPU3D = 3 };
+
+enum Storage : int { STORE_F32 = 0, STORE_F16 = 1, STORE_BF16 = 2, STORE_F64 = 3 };
+
+/* One grid level in HBM.  Populations are structure-of-arrays,
+ * f[q][z][y][x] with a padded x pitch; q-planes are qstride elements apart. */
+struct Level {
+    int nx, ny, nz;
+    int pitch;            /* elements per row, a multiple of 32 */
+    long long plane;      /* pitch * ny */
+    long long qstride;    /* plane * nz */
+    int storage;          /* Storage */
+};
+
+struct StepParams {
+    int model;
+    int les;
+    float omega, cs, dpdy;
+    float u_in, rho_out;
+    float lid_u[3];
+    int lid_face;
+    int force_on;          /* accumulate momentum exchange at BODY nodes */
+    int t;                 /* time step index (stats, noise) */
+    int stats_on, start_av, start_fluc;
+    float stats_weight;
+    float noise_amp;
+    uint32_t noise_seed;
+    /* coarse-moment export for the coarse->fine interpolation */
+    int exp_x0, exp_y0, exp_nx, exp_ny;
+};
+
+/* launch configuration of the stream-collide kernel */
+constexpr int SC_BX = 32, SC_BY = 8;
+
+inline dim3 sc_grid(const Level& L) { return dim3(L.pitch / SC_BX, (L.ny + SC_BY - 1) / SC_BY, L.nz); }
+inline int sc_blocks(const Level& L) {
+    dim3 g = sc_grid(L);
+    return int(g.x * g.y * g.z);
+}
+
+/* kernel launchers (lbm_kernels.cu) */
+cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const void* fA, void* fB,
+                                  const uint8_t* mask, double* force_partials, float* stats,
+                                  float* mom_export, cudaStream_t s);
+cudaError_t launch_reduce_force(const double* partials, int n, double* out3, cudaStream_t s);
+cudaError_t launch_init(const Level& L, const uint8_t* mask, void* f, int kind, float u0, cudaStream_t s);
+cudaError_t launch_fields(const Level& L, const void* f, float* rho, float* u, float* v, float* w, cudaStream_t s);
+cudaError_t launch_pack(const Level& L, const void* f, float* compact, cudaStream_t s);
+cudaError_t launch_unpack(const Level& L, const float* compact, void* f, cudaStream_t s);
+cudaError_t launch_audit(const Level& L, const void* f, const uint8_t* mask, double* partials, int npart,
+                         double* out4, cudaStream_t s);
+int audit_partials(const Level& L);
+
+struct RefineParams {
+    int cnx, cny, cnz;
+    int fnx, fny, fnz;
+    float lrx0, lry0, lrz0;
+    float lrfactor;
+    int lrlevel;
+    int order;
+    float cs;
+    float omega_c, omega_f;
+    int quirk_fc_top_zflip;
+    int enx, eny;          /* exported coarse-moment footprint */
+};
+
+cudaError_t launch_interp_cf(const RefineParams& r, const Level& F, const float* mom_c, void* f_f,
+                             const uint8_t* mask_f, cudaStream_t s);
+cudaError_t launch_interp_fc(const RefineParams& r, const Level& C, const Level& F, const void* f_f, void* f_c,
+                             const uint8_t* mask_c, cudaStream_t s);
+
+}  // namespace lbm

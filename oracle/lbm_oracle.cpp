@@ -184,17 +184,22 @@ template <class T> inline void add_force(T* f, T dpdy) {
 /* LR7 mrt_collide (LR7:583-711): non-equilibrium moments relaxed at rate 1,
  * except the stress moments 9, 11, 13, 14, 15 which relax with omega (tau_eff
  * when LES is on). */
-template <class T> inline void collide_mrt(T* f, T omega, int les, T cs) {
+template <class T> inline void collide_mrt(T* f, T omega, int les, T cs, bool cpu3d = false) {
     if (les) omega = les_omega(f, omega, cs);
     T m[Q], meq[Q], n[Q];
     moments(f, m);
     meq_lr7(meq, m[0], m[3], m[5], m[7]);
+    /* CPU_3D's mrt_collide: meq2 = -7.53968254 |j|^2 (CPU:222) and m13, m14
+     * relaxed at rate 1 (CPU:246-248) */
+    if (cpu3d) meq[2] = -meq[2];
     for (int k = 0; k < Q; ++k) n[k] = m[k] - meq[k];
     n[0] = n[3] = n[5] = n[7] = 0;
     n[9] *= omega;
     n[11] *= omega;
-    n[13] *= omega;
-    n[14] *= omega;
+    if (!cpu3d) {
+        n[13] *= omega;
+        n[14] *= omega;
+    }
     n[15] *= omega;
     T df[Q];
     invert(n, df);
@@ -229,6 +234,7 @@ template <class T> inline void collide_bgk(T* f, T omega, int les, T cs, T dpdy)
 
 template <class T> inline void collide(int model, T* f, T omega, int les, T cs, T dpdy) {
     if (model == ORC_MRT) collide_mrt(f, omega, les, cs);
+    else if (model == ORC_MRT_CPU3D) collide_mrt(f, omega, les, cs, true);
     else if (model == ORC_MRT_DI3) collide_mrt_di3(f, omega, les, cs, dpdy);
     else collide_bgk(f, omega, les, cs, dpdy);
 }

@@ -43,7 +43,8 @@ enum {
 enum {
     ORC_MRT = 0,      /* LR7 mrt_collide, LR7:583-711 */
     ORC_MRT_DI3 = 1,  /* DynInlet3 MRT branch with bgk_meq, MRTtest/DynInlet3.cu:770-789 */
-    ORC_BGK = 2       /* DynInlet3 / CPU_3D BGK, MRTtest/DynInlet3.cu:806-827 */
+    ORC_BGK = 2,      /* DynInlet3 / CPU_3D BGK, MRTtest/DynInlet3.cu:806-827 */
+    ORC_MRT_CPU3D = 3 /* CPU_3D mrt_collide, CPU_3D/CPU_3D.cpp:164-409 */
 };
 
 typedef struct {

@@ -62,6 +62,10 @@ LR7_CONFIGS = {
                    OBSTY1="11.5f", RE="20.f", UMAX="0.05f", SmagLES=0, CS="0.01f", REFINEMENT=1,
                    LRFACTOR="0.5f", LRLEVEL=2, LRX0="12.25f", XLRDIM=32, LRY0="4.25f", YLRDIM=32,
                    LRZ0="-0.75f", ZLRDIM=8, ORDER=2, BLOCKSIZELRX=32, VELAV=0, START_VELAV=100000, START_VELFLUC=250000),
+    # tiny channel for the output-writer fixtures (statistics switch on at t = 5 and 12)
+    "tiny": dict(XDIM=64, YDIM=8, ZDIM=4, TMAX=20, STARTF=0, OBSTR1="2.f", OBSTX1="20.5f", OBSTY1="3.5f",
+                 RE="40.f", UMAX="0.05f", SmagLES=1, CS="0.01f", REFINEMENT=0, VELAV=1, START_VELAV=5,
+                 START_VELFLUC=12),
 }
 
 # CPU_3D workloads: the baseline timing at the 512x128x128 channel shape and a

@@ -1,0 +1,186 @@
+"""Generate the golden fixtures of tests/golden/ from the reference's own code.
+
+Runs the reference's device functions, kernels and writers (LRTurbTest/
+LRMultiGPU7.cu, MRTtest/DynInlet3.cu, CPU_3D/CPU_3D.cpp) through the host
+harness that oracle/ref_recipe.py stages and builds in oracle/_ref/ (needs the
+reference sources, i.e. the development container).  Seeded inputs; rerunning
+reproduces the files.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import ctypes
+import gzip
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(ROOT / "oracle"))
+import ref_recipe  # noqa: E402
+
+P = ctypes.c_void_p
+F = ctypes.c_float
+
+
+def ptr(a):
+    return a.ctypes.data_as(P)
+
+
+def lib(name):
+    return ctypes.CDLL(str(ref_recipe.REF_DIR / name))
+
+
+CX = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1, 0, 1, 0, -1, 0, 0, 1, 0, -1, 0])
+CY = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1, 0, 0, 1, 0, -1, 0, 0, 1, 0, -1])
+CZ = np.array([0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, -1, -1, -1, -1, -1])
+W = np.array([1 / 3] + [1 / 18] * 4 + [1 / 36] * 4 + [1 / 18] + [1 / 36] * 4 + [1 / 18] + [1 / 36] * 4)
+
+
+def random_cells(n, seed):
+    """near-equilibrium populations: BGK equilibrium of random (rho, j) plus noise"""
+    rng = np.random.default_rng(seed)
+    rho = 1 + 0.05 * rng.standard_normal(n)
+    u = 0.06 * rng.standard_normal((3, n))
+    cu = np.outer(CX, u[0]) + np.outer(CY, u[1]) + np.outer(CZ, u[2])
+    feq = W[:, None] * (rho + 3 * cu + 4.5 * cu ** 2 - 1.5 * (u ** 2).sum(0))
+    f = feq + 2e-3 * rng.standard_normal(feq.shape) * W[:, None]
+    return np.ascontiguousarray(f.T, np.float32)
+
+
+def fields(f):
+    g = f.astype(np.float64)
+    return np.stack([g.sum(0)] + [np.tensordot(c, g, 1) for c in (CX, CY, CZ)]).astype(np.float32)
+
+
+def cells():
+    n = 64
+    f0 = random_cells(n, 20251203)
+    out = dict(f0=f0)
+    les = lib("lr7_chan_les.so")
+    mrt = lib("lr7_chan_mrt.so")
+    lr = lib("lr7_lr.so")
+    di3 = lib("di3.so")
+    c3 = lib("cpu3d.so")
+    for om in (1.2, 1.8, 1.95):
+        g = f0.copy()
+        les.ref_mrt_collide(ptr(g), n, F(om))
+        out[f"lr7_mrt_les_cs0.01_om{om}"] = g
+        g = f0.copy()
+        mrt.ref_mrt_collide(ptr(g), n, F(om))
+        out[f"lr7_mrt_om{om}"] = g
+        for use_mrt, name in ((1, "mrt"), (0, "bgk")):
+            g = f0.copy()
+            di3.ref_di3_collide(ptr(g), n, F(om), F(-5.16e-7), use_mrt)
+            out[f"di3_{name}_les_cs0.02_dpdy-5.16e-7_om{om}"] = g
+        g = f0.copy()
+        c3.ref_cpu3d_mrt(ptr(g), n, F(om))
+        out[f"cpu3d_mrt_om{om}"] = g
+        g = f0.copy()
+        c3.ref_cpu3d_bgk(ptr(g), n, F(om))
+        out[f"cpu3d_bgk_om{om}"] = g
+    for kind, val in ((3, 0.05), (4, 1.0), (5, 0.04), (6, 1.0)):
+        g = f0.copy()
+        les.ref_extrap(kind, ptr(g), n, F(val))
+        out[f"extrap_{kind}_{val}"] = g
+    g = f0.copy()
+    c3.ref_cpu3d_lid_west(ptr(g), n)
+    out["cpu3d_lid_west"] = g
+    mom = np.zeros((n, 9), np.float32)
+    les.ref_physical_moments(ptr(f0), ptr(mom), n)
+    out["physical_moments"] = mom
+    s = np.zeros((n, 6), np.float32)
+    les.ref_strain_rate(ptr(mom), ptr(s), n)
+    out["strain_rate"] = s
+    for om in (1.9, 1.6):
+        g = np.zeros((n, 19), np.float32)
+        lr.ref_invert_les_cf(ptr(mom), ptr(g), n, F(om))
+        out[f"invert_les_cf_cs0.01_lrf0.5_om{om}"] = g
+        g = np.zeros((n, 19), np.float32)
+        lr.ref_invert_les_fc(ptr(mom), ptr(g), n, F(om))
+        out[f"invert_les_fc_cs0.01_lrf0.5_om{om}"] = g
+    g = np.zeros(19, np.float32)
+    les.ref_init_meq(ptr(g), F(0.05))
+    out["init_meq_u0.05"] = g
+    np.savez_compressed(HERE / "cells.npz", **out)
+
+
+def write_inputs_text(L):
+    buf = ctypes.create_string_buffer(1 << 14)
+    n = L.ref_write_inputs(buf, len(buf))
+    assert n > 0
+    return buf.value.decode()
+
+
+def runs():
+    meta = {}
+    arrays = {}
+    for name, steps in (("chan_les", 200), ("chan_mrt", 200), ("lr", 100)):
+        cfg = ref_recipe.LR7_CONFIGS[name]
+        L = lib(f"lr7_{name}.so")
+        L.ref_setup(None, None)
+        X, Y, Z = cfg["XDIM"], cfg["YDIM"], cfg["ZDIM"]
+        img = np.zeros((Z, Y, X), np.int32)
+        L.ref_image(ptr(img))
+        arrays[f"{name}_image"] = img.astype(np.int16)
+        L.ref_run(0, steps)
+        f = np.zeros((19, Z, Y, X), np.float32)
+        L.ref_get_coarse(ptr(f))
+        arrays[f"{name}_fields"] = fields(f)
+        Fr = np.zeros((3, cfg["TMAX"]), np.float32)
+        L.ref_get_forces(ptr(Fr), cfg["TMAX"])
+        arrays[f"{name}_forces"] = Fr[:, :steps].T.copy()
+        prm = np.zeros(4, np.float32)
+        L.ref_get_params(ptr(prm))
+        arrays[f"{name}_params"] = prm
+        meta[name] = dict(steps=steps, inputs=write_inputs_text(L), config={k: str(v) for k, v in cfg.items()})
+        if cfg.get("REFINEMENT") == 1:
+            fx, fy, fz = cfg["XLRDIM"], cfg["YLRDIM"], cfg["ZLRDIM"]
+            ff = np.zeros((19, fz, fy, fx), np.float32)
+            L.ref_get_fine(ptr(ff))
+            arrays[f"{name}_fine_fields"] = fields(ff)
+            imgf = np.zeros((fz, fy, fx), np.int32)
+            L.ref_image_lr(ptr(imgf))
+            arrays[f"{name}_fine_image"] = imgf.astype(np.int16)
+    np.savez_compressed(HERE / "runs.npz", **arrays)
+    (HERE / "runs.json").write_text(json.dumps(meta, indent=1))
+
+
+def writer():
+    """WriteInputs / WriteResults / WriteForces text of a tiny channel run"""
+    cfg = ref_recipe.LR7_CONFIGS["tiny"]
+    L = lib("lr7_tiny.so")
+    L.ref_setup(None, None)
+    steps = cfg["TMAX"]
+    L.ref_run(0, steps)
+    X, Y, Z = cfg["XDIM"], cfg["YDIM"], cfg["ZDIM"]
+    f = np.zeros((19, Z, Y, X), np.float32)
+    L.ref_get_coarse(ptr(f))
+    zone = ctypes.create_string_buffer(1 << 22)
+    sl = ctypes.create_string_buffer(1 << 20)
+    assert L.ref_write_results(zone, len(zone), sl, len(sl)) == 0
+    forces = ctypes.create_string_buffer(1 << 16)
+    assert L.ref_write_forces(forces, len(forces), 0) > 0
+    np.savez_compressed(HERE / "writer_tiny.npz", f=f)
+    with gzip.open(HERE / "writer_tiny_part0.dat.gz", "wt") as fh:
+        fh.write(zone.value.decode())
+    with gzip.open(HERE / "writer_tiny_slice.dat.gz", "wt") as fh:
+        fh.write(sl.value.decode())
+    (HERE / "writer_tiny.force").write_text(forces.value.decode())
+    (HERE / "writer_tiny.inputs").write_text(write_inputs_text(L))
+
+
+if __name__ == "__main__":
+    if not ref_recipe.staged():
+        if not ref_recipe.stage():
+            sys.exit("reference sources not found; set LBM_REFERENCE")
+    ref_recipe.build_ref()
+    cells()
+    runs()
+    writer()
+    for p in sorted(HERE.iterdir()):
+        print(f"{p.stat().st_size:>9} {p.name}")

@@ -1,0 +1,37 @@
+/*
+ * cell_ops_shim.cu -- test-only host build of the product's per-cell operators
+ * (lbm_multigpu_gb300/csrc/d3q19.cuh) so their arithmetic can be compared with
+ * the oracle on a machine without a GPU.  Not part of the product library.
+ */
+#include <stdint.h>
+
+#include "../../lbm_multigpu_gb300/csrc/d3q19.cuh"
+
+using namespace lbm;
+
+extern "C" {
+
+void cell_collide(int model, int les, float omega, float cs, float dpdy, float* f, int n) {
+    for (int i = 0; i < n; ++i) collide<float>(model, f + 19L * i, omega, les != 0, cs, dpdy);
+}
+void cell_collide_d(int model, int les, double omega, double cs, double dpdy, double* f, int n) {
+    for (int i = 0; i < n; ++i) collide<double>(model, f + 19L * i, omega, les != 0, cs, dpdy);
+}
+void cell_extrap(int type, float* f, int n, float rho, float u_in) {
+    for (int i = 0; i < n; ++i) extrap<float>(type, f + 19L * i, rho, u_in);
+}
+void cell_lid(float* f, int n, int face, float ux, float uy, float uz) {
+    for (int i = 0; i < n; ++i) lid<float>(f + 19L * i, face, ux, uy, uz);
+}
+void cell_physical_moments(const float* f, float* mom, int n) {
+    for (int i = 0; i < n; ++i) physical_moments<float>(f + 19L * i, mom + 9L * i);
+}
+void cell_strain_rate(const float* mom, float* s, int n) {
+    for (int i = 0; i < n; ++i) strain_rate<float>(mom + 9L * i, s + 6L * i);
+}
+void cell_invert_scaled(const float* mom, float sf, float* f, int n) {
+    for (int i = 0; i < n; ++i) invert_scaled<float>(mom + 9L * i, sf, f + 19L * i);
+}
+float cell_philox_uniform(uint32_t seed, uint32_t cell, uint32_t step) { return philox_uniform(seed, cell, step); }
+
+}  // extern "C"
