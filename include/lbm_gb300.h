@@ -132,16 +132,22 @@ int lbm_write_outputs(lbm_handle* h, const char* casename);
 /* One stream-collide step of a level from device buffer fA into fB: the work
  * of update_inn/update_top/update_bot (LR7:1127-1628) over a single domain
  * with periodic z.  Buffers are float[19][nz][ny][pitch] (pitch a multiple of
- * 32, >= nx), mask uint8[nz][ny][pitch].  model: 0 MRT (LR7 mrt_collide),
- * 1 MRT with bgk_meq (DynInlet3), 2 BGK, 3 CPU_3D MRT.  les != 0 folds the
- * Smagorinsky eddy viscosity into tau (cs is the reference's CS).  When
- * force_out != NULL the FP64 momentum-exchange force of this step is ADDED to
- * force_out[0..2] (device memory); scratch must then hold
- * lbm_force_scratch_doubles(nx, ny, nz, pitch) doubles of device memory. */
+ * 32, >= nx, 19*nz*ny*pitch < 2^31), mask uint8[nz][ny][pitch] of lbm_node
+ * values.  model: 0 MRT (LR7 mrt_collide), 1 MRT with bgk_meq (DynInlet3),
+ * 2 BGK, 3 CPU_3D MRT.  les != 0 folds the Smagorinsky eddy viscosity into
+ * tau (cs is the reference's CS).  Enqueued on cuda_stream (NULL: default). */
 int lbm_stream_collide_f32(const float* fA, float* fB, const uint8_t* mask, int nx, int ny, int nz, int pitch,
                            int model, int les, float omega, float cs, float u_in, float rho_out, int t,
-                           double* force_out, double* scratch, void* cuda_stream);
-size_t lbm_force_scratch_doubles(int nx, int ny, int nz, int pitch);
+                           void* cuda_stream);
+/* FP64 momentum-exchange force 2 sum_q c_q f_q over the BODY nodes of mask,
+ * pulled from fA (the force the reference sums at LR7:1494-1502 and
+ * 1607-1626 during the step that reads fA).  The three sums are ADDED to
+ * force_out[0..2] (device memory); scratch is device memory of
+ * lbm_body_force_scratch_doubles() doubles; the sum order is fixed, so the
+ * result is reproducible. */
+int lbm_body_force_f32(const float* fA, const uint8_t* mask, int nx, int ny, int nz, int pitch, double* force_out,
+                       double* scratch, void* cuda_stream);
+size_t lbm_body_force_scratch_doubles(void);
 
 #ifdef __cplusplus
 }

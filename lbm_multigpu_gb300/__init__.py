@@ -59,8 +59,9 @@ SIGNATURES = [
     ("lbm_audit", _I, [_P, _I, _P]),
     ("lbm_write_inputs", _I, [_P, ctypes.c_char_p, _SZ, ctypes.POINTER(_SZ)]),
     ("lbm_write_outputs", _I, [_P, ctypes.c_char_p]),
-    ("lbm_stream_collide_f32", _I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _F, _F, _F, _F, _I, _P, _P, _P]),
-    ("lbm_force_scratch_doubles", _SZ, [_I, _I, _I, _I]),
+    ("lbm_stream_collide_f32", _I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _F, _F, _F, _F, _I, _P]),
+    ("lbm_body_force_f32", _I, [_P, _P, _I, _I, _I, _I, _P, _P, _P]),
+    ("lbm_body_force_scratch_doubles", _SZ, []),
 ]
 
 

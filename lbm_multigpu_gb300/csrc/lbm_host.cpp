@@ -401,8 +401,9 @@ struct LevelState {
     uint8_t* mask = nullptr;        /* device, pitched */
     std::vector<uint8_t> hmask;     /* host, compact */
     float* stats = nullptr;         /* device, 4 x qstride */
+    unsigned* body = nullptr;       /* device, pitched indices of BODY nodes */
+    int nbody = 0;
     double* fpart = nullptr;        /* per-block force partials */
-    int nblocks = 0;
 };
 
 }  // namespace
@@ -433,6 +434,7 @@ void free_level(LevelState& s) {
     cudaFree(s.f[1]);
     cudaFree(s.mask);
     cudaFree(s.stats);
+    cudaFree(s.body);
     cudaFree(s.fpart);
     s = LevelState();
 }
@@ -446,7 +448,8 @@ int alloc_level(LevelState& s, int nx, int ny, int nz, int storage, bool stats) 
     L.plane = (long long)L.pitch * ny;
     L.qstride = L.plane * nz;
     L.storage = storage;
-    if (L.qstride * 19 > (1LL << 40)) return fail(LBM_ERR_CONFIG, "level %dx%dx%d too large", nx, ny, nz);
+    if (L.qstride * 19 >= (1LL << 31))
+        return fail(LBM_ERR_CONFIG, "level %dx%dx%d too large: 19 populations must index below 2^31", nx, ny, nz);
     const size_t bytes = size_t(L.qstride) * 19 * storage_bytes(storage);
     for (int i = 0; i < 2; ++i) {
         CUDA_TRY(cudaMalloc(&s.f[i], bytes));
@@ -458,8 +461,7 @@ int alloc_level(LevelState& s, int nx, int ny, int nz, int storage, bool stats) 
         CUDA_TRY(cudaMalloc(&s.stats, size_t(L.qstride) * 4 * sizeof(float)));
         CUDA_TRY(cudaMemset(s.stats, 0, size_t(L.qstride) * 4 * sizeof(float)));
     }
-    s.nblocks = sc_blocks(L);
-    CUDA_TRY(cudaMalloc(&s.fpart, size_t(s.nblocks) * 3 * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&s.fpart, size_t(force_partials()) * 3 * sizeof(double)));
     return LBM_OK;
 }
 
@@ -470,8 +472,18 @@ int upload_mask(lbm_handle* h, int level) {
     for (int z = 0; z < L.nz; ++z)
         for (int y = 0; y < L.ny; ++y)
             memcpy(&pitched[size_t(z) * L.plane + size_t(y) * L.pitch], &s.hmask[(size_t(z) * L.ny + y) * L.nx], L.nx);
+    std::vector<unsigned> body;
+    for (size_t i = 0; i < pitched.size(); ++i)
+        if (pitched[i] == BODY) body.push_back(unsigned(i));
     CUDA_TRY(cudaMemcpyAsync(s.mask, pitched.data(), pitched.size(), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
+    cudaFree(s.body);
+    s.body = nullptr;
+    s.nbody = int(body.size());
+    if (!body.empty()) {
+        CUDA_TRY(cudaMalloc(&s.body, body.size() * sizeof(unsigned)));
+        CUDA_TRY(cudaMemcpy(s.body, body.data(), body.size() * sizeof(unsigned), cudaMemcpyHostToDevice));
+    }
     return LBM_OK;
 }
 
@@ -552,8 +564,9 @@ int one_step(lbm_handle* h) {
         int rc = ensure_force_cap(h, fidx + 1);
         if (rc) return rc;
     }
-    CUDA_TRY(launch_stream_collide(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.fpart, C.stats, h->mom, h->stream));
-    if (p.force_on) CUDA_TRY(launch_reduce_force(C.fpart, C.nblocks, h->force_hist + 3LL * fidx, h->stream));
+    if (p.force_on)
+        CUDA_TRY(launch_force(C.L, C.f[C.cur], C.body, C.nbody, C.fpart, h->force_hist + 3LL * fidx, h->stream));
+    CUDA_TRY(launch_stream_collide(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, h->mom, h->stream));
     C.cur = 1 - C.cur;
     if (c.refinement) {
         LevelState& Fn = h->lv[1];
@@ -566,9 +579,11 @@ int one_step(lbm_handle* h) {
                 int rc = ensure_force_cap(h, fidx + 1);
                 if (rc) return rc;
             }
-            CUDA_TRY(launch_stream_collide(Fn.L, pf, Fn.f[Fn.cur], Fn.f[1 - Fn.cur], Fn.mask, Fn.fpart, Fn.stats,
-                                           nullptr, h->stream));
-            if (pf.force_on) CUDA_TRY(launch_reduce_force(Fn.fpart, Fn.nblocks, h->force_hist + 3LL * fidx, h->stream));
+            if (pf.force_on)
+                CUDA_TRY(launch_force(Fn.L, Fn.f[Fn.cur], Fn.body, Fn.nbody, Fn.fpart, h->force_hist + 3LL * fidx,
+                                      h->stream));
+            CUDA_TRY(launch_stream_collide(Fn.L, pf, Fn.f[Fn.cur], Fn.f[1 - Fn.cur], Fn.mask, Fn.stats, nullptr,
+                                           h->stream));
             Fn.cur = 1 - Fn.cur;
         }
         CUDA_TRY(launch_interp_cf(h->rp, Fn.L, h->mom, Fn.f[Fn.cur], Fn.mask, h->stream));
@@ -1024,23 +1039,9 @@ int lbm_write_outputs(lbm_handle* h, const char* casename) {
 
 /* ---- kernel-level API ---- */
 
-size_t lbm_force_scratch_doubles(int nx, int ny, int nz, int pitch) {
-    Level L{};
-    L.nx = nx;
-    L.ny = ny;
-    L.nz = nz;
-    L.pitch = pitch;
-    return size_t(sc_blocks(L)) * 3;
-}
-
-int lbm_stream_collide_f32(const float* fA, float* fB, const uint8_t* mask, int nx, int ny, int nz, int pitch, int model,
-                           int les, float omega, float cs, float u_in, float rho_out, int t, double* force_out,
-                           double* scratch, void* cuda_stream) {
-    if (!fA || !fB || !mask || fA == fB) return fail(LBM_ERR_ARG, "bad buffer pointers");
+static int kernel_level(Level& L, int nx, int ny, int nz, int pitch) {
     if (nx < 1 || ny < 1 || nz < 1 || pitch < nx || pitch % 32) return fail(LBM_ERR_ARG, "bad dimensions or pitch");
-    if (model < 0 || model > 3) return fail(LBM_ERR_ARG, "model %d unknown", model);
-    if (force_out && !scratch) return fail(LBM_ERR_ARG, "force_out needs scratch");
-    Level L{};
+    L = Level{};
     L.nx = nx;
     L.ny = ny;
     L.nz = nz;
@@ -1048,6 +1049,16 @@ int lbm_stream_collide_f32(const float* fA, float* fB, const uint8_t* mask, int 
     L.plane = (long long)pitch * ny;
     L.qstride = L.plane * nz;
     L.storage = STORE_F32;
+    if (L.qstride * 19 >= (1LL << 31)) return fail(LBM_ERR_ARG, "level too large: 19 populations must index below 2^31");
+    return LBM_OK;
+}
+
+int lbm_stream_collide_f32(const float* fA, float* fB, const uint8_t* mask, int nx, int ny, int nz, int pitch, int model,
+                           int les, float omega, float cs, float u_in, float rho_out, int t, void* cuda_stream) {
+    if (!fA || !fB || !mask || fA == fB) return fail(LBM_ERR_ARG, "bad buffer pointers");
+    if (model < 0 || model > 3) return fail(LBM_ERR_ARG, "model %d unknown", model);
+    Level L;
+    if (int rc = kernel_level(L, nx, ny, nz, pitch)) return rc;
     StepParams p{};
     p.model = model;
     p.les = les;
@@ -1056,11 +1067,19 @@ int lbm_stream_collide_f32(const float* fA, float* fB, const uint8_t* mask, int 
     p.u_in = u_in;
     p.rho_out = rho_out;
     p.t = t;
-    p.force_on = force_out ? 1 : 0;
     p.stats_weight = 1.f;
-    cudaStream_t s = (cudaStream_t)cuda_stream;
-    CUDA_TRY(launch_stream_collide(L, p, fA, fB, mask, scratch, nullptr, nullptr, s));
-    if (force_out) CUDA_TRY(launch_reduce_force(scratch, sc_blocks(L), force_out, s));
+    CUDA_TRY(launch_stream_collide(L, p, fA, fB, mask, nullptr, nullptr, (cudaStream_t)cuda_stream));
+    return LBM_OK;
+}
+
+size_t lbm_body_force_scratch_doubles(void) { return size_t(force_scan_partials()) * 3; }
+
+int lbm_body_force_f32(const float* fA, const uint8_t* mask, int nx, int ny, int nz, int pitch, double* force_out,
+                       double* scratch, void* cuda_stream) {
+    if (!fA || !mask || !force_out || !scratch) return fail(LBM_ERR_ARG, "null device pointer");
+    Level L;
+    if (int rc = kernel_level(L, nx, ny, nz, pitch)) return rc;
+    CUDA_TRY(launch_force_scan(L, fA, mask, scratch, force_out, (cudaStream_t)cuda_stream));
     return LBM_OK;
 }
 

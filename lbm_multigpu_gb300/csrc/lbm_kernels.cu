@@ -53,7 +53,6 @@ template <class S>
 __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, const StepParams p,
                                                                   const S* __restrict__ fA, S* __restrict__ fB,
                                                                   const uint8_t* __restrict__ mask,
-                                                                  double* __restrict__ fpart,
                                                                   float* __restrict__ stats,
                                                                   float* __restrict__ mom_export) {
     using F = Fmt<S>;
@@ -61,134 +60,150 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
     const int x = blockIdx.x * SC_BX + threadIdx.x;
     const int y = blockIdx.y * SC_BY + threadIdx.y;
     const int z = blockIdx.z;
-    const bool active = (x < L.nx) && (y < L.ny);
-    double fsx = 0.0, fsy = 0.0, fsz = 0.0;
+    if (x >= L.nx || y >= L.ny) return;
+    /* 32-bit element offsets: a level holds fewer than 2^31 elements per
+     * buffer (checked at allocation) */
+    const unsigned qs = unsigned(L.qstride);
+    const unsigned plane = unsigned(L.plane), pitch = unsigned(L.pitch);
+    const unsigned c = z * plane + y * pitch + x;
+    const int type = mask[c];
+    /* periodic neighbours; only boundary nodes, whose pulled values the
+     * reference discards or bounces, ever wrap in x or y */
+    const unsigned xm = (x == 0) ? L.nx - 1 : x - 1;
+    const unsigned xp = (x == L.nx - 1) ? 0 : x + 1;
+    const unsigned ym = (y == 0) ? L.ny - 1 : y - 1;
+    const unsigned yp = (y == L.ny - 1) ? 0 : y + 1;
+    const unsigned zm = (z == 0) ? L.nz - 1 : z - 1;
+    const unsigned zp = (z == L.nz - 1) ? 0 : z + 1;
+    const unsigned zb[3] = {zm * plane, z * plane, zp * plane};
+    const unsigned yb[3] = {ym * pitch, y * pitch, yp * pitch};
+    const unsigned xs[3] = {xm, unsigned(x), xp};
 
-    if (active) {
-        const long long qs = L.qstride;
-        const long long c = z * L.plane + (long long)y * L.pitch + x;
-        const int type = mask[c];
-        /* periodic neighbours; only boundary nodes, whose pulled values the
-         * reference discards or bounces, ever wrap in x or y */
-        const int xm = (x == 0) ? L.nx - 1 : x - 1;
-        const int xp = (x == L.nx - 1) ? 0 : x + 1;
-        const int ym = (y == 0) ? L.ny - 1 : y - 1;
-        const int yp = (y == L.ny - 1) ? 0 : y + 1;
-        const int zm = (z == 0) ? L.nz - 1 : z - 1;
-        const int zp = (z == L.nz - 1) ? 0 : z + 1;
+    T f[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        /* pull: the value arriving from x - c_q */
+        const unsigned src = q * qs + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)];
+        f[q] = F::ld(fA + src, q);
+    }
+
+    if (type == WALL || type == BODY) {
+        /* full-way bounce-back (LR7:1493-1526); the momentum exchange of BODY
+         * nodes is summed by k_force_list from the same fA */
+#pragma unroll
+        for (int q = 0; q < 19; ++q) F::st(fB + q * qs + c, f[opp(q)], q);
+    } else {
+        if (type >= WEST_INLET && type <= NORTH_OUTLET) {
+            /* rebuild from the neighbour's stored post-collision state */
+            unsigned nb;
+            if (type == WEST_INLET) nb = zb[1] + yb[1] + xp;
+            else if (type == EAST_OUTLET) nb = zb[1] + yb[1] + xm;
+            else if (type == SOUTH_INLET) nb = zb[1] + yb[2] + x;
+            else nb = zb[1] + yb[0] + x;
+#pragma unroll
+            for (int q = 0; q < 19; ++q) f[q] = F::ld(fA + q * qs + nb, q);
+            T uin = T(p.u_in);
+            if (p.noise_amp != 0.f) {
+                const uint32_t cell = uint32_t((z * L.ny + y) * L.nx + x);
+                const float xi = philox_uniform(p.noise_seed, cell, uint32_t(p.t));
+                uin = uin + T(p.u_in) * T(p.noise_amp) * (T(2) * T(xi) - T(1));
+            }
+            extrap<T>(type, f, T(p.rho_out), uin);
+        } else if (type == LID) {
+            lid<T>(f, p.lid_face, T(p.lid_u[0]), T(p.lid_u[1]), T(p.lid_u[2]));
+        }
+        collide<T>(p.model, f, T(p.omega), p.les != 0, T(p.cs), T(p.dpdy));
+
+        if (p.stats_on && p.t >= p.start_av) {
+            /* vel_av / vel_fluc (LR7:1018-1058): running mean, then variance */
+            T u = 0, v = 0;
+#pragma unroll
+            for (int q = 0; q < 19; ++q) {
+                if (cx(q)) u += T(cx(q)) * f[q];
+                if (cy(q)) v += T(cy(q)) * f[q];
+            }
+            float* au = stats;
+            float* av = stats + qs;
+            const float w = p.stats_weight;
+            if (p.t < p.start_fluc) {
+                const float n = float(p.t - p.start_av);
+                au[c] = (au[c] * n + float(u) * w) / (n + w);
+                av[c] = (av[c] * n + float(v) * w) / (n + w);
+            } else {
+                float* fu = stats + 2 * (size_t)qs;
+                float* fv = stats + 3 * (size_t)qs;
+                const float n = float(p.t - p.start_fluc);
+                const float du = (float(u) - au[c]) * (float(u) - au[c]);
+                const float dv = (float(v) - av[c]) * (float(v) - av[c]);
+                fu[c] = (fu[c] * n + du * w) / (n + w);
+                fv[c] = (fv[c] * n + dv * w) / (n + w);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 19; ++q) F::st(fB + q * qs + c, f[q], q);
+    }
+
+    if (p.exp_nx > 0) {
+        /* moments for the coarse->fine interpolation (LR7:1590-1605):
+         * post-collision for fluid nodes, the pulled values at bounce-back nodes */
+        const int ex = x - p.exp_x0, ey = y - p.exp_y0;
+        if (ex >= 0 && ex < p.exp_nx && ey >= 0 && ey < p.exp_ny) {
+            float ff[19], mom[9];
+#pragma unroll
+            for (int q = 0; q < 19; ++q) ff[q] = float(f[q]);
+            physical_moments<float>(ff, mom);
+            const unsigned ne = unsigned(p.exp_nx * p.exp_ny * L.nz);
+            const unsigned ce = (unsigned(z) * p.exp_ny + ey) * p.exp_nx + ex;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) mom_export[i * ne + ce] = mom[i];
+        }
+    }
+}
+
+/* Momentum exchange at BODY nodes (LR7:1494-1502, reduced per block at
+ * LR7:1607-1626): F += 2 sum_q c_q f_q over the populations a body node pulls
+ * from fA.  Runs over a compact list of body nodes (pitched indices) instead
+ * of inside the stream-collide kernel, so the hot kernel carries no FP64 and no
+ * block barrier; per-block FP64 partials are summed in a fixed order. */
+constexpr int FORCE_BLOCKS = 64, FORCE_THREADS = 256;
+template <class S>
+__global__ void __launch_bounds__(FORCE_THREADS) k_force_list(const Level L, const S* __restrict__ fA,
+                                                              const unsigned* __restrict__ body, int nbody,
+                                                              double* __restrict__ part) {
+    using F = Fmt<S>;
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int i = blockIdx.x * FORCE_THREADS + threadIdx.x; i < nbody; i += FORCE_BLOCKS * FORCE_THREADS) {
+        const unsigned c = body[i];
+        const int z = int(c / unsigned(L.plane));
+        const unsigned r = c - unsigned(z) * unsigned(L.plane);
+        const int y = int(r / unsigned(L.pitch)), x = int(r - unsigned(y) * unsigned(L.pitch));
+        const int xm = (x == 0) ? L.nx - 1 : x - 1, xp = (x == L.nx - 1) ? 0 : x + 1;
+        const int ym = (y == 0) ? L.ny - 1 : y - 1, yp = (y == L.ny - 1) ? 0 : y + 1;
+        const int zm = (z == 0) ? L.nz - 1 : z - 1, zp = (z == L.nz - 1) ? 0 : z + 1;
         const long long zb[3] = {zm * L.plane, z * L.plane, zp * L.plane};
         const long long yb[3] = {(long long)ym * L.pitch, (long long)y * L.pitch, (long long)yp * L.pitch};
         const int xs[3] = {xm, x, xp};
-
-        T f[19];
 #pragma unroll
-        for (int q = 0; q < 19; ++q) {
-            /* pull: the value arriving from x - c_q */
-            const long long src = zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)];
-            f[q] = F::ld(fA + q * qs + src, q);
-        }
-
-        if (type == WALL || type == BODY) {
-            if (type == BODY && p.force_on) {
-#pragma unroll
-                for (int q = 1; q < 19; ++q) {
-                    const double v = 2.0 * double(f[q]);
-                    if (cx(q)) fsx += cx(q) * v;
-                    if (cy(q)) fsy += cy(q) * v;
-                    if (cz(q)) fsz += cz(q) * v;
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < 19; ++q) F::st(fB + q * qs + c, f[opp(q)], q);
-        } else {
-            if (type >= WEST_INLET && type <= NORTH_OUTLET) {
-                /* rebuild from the neighbour's stored post-collision state */
-                long long nb = c;
-                if (type == WEST_INLET) nb = zb[1] + yb[1] + xp;
-                else if (type == EAST_OUTLET) nb = zb[1] + yb[1] + xm;
-                else if (type == SOUTH_INLET) nb = zb[1] + yb[2] + x;
-                else nb = zb[1] + yb[0] + x;
-#pragma unroll
-                for (int q = 0; q < 19; ++q) f[q] = F::ld(fA + q * qs + nb, q);
-                T uin = T(p.u_in);
-                if (p.noise_amp != 0.f) {
-                    const uint32_t cell = uint32_t((z * L.ny + y) * L.nx + x);
-                    const float xi = philox_uniform(p.noise_seed, cell, uint32_t(p.t));
-                    uin = uin + T(p.u_in) * T(p.noise_amp) * (T(2) * T(xi) - T(1));
-                }
-                extrap<T>(type, f, T(p.rho_out), uin);
-            } else if (type == LID) {
-                lid<T>(f, p.lid_face, T(p.lid_u[0]), T(p.lid_u[1]), T(p.lid_u[2]));
-            }
-            collide<T>(p.model, f, T(p.omega), p.les != 0, T(p.cs), T(p.dpdy));
-
-            if (p.stats_on && p.t >= p.start_av) {
-                /* vel_av / vel_fluc (LR7:1018-1058): running mean, then variance */
-                T u = 0, v = 0;
-#pragma unroll
-                for (int q = 0; q < 19; ++q) {
-                    if (cx(q)) u += T(cx(q)) * f[q];
-                    if (cy(q)) v += T(cy(q)) * f[q];
-                }
-                const long long ns = L.qstride;
-                float* au = stats;
-                float* av = stats + ns;
-                const float w = p.stats_weight;
-                if (p.t < p.start_fluc) {
-                    const float n = float(p.t - p.start_av);
-                    au[c] = (au[c] * n + float(u) * w) / (n + w);
-                    av[c] = (av[c] * n + float(v) * w) / (n + w);
-                } else {
-                    float* fu = stats + 2 * ns;
-                    float* fv = stats + 3 * ns;
-                    const float n = float(p.t - p.start_fluc);
-                    const float du = (float(u) - au[c]) * (float(u) - au[c]);
-                    const float dv = (float(v) - av[c]) * (float(v) - av[c]);
-                    fu[c] = (fu[c] * n + du * w) / (n + w);
-                    fv[c] = (fv[c] * n + dv * w) / (n + w);
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < 19; ++q) F::st(fB + q * qs + c, f[q], q);
-        }
-
-        if (p.exp_nx > 0) {
-            const int ex = x - p.exp_x0, ey = y - p.exp_y0;
-            if (ex >= 0 && ex < p.exp_nx && ey >= 0 && ey < p.exp_ny) {
-                float ff[19], mom[9];
-#pragma unroll
-                for (int q = 0; q < 19; ++q) ff[q] = float(f[q]);
-                physical_moments<float>(ff, mom);
-                const long long ne = (long long)p.exp_nx * p.exp_ny * L.nz;
-                const long long ce = ((long long)z * p.exp_ny + ey) * p.exp_nx + ex;
-#pragma unroll
-                for (int i = 0; i < 9; ++i) mom_export[i * ne + ce] = mom[i];
-            }
+        for (int q = 1; q < 19; ++q) {
+            const double v = 2.0 * double(F::ld(fA + q * L.qstride + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)], q));
+            if (cx(q)) s[0] += cx(q) * v;
+            if (cy(q)) s[1] += cy(q) * v;
+            if (cz(q)) s[2] += cz(q) * v;
         }
     }
-
-    if (p.force_on) {
-        /* deterministic block sum in FP64: warp shuffles, then one warp */
-        __shared__ double red[SC_BY][3];
+    __shared__ double red[3][FORCE_THREADS / 32];
+    for (int k = 0; k < 3; ++k) {
+        double v = s[k];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            fsx += __shfl_down_sync(0xffffffffu, fsx, o);
-            fsy += __shfl_down_sync(0xffffffffu, fsy, o);
-            fsz += __shfl_down_sync(0xffffffffu, fsz, o);
-        }
-        if (threadIdx.x == 0) {
-            red[threadIdx.y][0] = fsx;
-            red[threadIdx.y][1] = fsy;
-            red[threadIdx.y][2] = fsz;
-        }
-        __syncthreads();
-        if (threadIdx.y == 0 && threadIdx.x < 3) {
-            double s = 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double v = 0.0;
 #pragma unroll
-            for (int w = 0; w < SC_BY; ++w) s += red[w][threadIdx.x];
-            const long long b = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-            fpart[b * 3 + threadIdx.x] = s;
-        }
+        for (int w = 0; w < FORCE_THREADS / 32; ++w) v += red[threadIdx.x][w];
+        part[3 * blockIdx.x + threadIdx.x] = v;
     }
 }
 
@@ -533,15 +548,76 @@ __global__ void k_interp_fc(const RefineParams r, const Level C, const Level F, 
     }
 
 cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const void* fA, void* fB, const uint8_t* mask,
-                                  double* force_partials, float* stats, float* mom_export, cudaStream_t s) {
+                                  float* stats, float* mom_export, cudaStream_t s) {
     const dim3 block(SC_BX, SC_BY), grid = sc_grid(L);
-    LBM_DISPATCH(L.storage, (k_stream_collide<S><<<grid, block, 0, s>>>(L, p, (const S*)fA, (S*)fB, mask,
-                                                                         force_partials, stats, mom_export)));
+    LBM_DISPATCH(L.storage, (k_stream_collide<S><<<grid, block, 0, s>>>(L, p, (const S*)fA, (S*)fB, mask, stats,
+                                                                         mom_export)));
     return cudaGetLastError();
 }
 
-cudaError_t launch_reduce_force(const double* partials, int n, double* out3, cudaStream_t s) {
-    k_reduce3<<<1, 1024, 0, s>>>(partials, n, out3);
+int force_partials() { return FORCE_BLOCKS; }
+
+cudaError_t launch_force(const Level& L, const void* fA, const unsigned* body, int nbody, double* partials,
+                         double* out3, cudaStream_t s) {
+    if (nbody <= 0) return cudaSuccess;
+    LBM_DISPATCH(L.storage, (k_force_list<S><<<FORCE_BLOCKS, FORCE_THREADS, 0, s>>>(L, (const S*)fA, body, nbody,
+                                                                                    partials)));
+    k_reduce3<<<1, 64, 0, s>>>(partials, FORCE_BLOCKS, out3);
+    return cudaGetLastError();
+}
+
+/* momentum exchange by scanning the mask (the kernel-level API has no body
+ * list): grid-stride over rows, FP64 per-block partials, fixed-order sum */
+constexpr int SCAN_BLOCKS = 1216; /* 8 blocks per SM on a 152-SM GB300 */
+template <class S>
+__global__ void __launch_bounds__(256) k_force_scan(const Level L, const S* __restrict__ fA,
+                                                    const uint8_t* __restrict__ mask, double* __restrict__ part) {
+    using F = Fmt<S>;
+    double s[3] = {0.0, 0.0, 0.0};
+    const long long rows = (long long)L.ny * L.nz;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (long long r = (long long)blockIdx.x * 8 + warp; r < rows; r += (long long)gridDim.x * 8) {
+        const int y = int(r % L.ny), z = int(r / L.ny);
+        for (int x = lane; x < L.nx; x += 32) {
+            if (mask[z * L.plane + (long long)y * L.pitch + x] != BODY) continue;
+            const int xm = (x == 0) ? L.nx - 1 : x - 1, xp = (x == L.nx - 1) ? 0 : x + 1;
+            const int ym = (y == 0) ? L.ny - 1 : y - 1, yp = (y == L.ny - 1) ? 0 : y + 1;
+            const int zm = (z == 0) ? L.nz - 1 : z - 1, zp = (z == L.nz - 1) ? 0 : z + 1;
+            const long long zb[3] = {zm * L.plane, z * L.plane, zp * L.plane};
+            const long long yb[3] = {(long long)ym * L.pitch, (long long)y * L.pitch, (long long)yp * L.pitch};
+            const int xs[3] = {xm, x, xp};
+#pragma unroll
+            for (int q = 1; q < 19; ++q) {
+                const double v =
+                    2.0 * double(F::ld(fA + q * L.qstride + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)], q));
+                if (cx(q)) s[0] += cx(q) * v;
+                if (cy(q)) s[1] += cy(q) * v;
+                if (cz(q)) s[2] += cz(q) * v;
+            }
+        }
+    }
+    __shared__ double red[3][8];
+    for (int k = 0; k < 3; ++k) {
+        double v = s[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double v = 0.0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) v += red[threadIdx.x][w];
+        part[3 * blockIdx.x + threadIdx.x] = v;
+    }
+}
+
+int force_scan_partials() { return SCAN_BLOCKS; }
+
+cudaError_t launch_force_scan(const Level& L, const void* fA, const uint8_t* mask, double* partials, double* out3,
+                              cudaStream_t s) {
+    LBM_DISPATCH(L.storage, (k_force_scan<S><<<SCAN_BLOCKS, 256, 0, s>>>(L, (const S*)fA, mask, partials)));
+    k_reduce3<<<1, 1024, 0, s>>>(partials, SCAN_BLOCKS, out3);
     return cudaGetLastError();
 }
 

@@ -65,9 +65,15 @@ inline int sc_blocks(const Level& L) {
 
 /* kernel launchers (lbm_kernels.cu) */
 cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const void* fA, void* fB,
-                                  const uint8_t* mask, double* force_partials, float* stats,
-                                  float* mom_export, cudaStream_t s);
-cudaError_t launch_reduce_force(const double* partials, int n, double* out3, cudaStream_t s);
+                                  const uint8_t* mask, float* stats, float* mom_export, cudaStream_t s);
+/* FP64 momentum exchange over a list of BODY nodes (pitched indices), ADDED to out3 */
+cudaError_t launch_force(const Level& L, const void* fA, const unsigned* body, int nbody, double* partials,
+                         double* out3, cudaStream_t s);
+int force_partials();
+/* the same sum found by scanning the mask; partials holds force_scan_partials()*3 doubles */
+cudaError_t launch_force_scan(const Level& L, const void* fA, const uint8_t* mask, double* partials, double* out3,
+                              cudaStream_t s);
+int force_scan_partials();
 cudaError_t launch_init(const Level& L, const uint8_t* mask, void* f, int kind, float u0, cudaStream_t s);
 cudaError_t launch_fields(const Level& L, const void* f, float* rho, float* u, float* v, float* w, cudaStream_t s);
 cudaError_t launch_pack(const Level& L, const void* f, float* compact, cudaStream_t s);
