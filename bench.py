@@ -1,0 +1,360 @@
+"""Throughput benchmark of the D3Q19 stream-collide path on GB300.
+
+Workload (the channel configuration the metric is quoted on): D3Q19 MRT with
+Smagorinsky LES (Cs^2 = CS = 0.01), 512x128x128 nodes, tau0 = 0.52
+(RE = 3*UMAX*D/(tau0-0.5) = 120, D = 16), inlet u = 0.05 with 1 % seeded
+per-node-per-step noise, zero-gradient outlet, periodic z, no-slip y walls,
+a square cylinder of side 16 nodes at x = 128; the reference's momentum
+exchange drag/lift is computed every step.  Synthetic inputs: the flow starts
+from the equilibrium at the inlet velocity, as the reference initialises it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+One JSON line on rank 0.  `value` is whole-job MLUPS with the populations
+resident in HBM (N GPUs run N independent replicas: the build is single-GPU,
+the metric scales weakly); `e2e` is the same run driven through the public
+API from pinned host buffers (initial populations in, every step's force out,
+final populations out, all inside the timed region); `roofline` is the
+dominant kernel (stream-collide) against the measured HBM copy bandwidth;
+`cpu_baseline` times the reference's own CPU code (CPU_3D/CPU_3D.cpp, staged
+and built by oracle/ref_recipe.py) on a bounded sample of the same shape.
+`--impl reference` times that CPU program alone (the reference arm).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NX, NY, NZ = 512, 128, 128
+CELLS = NX * NY * NZ
+BYTES_PER_CELL = {"fp32": 152, "fp16": 76, "bf16": 76, "fp64": 304}
+WORKLOAD = ("D3Q19 MRT+Smagorinsky channel 512x128x128, square cylinder side 16 at x=128, tau0=0.52 (RE=120), "
+            "CS=0.01 (Cs=0.1), inlet 0.05 + 1% seeded noise, periodic z, drag/lift every step")
+
+
+def inputs_text(precision: str, tmax: int) -> str:
+    import lbm_multigpu_gb300 as lbm
+
+    return lbm.make_inputs(NX, NY, NZ, obst1=(128.5, 63.5, 0.0), r1=8.0, re=120.0, umax=0.05, tmax=tmax, les=1,
+                           cs=0.01, model="MRT", geometry="channel_square", precision=precision, inlet_noise=0.01,
+                           seed=12345)
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return dict(hbm_gbs=float(d["hbm_gbs"]), src="measured")
+    return dict(hbm_gbs=6800.0, src="fallback")
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region"""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.15)
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(name)
+        return dict(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=mx, reasons=sorted(reasons),
+                    samples=len(sm))
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def time_precision(precision: str, steps: int, warmup: int, world: int, dist, with_clocks: bool, gpu: int):
+    """resident-in-HBM run of `steps` steps after `warmup`; returns (ms, clocks)"""
+    import lbm_multigpu_gb300 as lbm
+
+    s = lbm.Solver(inputs_text(precision, warmup + steps + 10))
+    s.step(warmup)
+    s.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = None
+    if with_clocks:
+        with ClockSampler(gpu) as cs:
+            ms = s.step_timed(steps)
+        clocks = cs.summary()
+    else:
+        ms = s.step_timed(steps)
+    if dist:
+        dist.barrier()
+    kernel_ms = s.time_stream_collide(20)
+    audit = s.audit()
+    s.close()
+    return ms, kernel_ms, clocks, audit
+
+
+def time_e2e(steps: int, world: int, dist) -> dict:
+    """the same workload through the public API with host buffers in the
+    timed region: pinned initial populations in, each step's force out,
+    final populations out"""
+    import numpy as np
+    import torch
+
+    import lbm_multigpu_gb300 as lbm
+
+    s = lbm.Solver(inputs_text("fp32", steps + 10))
+    f0 = s.populations()
+    host_in = torch.empty(f0.shape, dtype=torch.float32, pin_memory=True).numpy()
+    host_in[...] = f0
+    host_out = torch.empty(f0.shape, dtype=torch.float32, pin_memory=True).numpy()
+    force = np.zeros((steps, 3))
+    s.init_equilibrium()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    s.set_populations(host_in)
+    for i in range(steps):
+        s.step(1)
+        force[i] = s.last_force()
+    host_out[...] = s.populations()
+    t1 = time.perf_counter()
+    if dist:
+        dist.barrier()
+    s.close()
+    sec = t1 - t0
+    h2d = host_in.nbytes / steps
+    d2h = (host_out.nbytes + steps * 24) / steps
+    return dict(sec=sec, h2d=h2d, d2h=d2h, finite=bool(np.isfinite(force).all()))
+
+
+def cpu3d_binary() -> Path | None:
+    for name in ("cpu3d_c2_long", "cpu3d_c2"):
+        p = ROOT / "oracle" / "_ref" / name
+        if p.exists() and os.access(p, os.X_OK):
+            return p
+    return None
+
+
+def run_cpu3d(binary: Path) -> tuple[float, float]:
+    """the reference CPU program at the 512x128x128 shape; its own MLUPS print"""
+    r = subprocess.run([str(binary)], capture_output=True, text=True, timeout=600, cwd=str(binary.parent))
+    m = re.search(r"Time taken for main kernel: ([0-9.eE+-]+) \(([0-9.eE+-]+)MLUPS\)", r.stdout)
+    if not m:
+        raise RuntimeError("CPU_3D did not report MLUPS: " + r.stdout[-300:] + r.stderr[-300:])
+    return float(m.group(2)), float(m.group(1))
+
+
+def cpu_baseline(max_samples: int = 1) -> dict:
+    """reference CPU_3D (serial) if staged and built, else the oracle port"""
+    binary = cpu3d_binary()
+    if binary is not None:
+        vals, secs = [], 0.0
+        for _ in range(max(1, max_samples)):
+            v, sec = run_cpu3d(binary)
+            vals.append(v)
+            secs += sec
+        steps = 24 if binary.name.endswith("long") else 8
+        return dict(value=statistics.mean(vals), unit="MLUPS", cores=1, kind="reference",
+                    sample=f"CPU_3D/CPU_3D.cpp (staged, g++ -O3 -march=native), 512x128x128, {steps} steps "
+                           f"x {len(vals)} run(s), {secs:.1f} s of loop time; its lid-cavity MRT at the same shape")
+    sys.path.insert(0, str(ROOT / "tests"))
+    import numpy as np
+
+    import lbm_multigpu_gb300 as lbm
+    from oracle_bindings import OracleRun, oracle
+
+    mask = lbm.inputs_mask(inputs_text("fp32", 10)).reshape(NZ, NY, NX)
+    o = OracleRun(NX, NY, NZ, mask, 1 / 0.52, model=0, les=1, cs=0.01, u_in=0.05, init_u=0.05, noise_amp=0.01)
+    o.step(1)
+    n = 3
+    t0 = time.perf_counter()
+    o.step(n)
+    sec = time.perf_counter() - t0
+    assert np.isfinite(o.fa).all()
+    return dict(value=CELLS * n / sec / 1e6, unit="MLUPS", cores=int(oracle().orc_num_threads()), kind="port",
+                sample=f"oracle restatement (OpenMP), 512x128x128, {n} steps, {sec:.1f} s")
+
+
+def reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    binary = cpu3d_binary()
+    samples = max(1, min(args.steps, 3))
+    if binary is None:
+        base = cpu_baseline()
+        line = dict(metric="MLUPS", value=base["value"], unit="MLUPS", impl="reference", n_gpus=args.gpus,
+                    steps=args.steps, warmup=args.warmup, higher_is_better=True, scaling="weak",
+                    config=dict(workload=WORKLOAD), cpu_baseline=base,
+                    e2e=dict(value=base["value"], unit="MLUPS", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+        print(json.dumps(line))
+        return
+    for _ in range(min(args.warmup, 1)):
+        run_cpu3d(binary)
+    vals, secs = [], 0.0
+    for _ in range(samples):
+        v, sec = run_cpu3d(binary)
+        vals.append(v)
+        secs += sec
+    steps = 24 if binary.name.endswith("long") else 8
+    value = statistics.mean(vals)
+    base = dict(value=value, unit="MLUPS", cores=1, kind="reference",
+                sample=f"CPU_3D/CPU_3D.cpp (serial, g++ -O3 -march=native), 512x128x128, {steps} steps x "
+                       f"{samples} run(s), {secs:.1f} s of loop time")
+    line = dict(metric="MLUPS", value=value, unit="MLUPS", impl="reference", n_gpus=args.gpus, steps=args.steps,
+                warmup=args.warmup, ms_per_step=1e3 * CELLS / (value * 1e6), higher_is_better=True, scaling="weak",
+                vs_baseline=None, dtype="f32", data="synthetic",
+                config=dict(workload=WORKLOAD, note="the reference's only CPU path (CPU_3D, lid-cavity MRT) at "
+                                                    "the channel's shape; one 'step' is one program run"),
+                cpu_baseline=base, e2e=dict(value=value, unit="MLUPS", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--precision", default="all", choices=["all", "fp32", "fp16", "bf16"],
+                    help="storage precisions to time (all: fp32 reference point, then fp16 and bf16)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as td
+
+        td.init_process_group("nccl", device_id=torch.device("cuda", local))
+        dist = td
+    import __graft_entry__
+
+    if rank == 0 or not (ROOT / "lbm_multigpu_gb300" / "_build" / "liblbm_gb300.so").exists():
+        __graft_entry__.build()
+    if dist:
+        dist.barrier()
+    import numpy as np
+
+    # FP32 Smagorinsky (the reference point), then the FP16 / BF16 stores
+    main_prec = "fp32" if args.precision == "all" else args.precision
+    ms32, kms32, clocks, audit = time_precision(main_prec, args.steps, args.warmup, world, dist, True, local)
+    res = {}
+    for prec in (("fp16", "bf16") if args.precision == "all" else ()):
+        ms, kms, _, _ = time_precision(prec, args.steps, args.warmup, world, dist, False, local)
+        res[prec] = (ms, kms)
+
+    def worst(ms):
+        if not dist:
+            return ms
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    ms32 = worst(ms32)
+    for prec in res:
+        res[prec] = (worst(res[prec][0]), res[prec][1])
+    e2e = None if args.no_e2e else time_e2e(min(args.steps, 2000), world, dist)
+    e2e_sec = worst(e2e["sec"]) if e2e else None
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    pk = peaks()
+    mlups = world * CELLS * args.steps / (ms32 * 1e-3) / 1e6
+    kernel_gbs = CELLS * BYTES_PER_CELL[main_prec] / (kms32 * 1e-3) / 1e9
+    traffic = None
+    prof = ROOT / "profiles" / "traffic.json"
+    if prof.exists():
+        traffic = json.loads(prof.read_text()).get(f"k_stream_collide<{main_prec}>")
+    line = dict(
+        metric="MLUPS", value=mlups, unit="MLUPS", n_gpus=world, steps=args.steps, warmup=args.warmup,
+        ms_per_step=ms32 / args.steps, higher_is_better=True, scaling="weak", vs_baseline=None,
+        dtype={"fp32": "f32", "fp16": "f16 storage, f32 math", "bf16": "bf16 storage, f32 math"}[main_prec],
+        data="synthetic (equilibrium start at the inlet velocity, seeded Philox inlet noise)",
+        config=dict(workload=WORKLOAD, parallelism="replicas only" if world > 1 else "single GPU",
+                    cache="inputs >= 0.64 GB per step > 129 MB L2: no flush needed",
+                    precision=f"{main_prec} storage, fp32 math",
+                    forces="FP64 momentum exchange every step"),
+        roofline=dict(bound="hbm", achieved=kernel_gbs, peak=pk["hbm_gbs"], unit="GB/s",
+                      frac=kernel_gbs / pk["hbm_gbs"], traffic=traffic,
+                      peak_src=f"{pk['src']} (MEASURED_PEAKS.json hbm_gbs, burst copy)",
+                      kernel=f"k_stream_collide<{main_prec}>", kernel_ms=kms32,
+                      algorithmic_bytes_per_cell=BYTES_PER_CELL[main_prec]),
+        e2e=None if not e2e else dict(value=world * CELLS * min(args.steps, 2000) / e2e_sec / 1e6, unit="MLUPS",
+                                      h2d_bytes_per_step=e2e["h2d"], d2h_bytes_per_step=e2e["d2h"],
+                                      steps=min(args.steps, 2000)),
+        gpu_launches=args.steps * 3,
+        clocks=clocks,
+        audit=dict(mass=float(audit[0]), momentum=[float(a) for a in audit[1:]]),
+    )
+    for prec, (ms, kms) in res.items():
+        v = world * CELLS * args.steps / (ms * 1e-3) / 1e6
+        gbs = CELLS * BYTES_PER_CELL[prec] / (kms * 1e-3) / 1e9
+        line[f"{prec}_store"] = dict(value=v, ratio_vs_fp32=v / mlups, ms_per_step=ms / args.steps,
+                                     kernel_gbs=gbs, frac=gbs / pk["hbm_gbs"])
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -71,6 +71,11 @@ int lbm_inputs_mask(const char* inputs_text, int level, uint8_t* mask, size_t ca
 int lbm_format_tecplot(const char* inputs_text, int level, const float* f, const float* stats4, char* buf,
                        size_t cap, size_t* len, char* slice, size_t slice_cap, size_t* slice_len);
 
+/* The .force file text (WriteForces, LR7:2537-2545) of a force history
+ * fxyz[3*i + k], i = 0..n-1 for steps STARTF + i, for the record's UMAX,
+ * ZDIM, Obst1 radius and refinement level. */
+int lbm_format_forces(const char* inputs_text, const double* fxyz, int n, char* buf, size_t cap, size_t* len);
+
 /* ---- handle API: the reference program's main() (LR7:2575-3029) ---- */
 
 /* Parse a .inputs record (the text WriteInputs produces, LR7:2547-2573, plus
@@ -114,8 +119,17 @@ int lbm_get_stats(lbm_handle* h, int level, float* stats4);
  * (the reference's FX/FY/FZ arrays, LR7:1607-1626); *n = entries written */
 int lbm_get_forces(lbm_handle* h, double* fxyz, int max_steps, int* n);
 
+/* the force of the last step (3 doubles; zeros before STARTF) */
+int lbm_get_last_force(lbm_handle* h, double* f3);
+
 /* FP64 mass and momentum of the non-solid nodes of a level: out4 = {M, Jx, Jy, Jz} */
 int lbm_audit(lbm_handle* h, int level, double* out4);
+
+/* Profiling: n back-to-back launches of the stream-collide kernel alone on a
+ * level (no force, statistics or refinement work; the populations advance n
+ * steps but the step counter does not), timed with CUDA events on the
+ * handle's stream; *ms = mean duration of one launch. */
+int lbm_time_stream_collide(lbm_handle* h, int level, int n, float* ms);
 
 /* ---- run record and outputs (LR7:2350-2573) ---- */
 

@@ -18,7 +18,7 @@ from pathlib import Path
 
 import numpy as np
 
-__all__ = ["Solver", "LbmError", "library", "make_inputs", "normalize_inputs", "inputs_mask", "format_tecplot", "NODE", "MODELS"]
+__all__ = ["Solver", "LbmError", "library", "make_inputs", "normalize_inputs", "inputs_mask", "format_tecplot", "format_forces", "NODE", "MODELS"]
 
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "_build" / "liblbm_gb300.so"
@@ -39,6 +39,7 @@ SIGNATURES = [
     ("lbm_inputs_mask", _I, [ctypes.c_char_p, _I, _P, _SZ, ctypes.POINTER(_SZ)]),
     ("lbm_format_tecplot", _I, [ctypes.c_char_p, _I, _P, _P, ctypes.c_char_p, _SZ, ctypes.POINTER(_SZ),
                                 ctypes.c_char_p, _SZ, ctypes.POINTER(_SZ)]),
+    ("lbm_format_forces", _I, [ctypes.c_char_p, _P, _I, ctypes.c_char_p, _SZ, ctypes.POINTER(_SZ)]),
     ("lbm_create", _I, [ctypes.c_char_p, ctypes.POINTER(_P)]),
     ("lbm_destroy", _I, [_P]),
     ("lbm_get_dims", _I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
@@ -56,6 +57,8 @@ SIGNATURES = [
     ("lbm_get_fields", _I, [_P, _I, _P, _P, _P, _P]),
     ("lbm_get_stats", _I, [_P, _I, _P]),
     ("lbm_get_forces", _I, [_P, _P, _I, ctypes.POINTER(_I)]),
+    ("lbm_get_last_force", _I, [_P, _P]),
+    ("lbm_time_stream_collide", _I, [_P, _I, _I, ctypes.POINTER(_F)]),
     ("lbm_audit", _I, [_P, _I, _P]),
     ("lbm_write_inputs", _I, [_P, ctypes.c_char_p, _SZ, ctypes.POINTER(_SZ)]),
     ("lbm_write_outputs", _I, [_P, ctypes.c_char_p]),
@@ -138,6 +141,7 @@ def make_inputs(nx: int, ny: int, nz: int, *, obst1=(0.0, 0.0, 0.0), r1=1.0, obs
         ("Obst2 radius:", _fmt(r2)),
         ("RE:", _fmt(re)),
         ("UMAX:", _fmt(umax)),
+        ("omega", ": 0"),  # derived; the library writes the value it computes
     ]
     if dpdy is not None:
         lines.append(("DPDY", ": " + _fmt(dpdy)))
@@ -154,6 +158,7 @@ def make_inputs(nx: int, ny: int, nz: int, *, obst1=(0.0, 0.0, 0.0), r1=1.0, obs
         ("LR factor", _fmt(lr_factor)),
         ("LR location", "x".join(_fmt(v) for v in lr_origin)),
         ("LR blocksize:", "64x1x1"),
+        ("omega in LR", ": 0"),
         ("GPUs per node", ": 1"),
     ]
     names = {"geometry": "GEOMETRY:", "precision": "PRECISION:", "tau": "TAU:", "lid_velocity": "LID velocity:",
@@ -197,6 +202,17 @@ def format_tecplot(text: str, f: np.ndarray, level: int = 0, stats: np.ndarray |
     a, b = ctypes.create_string_buffer(n.value + 1), ctypes.create_string_buffer(m.value + 1)
     _check(lib.lbm_format_tecplot(*args, a, n.value + 1, ctypes.byref(n), b, m.value + 1, ctypes.byref(m)))
     return a.value.decode(), b.value.decode()
+
+
+def format_forces(text: str, forces: np.ndarray) -> str:
+    """.force file text of a per-step force history (n, 3) (no GPU)"""
+    lib = library()
+    F = np.ascontiguousarray(forces, np.float64).reshape(-1, 3)
+    n = _SZ(0)
+    _check(lib.lbm_format_forces(text.encode(), _ptr(F), F.shape[0], None, 0, ctypes.byref(n)))
+    buf = ctypes.create_string_buffer(n.value + 1)
+    _check(lib.lbm_format_forces(text.encode(), _ptr(F), F.shape[0], buf, n.value + 1, ctypes.byref(n)))
+    return buf.value.decode()
 
 
 class Solver:
@@ -305,6 +321,16 @@ class Solver:
         got = _I()
         _check(self._lib.lbm_get_forces(self._h, _ptr(f), n, ctypes.byref(got)))
         return f[: got.value]
+
+    def last_force(self) -> np.ndarray:
+        f = np.zeros(3, np.float64)
+        _check(self._lib.lbm_get_last_force(self._h, _ptr(f)))
+        return f
+
+    def time_stream_collide(self, n: int, level: int = 0) -> float:
+        ms = _F()
+        _check(self._lib.lbm_time_stream_collide(self._h, level, n, ctypes.byref(ms)))
+        return float(ms.value)
 
     def audit(self, level: int = 0) -> np.ndarray:
         o = np.zeros(4, np.float64)

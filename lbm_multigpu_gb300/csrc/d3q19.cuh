@@ -40,12 +40,28 @@ __host__ __device__ constexpr float wq(int q) {
     return q == 0 ? 1.f / 3.f : (q <= 4 || q == 9 || q == 14) ? 1.f / 18.f : 1.f / 36.f;
 }
 
+/* square root and reciprocal of the LES closure: on the device in FP32 the
+ * hardware approximations (a few ulp, far below the FP32 step-to-step
+ * rounding the parity tolerance allows), IEEE otherwise */
+template <class T> __host__ __device__ __forceinline__ T lsqrt(T x) {
+#ifdef __CUDA_ARCH__
+    if constexpr (sizeof(T) == 4) return x > T(0) ? x * rsqrtf(x) : T(0);
+#endif
+    return sqrt(x);
+}
+template <class T> __host__ __device__ __forceinline__ T lrcp(T x) {
+#ifdef __CUDA_ARCH__
+    if constexpr (sizeof(T) == 4) return __fdividef(1.0f, x);
+#endif
+    return T(1) / x;
+}
+
 /* Smagorinsky relaxation (LR7:683-685): tau = tau0/2 + sqrt(tau0^2 + 18 sqrt2 CS Q)/2.
  * The reference's CS enters where the textbook formula has Cs^2. */
 template <class T> __host__ __device__ __forceinline__ T smag_omega(T omega, T cs, T qn) {
-    T tau0 = T(1) / omega;
-    T tau = T(0.5) * tau0 + T(0.5) * sqrt(tau0 * tau0 + T(18) * cs * T(1.4142135623730951) * qn);
-    return T(1) / tau;
+    T tau0 = lrcp(omega);
+    T tau = T(0.5) * tau0 + T(0.5) * lsqrt(tau0 * tau0 + T(18) * cs * T(1.4142135623730951) * qn);
+    return lrcp(tau);
 }
 
 /* Moment-space collision shared by the three MRT flavours.
@@ -108,7 +124,7 @@ __host__ __device__ __forceinline__ void collide_mrt(T f[19], T omega, bool les,
         const T tr = n1 * T(1.0 / 19.0);
         const T pxx = n1 * T(1.0 / 57.0) + n9 * T(1.0 / 3.0);
         const T pyy = T(0.5) * (tr - pxx + n11), pzz = T(0.5) * (tr - pxx - n11);
-        const T qn = sqrt(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (n13 * n13 + n14 * n14 + n15 * n15));
+        const T qn = lsqrt(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (n13 * n13 + n14 * n14 + n15 * n15));
         omega = smag_omega(omega, cs, qn);
     }
     /* relaxation: stress moments with omega, the rest to equilibrium */
@@ -227,7 +243,7 @@ template <class T> __host__ __device__ __forceinline__ void collide_bgk(T f[19],
         pxy -= jx * jy;
         pyz -= jy * jz;
         pxz -= jx * jz;
-        const T qn = sqrt(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (pxy * pxy + pyz * pyz + pxz * pxz));
+        const T qn = lsqrt(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (pxy * pxy + pyz * pyz + pxz * pxz));
         omega = smag_omega(omega, cs, qn);
     }
     const T base = rho - T(1.5) * usq;

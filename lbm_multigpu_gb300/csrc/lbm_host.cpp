@@ -404,6 +404,7 @@ struct LevelState {
     unsigned* body = nullptr;       /* device, pitched indices of BODY nodes */
     int nbody = 0;
     double* fpart = nullptr;        /* per-block force partials */
+    unsigned* done = nullptr;       /* blocks finished in the force kernel (reset by its last block) */
 };
 
 }  // namespace
@@ -436,10 +437,24 @@ void free_level(LevelState& s) {
     cudaFree(s.stats);
     cudaFree(s.body);
     cudaFree(s.fpart);
+    cudaFree(s.done);
     s = LevelState();
 }
 
-int alloc_level(LevelState& s, int nx, int ny, int nz, int storage, bool stats) {
+/* FP16/BF16 offsets: the incompressible equilibrium at rho = 1 and the
+ * reference velocity u0 (the inlet velocity of a channel, rest otherwise) */
+void set_offsets(Level& L, float u0) {
+    static const int CX[19] = {0, 1, 0, -1, 0, 1, -1, -1, 1, 0, 1, 0, -1, 0, 0, 1, 0, -1, 0};
+    for (int q = 0; q < 19; ++q) {
+        const float w = q == 0 ? 1.f / 3.f : (q <= 4 || q == 9 || q == 14) ? 1.f / 18.f : 1.f / 36.f;
+        const float cu = float(CX[q]) * u0;
+        L.off[q] = (L.storage == STORE_F16 || L.storage == STORE_BF16)
+                       ? w * (1.f + 3.f * cu + 4.5f * cu * cu - 1.5f * u0 * u0)
+                       : 0.f;
+    }
+}
+
+int alloc_level(LevelState& s, int nx, int ny, int nz, int storage, bool stats, float u_ref) {
     Level& L = s.L;
     L.nx = nx;
     L.ny = ny;
@@ -448,6 +463,7 @@ int alloc_level(LevelState& s, int nx, int ny, int nz, int storage, bool stats) 
     L.plane = (long long)L.pitch * ny;
     L.qstride = L.plane * nz;
     L.storage = storage;
+    set_offsets(L, u_ref);
     if (L.qstride * 19 >= (1LL << 31))
         return fail(LBM_ERR_CONFIG, "level %dx%dx%d too large: 19 populations must index below 2^31", nx, ny, nz);
     const size_t bytes = size_t(L.qstride) * 19 * storage_bytes(storage);
@@ -462,6 +478,8 @@ int alloc_level(LevelState& s, int nx, int ny, int nz, int storage, bool stats) 
         CUDA_TRY(cudaMemset(s.stats, 0, size_t(L.qstride) * 4 * sizeof(float)));
     }
     CUDA_TRY(cudaMalloc(&s.fpart, size_t(force_partials()) * 3 * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&s.done, sizeof(unsigned)));
+    CUDA_TRY(cudaMemset(s.done, 0, sizeof(unsigned)));
     return LBM_OK;
 }
 
@@ -565,7 +583,8 @@ int one_step(lbm_handle* h) {
         if (rc) return rc;
     }
     if (p.force_on)
-        CUDA_TRY(launch_force(C.L, C.f[C.cur], C.body, C.nbody, C.fpart, h->force_hist + 3LL * fidx, h->stream));
+        CUDA_TRY(launch_force(C.L, C.f[C.cur], C.body, C.nbody, C.fpart, C.done, h->force_hist + 3LL * fidx,
+                              h->stream));
     CUDA_TRY(launch_stream_collide(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, h->mom, h->stream));
     C.cur = 1 - C.cur;
     if (c.refinement) {
@@ -580,8 +599,8 @@ int one_step(lbm_handle* h) {
                 if (rc) return rc;
             }
             if (pf.force_on)
-                CUDA_TRY(launch_force(Fn.L, Fn.f[Fn.cur], Fn.body, Fn.nbody, Fn.fpart, h->force_hist + 3LL * fidx,
-                                      h->stream));
+                CUDA_TRY(launch_force(Fn.L, Fn.f[Fn.cur], Fn.body, Fn.nbody, Fn.fpart, Fn.done,
+                                      h->force_hist + 3LL * fidx, h->stream));
             CUDA_TRY(launch_stream_collide(Fn.L, pf, Fn.f[Fn.cur], Fn.f[1 - Fn.cur], Fn.mask, Fn.stats, nullptr,
                                            h->stream));
             Fn.cur = 1 - Fn.cur;
@@ -643,6 +662,19 @@ int lbm_inputs_mask(const char* inputs_text, int level, uint8_t* mask, size_t ca
 
 static void write_level(std::ostream& out, std::ostream* slice, const Config& c, int level, const std::vector<float>& f,
                         const std::vector<float>& st, int nx, int ny, int nz);
+
+/* WriteForces (LR7:2537-2545): "t, Fx/ref, Fy/ref, Fz/ref" with
+ * ref = UMAX^2 ZDIM OBSTR1 (times LRLEVEL^2 with refinement), in FP32 as the
+ * reference prints it */
+static std::string format_forces(const Config& c, const double* F, int n) {
+    std::ostringstream o;
+    float ref = c.umax * c.umax * c.nz * c.r1;
+    if (c.refinement) ref *= std::lround(1.0 / c.lrfactor) * std::lround(1.0 / c.lrfactor);
+    for (int i = 0; i < n; ++i)
+        o << i + c.startf << ", " << float(F[3 * i]) / ref << ", " << float(F[3 * i + 1]) / ref << ", "
+          << float(F[3 * i + 2]) / ref << std::endl;
+    return o.str();
+}
 
 static int copy_out(const std::string& s, char* buf, size_t cap, size_t* len) {
     if (len) *len = s.size();
@@ -718,11 +750,13 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
         return bail(fail(LBM_ERR_CUDA, "cannot create a CUDA stream"));
     cudaEventCreate(&h->ev0);
     cudaEventCreate(&h->ev1);
-    if ((rc = alloc_level(h->lv[0], c.nx, c.ny, c.nz, storage, c.velav != 0))) return bail(rc);
+    /* reference velocity of the FP16/BF16 offsets: the inlet velocity of a channel */
+    const float u_ref = c.geometry.rfind("channel", 0) == 0 ? c.umax : 0.f;
+    if ((rc = alloc_level(h->lv[0], c.nx, c.ny, c.nz, storage, c.velav != 0, u_ref))) return bail(rc);
     mask_base(c, h->lv[0].hmask);
     if ((rc = upload_mask(h, 0))) return bail(rc);
     if (c.refinement) {
-        if ((rc = alloc_level(h->lv[1], c.lrx, c.lry, c.lrz, storage, c.velav != 0))) return bail(rc);
+        if ((rc = alloc_level(h->lv[1], c.lrx, c.lry, c.lrz, storage, c.velav != 0, u_ref))) return bail(rc);
         mask_fine(c, h->lv[1].hmask);
         if ((rc = upload_mask(h, 1))) return bail(rc);
         h->enx = int(c.lrx * c.lrfactor) + 1;
@@ -918,6 +952,38 @@ int lbm_get_forces(lbm_handle* h, double* fxyz, int max_steps, int* n) {
     return LBM_OK;
 }
 
+int lbm_get_last_force(lbm_handle* h, double* f3) {
+    if (!h || !f3) return fail(LBM_ERR_ARG, "null argument");
+    const int i = h->t - 1 - h->cfg.startf;
+    if (i < 0 || i >= h->force_cap) {
+        f3[0] = f3[1] = f3[2] = 0.0;
+        return LBM_OK;
+    }
+    CUDA_TRY(cudaMemcpyAsync(f3, h->force_hist + 3LL * i, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return LBM_OK;
+}
+
+int lbm_time_stream_collide(lbm_handle* h, int level, int n, float* ms) {
+    if (int rc = check_level(h, level)) return rc;
+    if (n < 1 || !ms) return fail(LBM_ERR_ARG, "bad argument");
+    LevelState& s = h->lv[level];
+    StepParams p = base_params(h, level);
+    p.t = h->t;
+    p.stats_on = 0;
+    CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+    for (int i = 0; i < n; ++i) {
+        CUDA_TRY(launch_stream_collide(s.L, p, s.f[s.cur], s.f[1 - s.cur], s.mask, nullptr, nullptr, h->stream));
+        s.cur = 1 - s.cur;
+    }
+    CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
+    CUDA_TRY(cudaEventSynchronize(h->ev1));
+    float t = 0;
+    CUDA_TRY(cudaEventElapsedTime(&t, h->ev0, h->ev1));
+    *ms = t / n;
+    return LBM_OK;
+}
+
 int lbm_audit(lbm_handle* h, int level, double* out4) {
     if (int rc = check_level(h, level)) return rc;
     if (!out4) return fail(LBM_ERR_ARG, "out4 is null");
@@ -1024,17 +1090,19 @@ int lbm_write_outputs(lbm_handle* h, const char* casename) {
         write_level(part, &slice, c, l, f, st, s.L.nx, s.L.ny, s.L.nz);
         part << std::endl;
     }
-    /* WriteForces (LR7:2537-2545): t, F/ref with ref = UMAX^2 ZDIM OBSTR1 (x LRLEVEL^2) */
     const int nf = std::max(0, c.tmax - c.startf);
     std::vector<double> F(size_t(std::max(nf, 1)) * 3, 0.0);
     int got = 0;
     if (int rc = lbm_get_forces(h, F.data(), nf, &got)) return rc;
-    float ref = c.umax * c.umax * c.nz * c.r1;
-    if (c.refinement) ref *= std::lround(1.0 / c.lrfactor) * std::lround(1.0 / c.lrfactor);
-    for (int i = 0; i < nf; ++i)
-        force << i + c.startf << ", " << float(F[3 * i]) / ref << ", " << float(F[3 * i + 1]) / ref << ", "
-              << float(F[3 * i + 2]) / ref << std::endl;
+    force << format_forces(c, F.data(), nf);
     return LBM_OK;
+}
+
+int lbm_format_forces(const char* inputs_text, const double* fxyz, int n, char* buf, size_t cap, size_t* len) {
+    Config c;
+    if (int rc = parse_inputs(inputs_text, c)) return rc;
+    if (!fxyz || n < 0) return fail(LBM_ERR_ARG, "bad force history");
+    return copy_out(format_forces(c, fxyz, n), buf, cap, len);
 }
 
 /* ---- kernel-level API ---- */
@@ -1049,6 +1117,7 @@ static int kernel_level(Level& L, int nx, int ny, int nz, int pitch) {
     L.plane = (long long)pitch * ny;
     L.qstride = L.plane * nz;
     L.storage = STORE_F32;
+    set_offsets(L, 0.f);
     if (L.qstride * 19 >= (1LL << 31)) return fail(LBM_ERR_ARG, "level too large: 19 populations must index below 2^31");
     return LBM_OK;
 }

@@ -24,29 +24,33 @@
 
 namespace lbm {
 
-/* ---- storage formats: FP32, FP16/BF16 offset (f - w) with FP32 math, FP64 ---- */
+/* ---- storage formats: FP32, FP64, and FP16/BF16 holding f - off with FP32
+ * math; off is the equilibrium at the level's reference velocity (Level::off),
+ * so the stored numbers are small deviations and keep their relative precision */
 template <class S> struct Fmt;
 template <> struct Fmt<float> {
     using T = float;
-    static __device__ __forceinline__ float ld(const float* p, int) { return __ldg(p); }
-    static __device__ __forceinline__ void st(float* p, float v, int) { *p = v; }
+    static __device__ __forceinline__ float ld(const float* p, float) { return __ldg(p); }
+    static __device__ __forceinline__ void st(float* p, float v, float) { *p = v; }
 };
 template <> struct Fmt<double> {
     using T = double;
-    static __device__ __forceinline__ double ld(const double* p, int) { return __ldg(p); }
-    static __device__ __forceinline__ void st(double* p, double v, int) { *p = v; }
+    static __device__ __forceinline__ double ld(const double* p, float) { return __ldg(p); }
+    static __device__ __forceinline__ void st(double* p, double v, float) { *p = v; }
 };
 template <> struct Fmt<__half> {
     using T = float;
-    static __device__ __forceinline__ float ld(const __half* p, int q) { return __half2float(__ldg(p)) + wq(q); }
-    static __device__ __forceinline__ void st(__half* p, float v, int q) { *p = __float2half_rn(v - wq(q)); }
+    static __device__ __forceinline__ float ld(const __half* p, float off) { return __half2float(__ldg(p)) + off; }
+    static __device__ __forceinline__ void st(__half* p, float v, float off) { *p = __float2half_rn(v - off); }
 };
 template <> struct Fmt<__nv_bfloat16> {
     using T = float;
-    static __device__ __forceinline__ float ld(const __nv_bfloat16* p, int q) {
-        return __bfloat162float(__ldg(p)) + wq(q);
+    static __device__ __forceinline__ float ld(const __nv_bfloat16* p, float off) {
+        return __bfloat162float(__ldg(p)) + off;
     }
-    static __device__ __forceinline__ void st(__nv_bfloat16* p, float v, int q) { *p = __float2bfloat16_rn(v - wq(q)); }
+    static __device__ __forceinline__ void st(__nv_bfloat16* p, float v, float off) {
+        *p = __float2bfloat16_rn(v - off);
+    }
 };
 
 template <class S>
@@ -84,14 +88,14 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
     for (int q = 0; q < 19; ++q) {
         /* pull: the value arriving from x - c_q */
         const unsigned src = q * qs + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)];
-        f[q] = F::ld(fA + src, q);
+        f[q] = F::ld(fA + src, L.off[q]);
     }
 
     if (type == WALL || type == BODY) {
         /* full-way bounce-back (LR7:1493-1526); the momentum exchange of BODY
          * nodes is summed by k_force_list from the same fA */
 #pragma unroll
-        for (int q = 0; q < 19; ++q) F::st(fB + q * qs + c, f[opp(q)], q);
+        for (int q = 0; q < 19; ++q) F::st(fB + q * qs + c, f[opp(q)], L.off[q]);
     } else {
         if (type >= WEST_INLET && type <= NORTH_OUTLET) {
             /* rebuild from the neighbour's stored post-collision state */
@@ -101,7 +105,7 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
             else if (type == SOUTH_INLET) nb = zb[1] + yb[2] + x;
             else nb = zb[1] + yb[0] + x;
 #pragma unroll
-            for (int q = 0; q < 19; ++q) f[q] = F::ld(fA + q * qs + nb, q);
+            for (int q = 0; q < 19; ++q) f[q] = F::ld(fA + q * qs + nb, L.off[q]);
             T uin = T(p.u_in);
             if (p.noise_amp != 0.f) {
                 const uint32_t cell = uint32_t((z * L.ny + y) * L.nx + x);
@@ -140,7 +144,7 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
             }
         }
 #pragma unroll
-        for (int q = 0; q < 19; ++q) F::st(fB + q * qs + c, f[q], q);
+        for (int q = 0; q < 19; ++q) F::st(fB + q * qs + c, f[q], L.off[q]);
     }
 
     if (p.exp_nx > 0) {
@@ -164,34 +168,42 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
  * LR7:1607-1626): F += 2 sum_q c_q f_q over the populations a body node pulls
  * from fA.  Runs over a compact list of body nodes (pitched indices) instead
  * of inside the stream-collide kernel, so the hot kernel carries no FP64 and no
- * block barrier; per-block FP64 partials are summed in a fixed order. */
-constexpr int FORCE_BLOCKS = 64, FORCE_THREADS = 256;
+ * block barrier.  Per node the sum is FP32 (as in the reference); across nodes
+ * it is FP64: per-block partials, and the last block to finish adds them in
+ * block order, so the result does not depend on scheduling. */
+constexpr int FORCE_BLOCKS = 152, FORCE_THREADS = 256;
 template <class S>
 __global__ void __launch_bounds__(FORCE_THREADS) k_force_list(const Level L, const S* __restrict__ fA,
                                                               const unsigned* __restrict__ body, int nbody,
-                                                              double* __restrict__ part) {
+                                                              double* __restrict__ part, unsigned* __restrict__ done,
+                                                              double* __restrict__ out3) {
     using F = Fmt<S>;
+    using T = typename F::T;
     double s[3] = {0.0, 0.0, 0.0};
+    const unsigned plane = unsigned(L.plane), pitch = unsigned(L.pitch), qs = unsigned(L.qstride);
     for (int i = blockIdx.x * FORCE_THREADS + threadIdx.x; i < nbody; i += FORCE_BLOCKS * FORCE_THREADS) {
         const unsigned c = body[i];
-        const int z = int(c / unsigned(L.plane));
-        const unsigned r = c - unsigned(z) * unsigned(L.plane);
-        const int y = int(r / unsigned(L.pitch)), x = int(r - unsigned(y) * unsigned(L.pitch));
-        const int xm = (x == 0) ? L.nx - 1 : x - 1, xp = (x == L.nx - 1) ? 0 : x + 1;
-        const int ym = (y == 0) ? L.ny - 1 : y - 1, yp = (y == L.ny - 1) ? 0 : y + 1;
-        const int zm = (z == 0) ? L.nz - 1 : z - 1, zp = (z == L.nz - 1) ? 0 : z + 1;
-        const long long zb[3] = {zm * L.plane, z * L.plane, zp * L.plane};
-        const long long yb[3] = {(long long)ym * L.pitch, (long long)y * L.pitch, (long long)yp * L.pitch};
-        const int xs[3] = {xm, x, xp};
+        const unsigned z = c / plane, r = c - z * plane;
+        const unsigned y = r / pitch, x = r - y * pitch;
+        const unsigned xm = (x == 0) ? L.nx - 1 : x - 1, xp = (x == unsigned(L.nx) - 1) ? 0 : x + 1;
+        const unsigned ym = (y == 0) ? L.ny - 1 : y - 1, yp = (y == unsigned(L.ny) - 1) ? 0 : y + 1;
+        const unsigned zm = (z == 0) ? L.nz - 1 : z - 1, zp = (z == unsigned(L.nz) - 1) ? 0 : z + 1;
+        const unsigned zb[3] = {zm * plane, z * plane, zp * plane};
+        const unsigned yb[3] = {ym * pitch, y * pitch, yp * pitch};
+        const unsigned xs[3] = {xm, x, xp};
+        T a[3] = {0, 0, 0};
 #pragma unroll
         for (int q = 1; q < 19; ++q) {
-            const double v = 2.0 * double(F::ld(fA + q * L.qstride + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)], q));
-            if (cx(q)) s[0] += cx(q) * v;
-            if (cy(q)) s[1] += cy(q) * v;
-            if (cz(q)) s[2] += cz(q) * v;
+            const T v = T(2) * F::ld(fA + q * qs + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)], L.off[q]);
+            if (cx(q)) a[0] += T(cx(q)) * v;
+            if (cy(q)) a[1] += T(cy(q)) * v;
+            if (cz(q)) a[2] += T(cz(q)) * v;
         }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) s[k] += double(a[k]);
     }
     __shared__ double red[3][FORCE_THREADS / 32];
+    __shared__ bool last;
     for (int k = 0; k < 3; ++k) {
         double v = s[k];
 #pragma unroll
@@ -204,6 +216,22 @@ __global__ void __launch_bounds__(FORCE_THREADS) k_force_list(const Level L, con
 #pragma unroll
         for (int w = 0; w < FORCE_THREADS / 32; ++w) v += red[threadIdx.x][w];
         part[3 * blockIdx.x + threadIdx.x] = v;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(done, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (last) {
+        /* warp k sums component k: lane-strided partials, then a fixed shuffle tree */
+        const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        if (k < 3) {
+            double v = 0.0;
+            for (int b = lane; b < int(gridDim.x); b += 32) v += __ldcg(part + 3 * b + k);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) out3[k] += v;
+        }
+        if (threadIdx.x == 0) *done = 0u;
     }
 }
 
@@ -254,7 +282,7 @@ __global__ void k_init(const Level L, const uint8_t* __restrict__ mask, S* __res
         }
     }
 #pragma unroll
-    for (int q = 0; q < 19; ++q) F::st(f + q * L.qstride + c, g[q], q);
+    for (int q = 0; q < 19; ++q) F::st(f + q * L.qstride + c, g[q], L.off[q]);
 }
 
 /* density and momentum (the reference's u, v, w are momenta) into compact arrays */
@@ -268,7 +296,7 @@ __global__ void k_fields(const Level L, const S* __restrict__ f, float* rho, flo
     T r = 0, a = 0, b = 0, d = 0;
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        const T g = F::ld(f + q * L.qstride + c, q);
+        const T g = F::ld(f + q * L.qstride + c, L.off[q]);
         r += g;
         if (cx(q)) a += T(cx(q)) * g;
         if (cy(q)) b += T(cy(q)) * g;
@@ -288,7 +316,7 @@ template <class S> __global__ void k_pack(const Level L, const S* __restrict__ f
     const long long c = z * L.plane + (long long)y * L.pitch + x;
     const long long n = (long long)L.nx * L.ny * L.nz, o = ((long long)z * L.ny + y) * L.nx + x;
 #pragma unroll
-    for (int q = 0; q < 19; ++q) out[q * n + o] = float(F::ld(f + q * L.qstride + c, q));
+    for (int q = 0; q < 19; ++q) out[q * n + o] = float(F::ld(f + q * L.qstride + c, L.off[q]));
 }
 
 template <class S> __global__ void k_unpack(const Level L, const float* __restrict__ in, S* __restrict__ f) {
@@ -298,7 +326,7 @@ template <class S> __global__ void k_unpack(const Level L, const float* __restri
     const long long c = z * L.plane + (long long)y * L.pitch + x;
     const long long n = (long long)L.nx * L.ny * L.nz, o = ((long long)z * L.ny + y) * L.nx + x;
 #pragma unroll
-    for (int q = 0; q < 19; ++q) F::st(f + q * L.qstride + c, in[q * n + o], q);
+    for (int q = 0; q < 19; ++q) F::st(f + q * L.qstride + c, in[q * n + o], L.off[q]);
 }
 
 /* FP64 mass and momentum of the non-solid nodes; grid-stride over rows so the
@@ -317,14 +345,17 @@ __global__ void __launch_bounds__(256) k_audit(const Level L, const S* __restric
             const long long c = z * L.plane + (long long)y * L.pitch + x;
             const int t = mask[c];
             if (t == WALL || t == BODY) continue;
+            typename F::T m[4] = {0, 0, 0, 0};
 #pragma unroll
             for (int q = 0; q < 19; ++q) {
-                const double g = double(F::ld(f + q * L.qstride + c, q));
-                acc[0] += g;
-                if (cx(q)) acc[1] += cx(q) * g;
-                if (cy(q)) acc[2] += cy(q) * g;
-                if (cz(q)) acc[3] += cz(q) * g;
+                const typename F::T g = F::ld(f + q * L.qstride + c, L.off[q]);
+                m[0] += g;
+                if (cx(q)) m[1] += cx(q) * g;
+                if (cy(q)) m[2] += cy(q) * g;
+                if (cz(q)) m[3] += cz(q) * g;
             }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[k] += double(m[k]);
         }
     }
     __shared__ double red[4][8];
@@ -369,7 +400,7 @@ __global__ void k_audit_final(const double* __restrict__ part, int n, double* __
 template <class S>
 __device__ __forceinline__ void load19(const Level& L, const S* f, long long c, float g[19]) {
 #pragma unroll
-    for (int q = 0; q < 19; ++q) g[q] = float(Fmt<S>::ld(f + q * L.qstride + c, q));
+    for (int q = 0; q < 19; ++q) g[q] = float(Fmt<S>::ld(f + q * L.qstride + c, L.off[q]));
 }
 
 /* second-order correction of the interpolated momentum from the 8 corner
@@ -468,7 +499,7 @@ __global__ void k_interp_cf(const RefineParams r, const Level F, const float* __
     float g[19];
     invert_scaled<float>(mom, SF, g);
 #pragma unroll
-    for (int q = 0; q < 19; ++q) Fmt<S>::st(f_f + q * F.qstride + cf, g[q], q);
+    for (int q = 0; q < 19; ++q) Fmt<S>::st(f_f + q * F.qstride + cf, g[q], F.off[q]);
 }
 
 /* InterpFC (LR7:2172-2348): coarse nodes strictly inside the patch (2-node
@@ -533,7 +564,7 @@ __global__ void k_interp_fc(const RefineParams r, const Level C, const Level F, 
     float g[19];
     invert_scaled<float>(mom, SF, g);
 #pragma unroll
-    for (int q = 0; q < 19; ++q) Fmt<S>::st(f_c + q * C.qstride + cc, g[q], q);
+    for (int q = 0; q < 19; ++q) Fmt<S>::st(f_c + q * C.qstride + cc, g[q], C.off[q]);
 }
 
 /* ---- launchers ---- */
@@ -558,11 +589,10 @@ cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const voi
 int force_partials() { return FORCE_BLOCKS; }
 
 cudaError_t launch_force(const Level& L, const void* fA, const unsigned* body, int nbody, double* partials,
-                         double* out3, cudaStream_t s) {
+                         unsigned* done, double* out3, cudaStream_t s) {
     if (nbody <= 0) return cudaSuccess;
     LBM_DISPATCH(L.storage, (k_force_list<S><<<FORCE_BLOCKS, FORCE_THREADS, 0, s>>>(L, (const S*)fA, body, nbody,
-                                                                                    partials)));
-    k_reduce3<<<1, 64, 0, s>>>(partials, FORCE_BLOCKS, out3);
+                                                                                    partials, done, out3)));
     return cudaGetLastError();
 }
 
@@ -586,14 +616,18 @@ __global__ void __launch_bounds__(256) k_force_scan(const Level L, const S* __re
             const long long zb[3] = {zm * L.plane, z * L.plane, zp * L.plane};
             const long long yb[3] = {(long long)ym * L.pitch, (long long)y * L.pitch, (long long)yp * L.pitch};
             const int xs[3] = {xm, x, xp};
+            /* per node in the storage's arithmetic (as k_force_list), across nodes FP64 */
+            typename F::T a[3] = {0, 0, 0};
 #pragma unroll
             for (int q = 1; q < 19; ++q) {
-                const double v =
-                    2.0 * double(F::ld(fA + q * L.qstride + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)], q));
-                if (cx(q)) s[0] += cx(q) * v;
-                if (cy(q)) s[1] += cy(q) * v;
-                if (cz(q)) s[2] += cz(q) * v;
+                const typename F::T v = typename F::T(2) *
+                    F::ld(fA + q * L.qstride + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)], L.off[q]);
+                if (cx(q)) a[0] += cx(q) * v;
+                if (cy(q)) a[1] += cy(q) * v;
+                if (cz(q)) a[2] += cz(q) * v;
             }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) s[k] += double(a[k]);
         }
     }
     __shared__ double red[3][8];

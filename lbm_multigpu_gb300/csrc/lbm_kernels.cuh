@@ -35,6 +35,7 @@ struct Level {
     long long plane;      /* pitch * ny */
     long long qstride;    /* plane * nz */
     int storage;          /* Storage */
+    float off[19];        /* FP16/BF16 store f - off[q] (equilibrium at the reference velocity) */
 };
 
 struct StepParams {
@@ -68,7 +69,7 @@ cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const voi
                                   const uint8_t* mask, float* stats, float* mom_export, cudaStream_t s);
 /* FP64 momentum exchange over a list of BODY nodes (pitched indices), ADDED to out3 */
 cudaError_t launch_force(const Level& L, const void* fA, const unsigned* body, int nbody, double* partials,
-                         double* out3, cudaStream_t s);
+                         unsigned* done, double* out3, cudaStream_t s);
 int force_partials();
 /* the same sum found by scanning the mask; partials holds force_scan_partials()*3 doubles */
 cudaError_t launch_force_scan(const Level& L, const void* fA, const uint8_t* mask, double* partials, double* out3,

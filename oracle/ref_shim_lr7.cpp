@@ -334,6 +334,18 @@ void ref_get_moments(float* out) {
                 }
 }
 
+/* velAv u, velAv v, velFluc u, velFluc v as compact [4][ZDIM][YDIM][XDIM] */
+void ref_get_stats(float* out) {
+    const long N = long(XDIM) * YDIM * ZDIM;
+    const size_t P = S.pitch_e;
+    const vector<float>* src[4] = {&S.velAv[0], &S.velAv[1], &S.velFluc[0], &S.velFluc[1]};
+    for (int k = 0; k < 4; ++k)
+        for (int z = 0; z < ZDIM; ++z)
+            for (int y = 0; y < YDIM; ++y)
+                for (int x = 0; x < XDIM; ++x)
+                    out[k * N + (long(z) * YDIM + y) * XDIM + x] = (*src[k])[x + y * P + z * P * YDIM];
+}
+
 void ref_get_forces(float* out, int n) {
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < n && j < int(S.F[i].size()); ++j) out[i * n + j] = S.F[i][j];

@@ -165,11 +165,14 @@ def writer():
     assert L.ref_write_results(zone, len(zone), sl, len(sl)) == 0
     forces = ctypes.create_string_buffer(1 << 16)
     assert L.ref_write_forces(forces, len(forces), 0) > 0
-    np.savez_compressed(HERE / "writer_tiny.npz", f=f)
-    with gzip.open(HERE / "writer_tiny_part0.dat.gz", "wt") as fh:
-        fh.write(zone.value.decode())
-    with gzip.open(HERE / "writer_tiny_slice.dat.gz", "wt") as fh:
-        fh.write(sl.value.decode())
+    st = np.zeros((4, Z, Y, X), np.float32)
+    L.ref_get_stats(ptr(st))
+    Fr = np.zeros((3, steps), np.float32)
+    L.ref_get_forces(ptr(Fr), steps)
+    np.savez_compressed(HERE / "writer_tiny.npz", f=f, stats=st, forces=Fr.T.copy())
+    for name, text in (("writer_tiny_part0.dat.gz", zone.value), ("writer_tiny_slice.dat.gz", sl.value)):
+        with gzip.GzipFile(HERE / name, "wb", mtime=0) as fh:
+            fh.write(text)
     (HERE / "writer_tiny.force").write_text(forces.value.decode())
     (HERE / "writer_tiny.inputs").write_text(write_inputs_text(L))
 
