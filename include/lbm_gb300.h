@@ -163,6 +163,22 @@ int lbm_body_force_f32(const float* fA, const uint8_t* mask, int nx, int ny, int
                        double* scratch, void* cuda_stream);
 size_t lbm_body_force_scratch_doubles(void);
 
+/* lbm_body_force_f32 for callers that cannot allocate device memory (a host
+ * framework that has reserved the device memory for its own allocator, a
+ * real-time loop that cannot afford cudaMalloc's latency and device-wide
+ * synchronisation, a plugin host that forbids allocation calls).  No
+ * counterpart in the reference.  Same inputs and output (the three sums are
+ * ADDED to force_out), no scratch argument: the partial sums live in a fixed
+ * 32 KiB array of the library's own device memory, one per device, held until
+ * the process exits.  It never allocates.  The first call on a device looks
+ * up that array's address (make the first call before capturing work into a
+ * stream).  All calls share the array: calls that overlap on the GPU (other
+ * streams, other threads) race and must be serialised by the caller.  Domains
+ * whose 19 populations need 2^31 or more elements are rejected (LBM_ERR_ARG),
+ * as by lbm_body_force_f32. */
+int lbm_body_force_f32_noalloc(const float* fA, const uint8_t* mask, int nx, int ny, int nz, int pitch,
+                               double* force_out, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

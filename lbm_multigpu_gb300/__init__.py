@@ -65,6 +65,7 @@ SIGNATURES = [
     ("lbm_stream_collide_f32", _I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _F, _F, _F, _F, _I, _P]),
     ("lbm_body_force_f32", _I, [_P, _P, _I, _I, _I, _I, _P, _P, _P]),
     ("lbm_body_force_scratch_doubles", _SZ, []),
+    ("lbm_body_force_f32_noalloc", _I, [_P, _P, _I, _I, _I, _I, _P, _P]),
 ]
 
 

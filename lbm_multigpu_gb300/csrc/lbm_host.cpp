@@ -409,6 +409,11 @@ struct LevelState {
 
 }  // namespace
 
+int lbm::set_error(int code, const char* what, cudaError_t e) {
+    if (e != cudaSuccess) return fail(code, "%s: %s", what, cudaGetErrorString(e));
+    return fail(code, "%s", what);
+}
+
 struct lbm_handle {
     Config cfg;
     int storage = STORE_F32;

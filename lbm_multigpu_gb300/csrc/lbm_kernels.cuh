@@ -75,6 +75,9 @@ int force_partials();
 cudaError_t launch_force_scan(const Level& L, const void* fA, const uint8_t* mask, double* partials, double* out3,
                               cudaStream_t s);
 int force_scan_partials();
+
+/* record an error for lbm_last_error(); returns code (lbm_host.cpp) */
+int set_error(int code, const char* what, cudaError_t e);
 cudaError_t launch_init(const Level& L, const uint8_t* mask, void* f, int kind, float u0, cudaStream_t s);
 cudaError_t launch_fields(const Level& L, const void* f, float* rho, float* u, float* v, float* w, cudaStream_t s);
 cudaError_t launch_pack(const Level& L, const void* f, float* compact, cudaStream_t s);
