@@ -314,7 +314,8 @@ template <class T> __host__ __device__ __forceinline__ void extrap(int type, T f
  * DirichletWest_Regularized, CPU:974-1054, written per face): density from the
  * known populations, unknowns by non-equilibrium bounce-back, then
  * f = feq + 4.5 w_q (c_q c_q - I/3) : Pi_neq. */
-template <class T> __host__ __device__ __forceinline__ void lid(T f[19], int face, T ux, T uy, T uz) {
+template <class T>
+__host__ __device__ __forceinline__ void lid(T f[19], int face, T ux, T uy, T uz, bool quirk = false) {
     const int axis = face >> 1;
     const int sgn = (face & 1) ? -1 : 1;
     T s0 = 0, s1 = 0;
@@ -333,6 +334,12 @@ template <class T> __host__ __device__ __forceinline__ void lid(T f[19], int fac
         const T cu = T(cx(q)) * ux + T(cy(q)) * uy + T(cz(q)) * uz;
         feq[q] = T(wq(q)) * (rho + T(3) * cu + T(4.5) * cu * cu - T(1.5) * usq);
     }
+    if (quirk) {
+        /* CPU_3D writes (v+w)*(u+w) and (-v+w)*(u+w) for the squares of
+         * populations 11 and 13 (CPU:1012, 1014) */
+        feq[11] = T(wq(11)) * (rho + T(3) * (uy + uz) + T(4.5) * (uy + uz) * (ux + uz) - T(1.5) * usq);
+        feq[13] = T(wq(13)) * (rho + T(3) * (-uy + uz) + T(4.5) * (-uy + uz) * (ux + uz) - T(1.5) * usq);
+    }
     T g[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) g[q] = f[q] - feq[q];
@@ -340,6 +347,10 @@ template <class T> __host__ __device__ __forceinline__ void lid(T f[19], int fac
     for (int q = 0; q < 19; ++q) {
         const int cn = (axis == 0 ? cx(q) : axis == 1 ? cy(q) : cz(q)) * sgn;
         if (cn > 0) g[q] = g[opp(q)];
+    }
+    if (quirk && face == 0) {
+        /* CPU:1023 sets f8 = feq6 + f6 - feq6 */
+        g[8] = (feq[6] + f[6] - feq[6]) - feq[8];
     }
     T P[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll

@@ -83,10 +83,12 @@ struct Config {
     float noise = 0;
     uint32_t seed = 12345u;
     int velav = 0;
-    int init = -1;                  /* 0: MRT equilibrium, 1: BGK equilibrium; -1: by model */
+    int init = -1;                  /* 0: MRT equilibrium, 1: BGK, 2: BGK incl. solids (CPU_3D); -1: by model */
     float init_u = -1e30f;          /* default: UMAX (channel), 0 (cavity / periodic) */
     int order = 2;
     int fc_zflip = 1;
+    int pull_clamp = 0;             /* "EDGE PULL: clamp" (CPU_3D) or "wrap" */
+    int lid_quirk = 0;              /* "LID BC: cpu3d" reproduces CPU_3D's lid as written */
     /* older records spell the LES line "Smagorinski LES: YES/NO"; DynInlet
      * records add "KP" (the inlet P-control gain, MRTtest/DynInlet3.cu:26) */
     bool les_yesno = false;
@@ -184,6 +186,14 @@ int parse_inputs(const char* text, Config& c) {
         else if (key == "Init velocity") F(c.init_u);
         else if (key == "ORDER") I(c.order);
         else if (key == "FC top zflip") I(c.fc_zflip);
+        else if (key == "EDGE PULL") {
+            ok = (val == "clamp" || val == "wrap");
+            c.pull_clamp = val == "clamp";
+        }
+        else if (key == "LID BC") {
+            ok = (val == "cpu3d" || val == "regularized");
+            c.lid_quirk = val == "cpu3d";
+        }
         else return fail(LBM_ERR_PARSE, ".inputs line %d: unknown key '%s'", lineno, key.c_str());
         if (!ok) return fail(LBM_ERR_PARSE, ".inputs line %d: cannot read value '%s' of '%s'", lineno, val.c_str(), key.c_str());
         c.layout.push_back({line.substr(0, tab), sep, key});
@@ -271,6 +281,8 @@ std::string value_of(const Config& c, const std::string& key, float omega, float
     else if (key == "Init velocity") o << c.init_u;
     else if (key == "ORDER") o << c.order;
     else if (key == "FC top zflip") o << c.fc_zflip;
+    else if (key == "EDGE PULL") o << (c.pull_clamp ? "clamp" : "wrap");
+    else if (key == "LID BC") o << (c.lid_quirk ? "cpu3d" : "regularized");
     return o.str();
 }
 
@@ -324,6 +336,8 @@ std::string write_inputs(const Config& c, float omega, float omegaLR) {
     if (c.init_u > -1e29f) line("Init velocity: ", "Init velocity");
     if (c.order != d.order) line("ORDER: ", "ORDER");
     if (c.fc_zflip != d.fc_zflip) line("FC top zflip: ", "FC top zflip");
+    if (c.pull_clamp) line("EDGE PULL: ", "EDGE PULL");
+    if (c.lid_quirk) line("LID BC: ", "LID BC");
     return o.str();
 }
 
@@ -542,6 +556,8 @@ StepParams base_params(const lbm_handle* h, int level) {
     p.lid_u[1] = lid_default ? 0.f : c.lid_u[1];
     p.lid_u[2] = lid_default ? 0.f : c.lid_u[2];
     p.lid_face = c.lid_face;
+    p.lid_quirk = c.lid_quirk;
+    p.pull_clamp = c.pull_clamp;
     p.stats_on = c.velav;
     p.start_av = c.start_av;
     p.start_fluc = c.start_fluc;

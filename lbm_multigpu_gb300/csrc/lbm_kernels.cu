@@ -73,12 +73,13 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
     const int type = mask[c];
     /* periodic neighbours; only boundary nodes, whose pulled values the
      * reference discards or bounces, ever wrap in x or y */
-    const unsigned xm = (x == 0) ? L.nx - 1 : x - 1;
-    const unsigned xp = (x == L.nx - 1) ? 0 : x + 1;
-    const unsigned ym = (y == 0) ? L.ny - 1 : y - 1;
-    const unsigned yp = (y == L.ny - 1) ? 0 : y + 1;
-    const unsigned zm = (z == 0) ? L.nz - 1 : z - 1;
-    const unsigned zp = (z == L.nz - 1) ? 0 : z + 1;
+    const bool cl = p.pull_clamp != 0;
+    const unsigned xm = (x == 0) ? (cl ? 0 : L.nx - 1) : x - 1;
+    const unsigned xp = (x == L.nx - 1) ? (cl ? x : 0) : x + 1;
+    const unsigned ym = (y == 0) ? (cl ? 0 : L.ny - 1) : y - 1;
+    const unsigned yp = (y == L.ny - 1) ? (cl ? y : 0) : y + 1;
+    const unsigned zm = (z == 0) ? (cl ? 0 : L.nz - 1) : z - 1;
+    const unsigned zp = (z == L.nz - 1) ? (cl ? z : 0) : z + 1;
     const unsigned zb[3] = {zm * plane, z * plane, zp * plane};
     const unsigned yb[3] = {ym * pitch, y * pitch, yp * pitch};
     const unsigned xs[3] = {xm, unsigned(x), xp};
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
             }
             extrap<T>(type, f, T(p.rho_out), uin);
         } else if (type == LID) {
-            lid<T>(f, p.lid_face, T(p.lid_u[0]), T(p.lid_u[1]), T(p.lid_u[2]));
+            lid<T>(f, p.lid_face, T(p.lid_u[0]), T(p.lid_u[1]), T(p.lid_u[2]), p.lid_quirk != 0);
         }
         collide<T>(p.model, f, T(p.omega), p.les != 0, T(p.cs), T(p.dpdy));
 
@@ -260,7 +261,8 @@ __global__ void k_reduce3(const double* __restrict__ part, int n, double* __rest
 
 /* initialize / initializeLR (LR7:1060-1125): rest state at rho = 1 with the
  * x velocity u0 (zero at bounce-back nodes).  kind 0: the MRT equilibrium
- * moments (mrt_meq + InvertMoments); kind 1: the BGK equilibrium. */
+ * moments (mrt_meq + InvertMoments); kind 1: the BGK equilibrium; kind 2: the
+ * BGK equilibrium at u0 on every node, solids included (CPU:1226-1308). */
 template <class S>
 __global__ void k_init(const Level L, const uint8_t* __restrict__ mask, S* __restrict__ f, int kind, float u0) {
     using F = Fmt<S>;
@@ -269,7 +271,7 @@ __global__ void k_init(const Level L, const uint8_t* __restrict__ mask, S* __res
     if (x >= L.nx || y >= L.ny) return;
     const long long c = z * L.plane + (long long)y * L.pitch + x;
     const int type = mask[c];
-    const T u = (type == WALL || type == BODY) ? T(0) : T(u0);
+    const T u = (kind != 2 && (type == WALL || type == BODY)) ? T(0) : T(u0);
     T g[19];
     if (kind == 0) {
         const T mom[9] = {T(1), u, T(0), T(0), T(0), T(0), T(0), T(0), T(0)};

@@ -45,6 +45,8 @@ struct StepParams {
     float u_in, rho_out;
     float lid_u[3];
     int lid_face;
+    int lid_quirk;         /* CPU_3D's regularised lid as written (CPU:1010-1023) */
+    int pull_clamp;        /* pulls from outside the domain clamp to the edge (CPU:1369-1388) instead of wrapping */
     int force_on;          /* accumulate momentum exchange at BODY nodes */
     int t;                 /* time step index (stats, noise) */
     int stats_on, start_av, start_fluc;

@@ -274,7 +274,7 @@ template <class T> inline void extrap(int kind, T* f, T rho_bc, T u_in) {
  * DirichletWest_Regularized (CPU:974-1054) written for any face: density from
  * the known populations, unknown populations by non-equilibrium bounce-back,
  * then f = feq + w_q 4.5 (c_q c_q - I/3) : Pi_neq. */
-template <class T> inline void lid(T* f, int face, T ux, T uy, T uz) {
+template <class T> inline void lid(T* f, int face, T ux, T uy, T uz, int quirk) {
     int axis = face / 2;
     int sgn = (face % 2 == 0) ? 1 : -1; /* inward normal component */
     const int* C[3] = {CX, CY, CZ};
@@ -288,8 +288,16 @@ template <class T> inline void lid(T* f, int face, T ux, T uy, T uz) {
     T rho = un + (s0 + T(2) * s1);
     T feq[Q];
     for (int q = 0; q < Q; ++q) feq[q] = feq_bgk<T>(q, rho, ux, uy, uz);
+    T usq = ux * ux + uy * uy + uz * uz;
+    if (quirk) {
+        /* CPU:1012, 1014: (v+w)*(u+w) and (-v+w)*(u+w) in place of the squares */
+        feq[11] = wq<T>(11) * (rho + T(3) * (uy + uz) + T(4.5) * (uy + uz) * (ux + uz) - T(1.5) * usq);
+        feq[13] = wq<T>(13) * (rho + T(3) * (-uy + uz) + T(4.5) * (-uy + uz) * (ux + uz) - T(1.5) * usq);
+    }
+    T f6 = f[6];
     for (int q = 0; q < Q; ++q)
         if (C[axis][q] * sgn > 0) f[q] = feq[q] + f[OPP[q]] - feq[OPP[q]];
+    if (quirk && face == 0) f[8] = feq[6] + f6 - feq[6]; /* CPU:1023 */
     T P[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     for (int q = 0; q < Q; ++q) {
         T g = f[q] - feq[q];
@@ -398,6 +406,7 @@ template <class T> inline void invert_les_fc(const T* mom, T omega_f, T cs, T lr
 }
 
 inline int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+inline int edge(int i, int n, int clamp) { return clamp ? (i < 0 ? 0 : (i >= n ? n - 1 : i)) : wrap(i, n); }
 
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), counter (cell, step, 0, 0),
  * key (seed, 0): the seeded inlet noise stream (extension, not in the reference). */
@@ -434,7 +443,8 @@ void step_impl(const orc_params* p, const uint8_t* mask, const T* fA, T* fB, dou
                  * periodic wrap, x/y wrap only reaches boundary nodes whose
                  * pulled values the reference discards */
                 for (int q = 0; q < Q; ++q) {
-                    int xs = wrap(x - CX[q], nx), ys = wrap(y - CY[q], ny), zs = wrap(z - CZ[q], nz);
+                    const int cl = p->pull_clamp;
+                    int xs = edge(x - CX[q], nx, cl), ys = edge(y - CY[q], ny, cl), zs = edge(z - CZ[q], nz, cl);
                     f[q] = fA[q * N + (long(zs) * ny + ys) * nx + xs];
                 }
                 if (im == ORC_WALL || im == ORC_BODY) {
@@ -471,7 +481,7 @@ void step_impl(const orc_params* p, const uint8_t* mask, const T* fA, T* fB, dou
                                              T(1));
                         extrap<T>(im, f, T(p->rho_out), uin);
                     } else if (im == ORC_LID) {
-                        lid<T>(f, p->lid_face, T(p->lid_u[0]), T(p->lid_u[1]), T(p->lid_u[2]));
+                        lid<T>(f, p->lid_face, T(p->lid_u[0]), T(p->lid_u[1]), T(p->lid_u[2]), p->lid_quirk);
                     }
                     collide<T>(p->model, f, T(p->omega), p->les, T(p->cs), T(p->dpdy));
                     if (p->stats_on && av_u) {
@@ -556,18 +566,20 @@ void orc_invert_les_fc(const float* mom, float* f, int n, float omega_f, float c
     for (int i = 0; i < n; ++i) invert_les_fc(mom + 9L * i, omega_f, cs, lrf, f + 19L * i);
 }
 
-void orc_lid(float* f, int n, int face, float ux, float uy, float uz) {
-    for (int i = 0; i < n; ++i) lid<float>(f + 19L * i, face, ux, uy, uz);
+void orc_lid(float* f, int n, int face, float ux, float uy, float uz, int quirk) {
+    for (int i = 0; i < n; ++i) lid<float>(f + 19L * i, face, ux, uy, uz, quirk);
 }
 
 /* initialize / initializeLR (LR7:1060-1125): equilibrium at rho = 1, u = u0
  * (zero at bounce-back nodes).  kind 0: mrt_meq + InvertMoments (LR7);
- * kind 1: BGK equilibrium (CPU_3D/CPU_3D.cpp:1226-1308, DI3). */
+ * kind 1: BGK equilibrium (DI3); kind 2: BGK equilibrium on every node,
+ * solids included (CPU_3D/CPU_3D.cpp:1226-1308). */
 void orc_init(const orc_params* p, const uint8_t* mask, float* f, int kind, float u0) {
     const long N = long(p->nx) * p->ny * p->nz;
 #pragma omp parallel for schedule(static)
     for (long c = 0; c < N; ++c) {
-        float u = (mask[c] == ORC_WALL || mask[c] == ORC_BODY) ? 0.f : u0;
+        /* kind 2: CPU_3D initialises every node, solids included, at u0 */
+        float u = (kind != 2 && (mask[c] == ORC_WALL || mask[c] == ORC_BODY)) ? 0.f : u0;
         float ff[Q];
         if (kind == 0) {
             float meq[Q];

@@ -69,6 +69,10 @@ typedef struct {
     /* inlet noise (extension, off in parity runs) */
     float noise_amp;
     uint32_t noise_seed;
+    /* CPU_3D semantics: pulls from outside the domain clamp to the edge
+     * (dmin/dmax, CPU:1369-1388); the lid as written (CPU:1010-1023) */
+    int pull_clamp;
+    int lid_quirk;
 } orc_params;
 
 typedef struct {
@@ -93,7 +97,7 @@ void orc_physical_moments(const float* f, float* mom, int n);
 void orc_strain_rate(const float* mom, float* s, int n);
 void orc_invert_les_cf(const float* mom, float* f, int n, float omega_c, float cs, float lrfactor);
 void orc_invert_les_fc(const float* mom, float* f, int n, float omega_f, float cs, float lrfactor);
-void orc_lid(float* f, int n, int face, float ux, float uy, float uz);
+void orc_lid(float* f, int n, int face, float ux, float uy, float uz, int quirk);
 
 /* whole-level operations on compact SoA arrays */
 void orc_init(const orc_params* p, const uint8_t* mask, float* f, int kind, float u0);

@@ -73,7 +73,11 @@ LR7_CONFIGS = {
 CPU3D_PROGRAMS = {
     "c2": dict(XDIM=512, YDIM=128, ZDIM=128, TMAX=8),
     "c2_long": dict(XDIM=512, YDIM=128, ZDIM=128, TMAX=24),
+    # its own lid-driven cavity, small, with the final output.dat kept (parity)
+    "cav24": dict(XDIM=24, YDIM=24, ZDIM=24, TMAX=100),
 }
+# programs whose output.dat is kept
+CPU3D_KEEP_OUTPUT = {"cav24"}
 
 
 def _cut(text: str, start_pat: str, stop_pat: str) -> str:
@@ -117,8 +121,9 @@ def stage(ref_root: Path = REF_ROOT) -> bool:
         s = t
         for k, v in cfg.items():
             s = re.sub(rf"(#define\s+{k}\s+)\S+", rf"\g<1>{v}", s, count=1)
-        # timing harness: the final tecplot dump of every node is not part of the loop
-        s = s.replace('output.open ("output.dat");', "/* output.dat dump disabled for timing */")
+        if name not in CPU3D_KEEP_OUTPUT:
+            # timing harness: the final tecplot dump of every node is not part of the loop
+            s = s.replace('output.open ("output.dat");', "/* output.dat dump disabled for timing */")
         (REF_DIR / f"cpu3d_{name}.cpp").write_text(s)
     return True
 

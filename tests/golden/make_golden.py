@@ -177,6 +177,26 @@ def writer():
     (HERE / "writer_tiny.inputs").write_text(write_inputs_text(L))
 
 
+def cpu3d_cavity():
+    """the reference CPU program's own lid-driven cavity (24^3, MRT with its
+    quirks, 100 steps): u, v, rho of its output.dat"""
+    import os
+    import subprocess
+    import tempfile
+
+    exe = ref_recipe.REF_DIR / "cpu3d_cav24"
+    with tempfile.TemporaryDirectory() as d:
+        r = subprocess.run([str(exe)], cwd=d, capture_output=True, text=True, timeout=120)
+        assert r.returncode == 0, r.stderr
+        lines = open(os.path.join(d, "output.dat")).read().splitlines()[2:]
+    n = 24
+    out = np.zeros((3, n, n, n), np.float32)
+    for line in lines:
+        x, y, z, u, v, w, rho = (float(t) for t in line.split(","))
+        out[:, int(z), int(y), int(x)] = (u, v, rho)
+    np.savez_compressed(HERE / "cpu3d_cavity24.npz", uvrho=out, steps=100)
+
+
 if __name__ == "__main__":
     if not ref_recipe.staged():
         if not ref_recipe.stage():
@@ -185,5 +205,6 @@ if __name__ == "__main__":
     cells()
     runs()
     writer()
+    cpu3d_cavity()
     for p in sorted(HERE.iterdir()):
         print(f"{p.stat().st_size:>9} {p.name}")

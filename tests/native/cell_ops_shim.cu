@@ -20,8 +20,8 @@ void cell_collide_d(int model, int les, double omega, double cs, double dpdy, do
 void cell_extrap(int type, float* f, int n, float rho, float u_in) {
     for (int i = 0; i < n; ++i) extrap<float>(type, f + 19L * i, rho, u_in);
 }
-void cell_lid(float* f, int n, int face, float ux, float uy, float uz) {
-    for (int i = 0; i < n; ++i) lid<float>(f + 19L * i, face, ux, uy, uz);
+void cell_lid(float* f, int n, int face, float ux, float uy, float uz, int quirk) {
+    for (int i = 0; i < n; ++i) lid<float>(f + 19L * i, face, ux, uy, uz, quirk != 0);
 }
 void cell_physical_moments(const float* f, float* mom, int n) {
     for (int i = 0; i < n; ++i) physical_moments<float>(f + 19L * i, mom + 9L * i);

@@ -178,3 +178,40 @@ def test_philox_noise_stream_bit_exact(orc, cellops):
     xs = np.array([orc.orc_noise_uniform(ctypes.c_uint32(12345), ctypes.c_uint32(i), ctypes.c_uint32(1))
                    for i in range(4000)])
     assert abs(xs.mean() - 0.5) < 0.02 and abs(xs.var() - 1 / 12) < 0.01
+
+
+def _cpu3d_cavity_inputs(product, n=24):
+    return product.make_inputs(n, n, n, r1=5.0, re=50.0, umax=0.04, model="MRT_CPU3D", geometry="cavity",
+                               lid_face="-x", lid_velocity=(0.0, 0.04, 0.0), init=2, init_velocity=0.04,
+                               edge_pull="clamp", lid_bc="cpu3d")
+
+
+def test_oracle_vs_reference_cpu_program(golden, product):
+    """the oracle in CPU_3D's semantics (clamped edge pulls, its regularised
+    lid as written, its MRT, every node initialised at UMAX) against the
+    output.dat of the reference CPU program itself (24^3 cavity, 100 steps)"""
+    d = np.load(golden["dir"] / "cpu3d_cavity24.npz")
+    want, steps = d["uvrho"], int(d["steps"])
+    n = 24
+    mask = product.inputs_mask(_cpu3d_cavity_inputs(product)).reshape(n, n, n)
+    assert (mask == 7).sum() == n * n and (mask[:, :, 0] == 7).all()
+    omega = np.float32(1.0) / (np.float32(3.0) * (np.float32(0.04) * np.float32(10.0) / np.float32(50.0)) +
+                               np.float32(0.5))
+    o = OracleRun(n, n, n, mask, float(omega), model=3, init_kind=2, init_u=0.04, lid_u=(0, 0.04, 0), lid_face=0,
+                  pull_clamp=1, lid_quirk=1)
+    o.step(steps)
+    rho, j = moments(o.fa)
+    # the program prints 6 significant digits
+    assert rel_l2(j[:2], want[:2]) < 1e-5
+    assert np.abs(rho - want[2]).max() < 2e-5
+
+
+def test_lid_regularisation_vs_reference(golden, orc, cellops):
+    """CPU_3D's DirichletWest_Regularized, per cell"""
+    c = golden["cells"]
+    f0, want = c["f0"].copy(), c["cpu3d_lid_west"]
+    n = f0.shape[0]
+    for lib, fn in ((orc, "orc_lid"), (cellops, "cell_lid")):
+        g = f0.copy()
+        getattr(lib, fn)(ptr(g), n, 0, F(0.0), F(0.04), F(0.0), 1)
+        np.testing.assert_allclose(g, want, atol=ATOL_CELL, rtol=0, err_msg=fn)

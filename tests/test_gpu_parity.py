@@ -161,6 +161,62 @@ def test_lid_cavity_bgk_vs_oracle(product):
 # FP16 / BF16 store f minus the equilibrium at the inlet velocity; on this
 # small channel (tau0 0.515, 200 steps) the velocity error against the FP64
 # twin is 1.4e-3 (FP16, 11-bit mantissa) and 3.5e-2 (BF16, 8 bits)
+def test_reference_cpu_program_cavity(product, golden):
+    """CPU_3D semantics on the GPU against the reference CPU program's output"""
+    lbm = product
+    d = np.load(golden["dir"] / "cpu3d_cavity24.npz")
+    n = 24
+    text = lbm.make_inputs(n, n, n, r1=5.0, re=50.0, umax=0.04, model="MRT_CPU3D", geometry="cavity", lid_face="-x",
+                           lid_velocity=(0.0, 0.04, 0.0), init=2, init_velocity=0.04, edge_pull="clamp",
+                           lid_bc="cpu3d")
+    with lbm.Solver(text) as s:
+        s.step(int(d["steps"]))
+        f = s.populations()
+    rho, j = moments(f)
+    assert rel_l2(j[:2], d["uvrho"][:2]) < 1e-5
+    assert np.abs(rho - d["uvrho"][2]).max() < 2e-5
+
+
+def _c1(lbm, n, steps, face, lid_u):
+    return lbm.make_inputs(n, n, n, umax=0.05, tmax=steps, model="BGK", geometry="cavity", tau=0.6,
+                           lid_velocity=lid_u, lid_face=face)
+
+
+def test_c1_cavity_64_vs_oracle_and_mass(product):
+    """BGK lid-driven cavity 64^3, tau 0.6, lid on the top face moving +x,
+    equilibrium start at rest, 1000 steps"""
+    lbm = product
+    n, steps = 64, 1000
+    with lbm.Solver(_c1(lbm, n, steps, "+z", (0.05, 0.0, 0.0))) as s:
+        m0 = s.audit()[0]
+        s.step(steps)
+        f, mask, m1 = s.populations(), s.mask(), s.audit()[0]
+    o = OracleRun(n, n, n, mask, 1 / 0.6, model=2, init_kind=1, init_u=0.0, lid_u=(0.05, 0, 0), lid_face=5)
+    o.step(steps)
+    assert _compare(f, o.fa, mask)[0] < RTOL
+    _, j = moments(f)
+    assert j[0].max() > 0.01 and np.isfinite(f).all()   # the lid drives the flow
+    assert abs(m1 - m0) / m0 < 1e-3
+
+
+def test_c1_cavity_axis_permutation(product):
+    """the same cavity in CPU_3D's orientation (lid at x = 0 moving +y) is the
+    axis-permuted image: x' = n-1-z, y' = x, z' = y"""
+    lbm = product
+    n, steps = 64, 300
+    with lbm.Solver(_c1(lbm, n, steps, "+z", (0.05, 0.0, 0.0))) as s:
+        s.step(steps)
+        _, ja = moments(s.populations())
+    with lbm.Solver(_c1(lbm, n, steps, "-x", (0.0, 0.05, 0.0))) as s:
+        s.step(steps)
+        _, jb = moments(s.populations())
+    # jb[c][z', y', x'] with x' = n-1-z, y' = x, z' = y  ->  index jb[:, y, x, n-1-z]
+    jbp = jb[:, :, :, ::-1]              # [c][y][x][z]
+    jbp = np.transpose(jbp, (0, 3, 1, 2))  # [c][z][y][x]
+    mapped = np.stack([jbp[1], jbp[2], -jbp[0]])
+    assert rel_l2(mapped, ja) < 1e-5
+
+
 @pytest.mark.parametrize("prec,tol", [("fp16", 2e-3), ("bf16", 5e-2), ("fp32", 1e-5)])
 def test_storage_precision_vs_fp64(product, prec, tol):
     lbm = product
