@@ -38,16 +38,17 @@ sys.path.insert(0, str(ROOT))
 NX, NY, NZ = 512, 128, 128
 CELLS = NX * NY * NZ
 BYTES_PER_CELL = {"fp32": 152, "fp16": 76, "bf16": 76, "fp64": 304}
-WORKLOAD = ("D3Q19 MRT+Smagorinsky channel 512x128x128, square cylinder side 16 at x=128, tau0=0.52 (RE=120), "
-            "CS=0.01 (Cs=0.1), inlet 0.05 + 1% seeded noise, periodic z, drag/lift every step")
+WORKLOAD = ("D3Q19 MRT+Smagorinsky channel 512x128x128, square cylinder side 16 at x=128 with half-way "
+            "bounce-back, tau0=0.52 (RE=120), CS=0.01 (Cs=0.1), inlet 0.05 + 1% seeded noise, periodic z, "
+            "drag/lift every step")
 
 
-def inputs_text(precision: str, tmax: int) -> str:
+def inputs_text(precision: str, tmax: int, bounceback: str = "halfway") -> str:
     import lbm_multigpu_gb300 as lbm
 
     return lbm.make_inputs(NX, NY, NZ, obst1=(128.5, 63.5, 0.0), r1=8.0, re=120.0, umax=0.05, tmax=tmax, les=1,
                            cs=0.01, model="MRT", geometry="channel_square", precision=precision, inlet_noise=0.01,
-                           seed=12345)
+                           seed=12345, bounceback=bounceback)
 
 
 def peaks() -> dict:
@@ -116,11 +117,12 @@ def dist_setup():
     return world, rank, local
 
 
-def time_precision(precision: str, steps: int, warmup: int, world: int, dist, with_clocks: bool, gpu: int):
+def time_precision(precision: str, steps: int, warmup: int, world: int, dist, with_clocks: bool, gpu: int,
+                   bounceback: str = "halfway"):
     """resident-in-HBM run of `steps` steps after `warmup`; returns (ms, clocks)"""
     import lbm_multigpu_gb300 as lbm
 
-    s = lbm.Solver(inputs_text(precision, warmup + steps + 10))
+    s = lbm.Solver(inputs_text(precision, warmup + steps + 10, bounceback))
     s.step(warmup)
     s.synchronize()
     if dist:
@@ -298,6 +300,11 @@ def main():
     for prec in (("fp16", "bf16") if args.precision == "all" else ()):
         ms, kms, _, _ = time_precision(prec, args.steps, args.warmup, world, dist, False, local)
         res[prec] = (ms, kms)
+    full = None
+    if args.precision == "all":
+        # the reference's own wall treatment (full-way, on-node bounce-back)
+        msf, kmsf, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, "fullway")
+        full = (msf, kmsf)
 
     def worst(ms):
         if not dist:
@@ -349,6 +356,11 @@ def main():
         gbs = CELLS * BYTES_PER_CELL[prec] / (kms * 1e-3) / 1e9
         line[f"{prec}_store"] = dict(value=v, ratio_vs_fp32=v / mlups, ms_per_step=ms / args.steps,
                                      kernel_gbs=gbs, frac=gbs / pk["hbm_gbs"])
+    if full:
+        v = world * CELLS * args.steps / (worst(full[0]) * 1e-3) / 1e6
+        gbs = CELLS * BYTES_PER_CELL["fp32"] / (full[1] * 1e-3) / 1e9
+        line["fp32_fullway_bounceback"] = dict(value=v, ms_per_step=worst(full[0]) / args.steps, kernel_ms=full[1],
+                                               kernel_gbs=gbs, frac=gbs / pk["hbm_gbs"])
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line))

@@ -165,7 +165,7 @@ def make_inputs(nx: int, ny: int, nz: int, *, obst1=(0.0, 0.0, 0.0), r1=1.0, obs
     names = {"geometry": "GEOMETRY:", "precision": "PRECISION:", "tau": "TAU:", "lid_velocity": "LID velocity:",
              "lid_face": "LID face:", "inlet_noise": "Inlet noise:", "seed": "Seed:", "velav": "VELAV:",
              "init": "Init:", "init_velocity": "Init velocity:", "order": "ORDER:", "fc_top_zflip": "FC top zflip:",
-             "edge_pull": "EDGE PULL:", "lid_bc": "LID BC:"}
+             "edge_pull": "EDGE PULL:", "lid_bc": "LID BC:", "bounceback": "BOUNCEBACK:"}
     for k, v in ext.items():
         if k not in names:
             raise KeyError(f"unknown .inputs extension key {k!r}")

@@ -88,6 +88,7 @@ struct Config {
     int order = 2;
     int fc_zflip = 1;
     int pull_clamp = 0;             /* "EDGE PULL: clamp" (CPU_3D) or "wrap" */
+    int halfway = 0;                /* "BOUNCEBACK: halfway" or "fullway" (the reference) */
     int lid_quirk = 0;              /* "LID BC: cpu3d" reproduces CPU_3D's lid as written */
     /* older records spell the LES line "Smagorinski LES: YES/NO"; DynInlet
      * records add "KP" (the inlet P-control gain, MRTtest/DynInlet3.cu:26) */
@@ -190,6 +191,10 @@ int parse_inputs(const char* text, Config& c) {
             ok = (val == "clamp" || val == "wrap");
             c.pull_clamp = val == "clamp";
         }
+        else if (key == "BOUNCEBACK") {
+            ok = (val == "halfway" || val == "fullway");
+            c.halfway = val == "halfway";
+        }
         else if (key == "LID BC") {
             ok = (val == "cpu3d" || val == "regularized");
             c.lid_quirk = val == "cpu3d";
@@ -283,6 +288,7 @@ std::string value_of(const Config& c, const std::string& key, float omega, float
     else if (key == "FC top zflip") o << c.fc_zflip;
     else if (key == "EDGE PULL") o << (c.pull_clamp ? "clamp" : "wrap");
     else if (key == "LID BC") o << (c.lid_quirk ? "cpu3d" : "regularized");
+    else if (key == "BOUNCEBACK") o << (c.halfway ? "halfway" : "fullway");
     return o.str();
 }
 
@@ -338,6 +344,7 @@ std::string write_inputs(const Config& c, float omega, float omegaLR) {
     if (c.fc_zflip != d.fc_zflip) line("FC top zflip: ", "FC top zflip");
     if (c.pull_clamp) line("EDGE PULL: ", "EDGE PULL");
     if (c.lid_quirk) line("LID BC: ", "LID BC");
+    if (c.halfway) line("BOUNCEBACK: ", "BOUNCEBACK");
     return o.str();
 }
 
@@ -419,6 +426,8 @@ struct LevelState {
     int nbody = 0;
     double* fpart = nullptr;        /* per-block force partials */
     unsigned* done = nullptr;       /* blocks finished in the force kernel (reset by its last block) */
+    bool has_lid = false;           /* the mask has LID nodes */
+    uint32_t* links = nullptr;      /* device, per node: bit q = pull source of q is solid */
 };
 
 }  // namespace
@@ -457,6 +466,7 @@ void free_level(LevelState& s) {
     cudaFree(s.body);
     cudaFree(s.fpart);
     cudaFree(s.done);
+    cudaFree(s.links);
     s = LevelState();
 }
 
@@ -502,24 +512,57 @@ int alloc_level(LevelState& s, int nx, int ny, int nz, int storage, bool stats, 
     return LBM_OK;
 }
 
+/* Upload a level's mask (pitched) with the NEAR_SOLID flag on non-solid nodes
+ * that pull from a solid neighbour, and build the force list: BODY nodes for
+ * full-way bounce-back, the fluid nodes next to BODY nodes for half-way. */
 int upload_mask(lbm_handle* h, int level) {
     LevelState& s = h->lv[level];
     const Level& L = s.L;
+    const bool clamp = h->cfg.pull_clamp, halfway = h->cfg.halfway;
     std::vector<uint8_t> pitched(size_t(L.qstride), WALL);
+    auto type_at = [&](int x, int y, int z) { return s.hmask[(size_t(z) * L.ny + y) * L.nx + x]; };
+    auto nb = [&](int i, int n) { return i < 0 ? (clamp ? 0 : i + n) : (i >= n ? (clamp ? n - 1 : i - n) : i); };
+    static const int CX[19] = {0, 1, 0, -1, 0, 1, -1, -1, 1, 0, 1, 0, -1, 0, 0, 1, 0, -1, 0};
+    static const int CY[19] = {0, 0, 1, 0, -1, 1, 1, -1, -1, 0, 0, 1, 0, -1, 0, 0, 1, 0, -1};
+    static const int CZ[19] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, -1, -1, -1, -1, -1};
+    std::vector<unsigned> list;
+    std::vector<uint32_t> links(halfway ? size_t(L.qstride) : 0, 0u);
+    s.has_lid = std::find(s.hmask.begin(), s.hmask.end(), uint8_t(LID)) != s.hmask.end();
     for (int z = 0; z < L.nz; ++z)
         for (int y = 0; y < L.ny; ++y)
-            memcpy(&pitched[size_t(z) * L.plane + size_t(y) * L.pitch], &s.hmask[(size_t(z) * L.ny + y) * L.nx], L.nx);
-    std::vector<unsigned> body;
-    for (size_t i = 0; i < pitched.size(); ++i)
-        if (pitched[i] == BODY) body.push_back(unsigned(i));
+            for (int x = 0; x < L.nx; ++x) {
+                const uint8_t t = type_at(x, y, z);
+                const size_t pc = size_t(z) * L.plane + size_t(y) * L.pitch + x;
+                uint8_t m = t;
+                bool near_solid = false, near_body = false;
+                uint32_t lk = 0;
+                if (t != WALL && t != BODY) {
+                    for (int q = 1; q < 19; ++q) {
+                        const uint8_t u = type_at(nb(x - CX[q], L.nx), nb(y - CY[q], L.ny), nb(z - CZ[q], L.nz));
+                        near_solid |= (u == WALL || u == BODY);
+                        near_body |= (u == BODY);
+                        if (u == WALL || u == BODY) lk |= 1u << q;
+                    }
+                }
+                if (halfway) links[pc] = lk;
+                if (near_solid) m |= NEAR_SOLID;
+                pitched[pc] = m;
+                if (halfway ? near_body : (t == BODY)) list.push_back(unsigned(pc));
+            }
     CUDA_TRY(cudaMemcpyAsync(s.mask, pitched.data(), pitched.size(), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
+    cudaFree(s.links);
+    s.links = nullptr;
+    if (halfway) {
+        CUDA_TRY(cudaMalloc(&s.links, links.size() * sizeof(uint32_t)));
+        CUDA_TRY(cudaMemcpy(s.links, links.data(), links.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    }
     cudaFree(s.body);
     s.body = nullptr;
-    s.nbody = int(body.size());
-    if (!body.empty()) {
-        CUDA_TRY(cudaMalloc(&s.body, body.size() * sizeof(unsigned)));
-        CUDA_TRY(cudaMemcpy(s.body, body.data(), body.size() * sizeof(unsigned), cudaMemcpyHostToDevice));
+    s.nbody = int(list.size());
+    if (!list.empty()) {
+        CUDA_TRY(cudaMalloc(&s.body, list.size() * sizeof(unsigned)));
+        CUDA_TRY(cudaMemcpy(s.body, list.data(), list.size() * sizeof(unsigned), cudaMemcpyHostToDevice));
     }
     return LBM_OK;
 }
@@ -558,6 +601,8 @@ StepParams base_params(const lbm_handle* h, int level) {
     p.lid_face = c.lid_face;
     p.lid_quirk = c.lid_quirk;
     p.pull_clamp = c.pull_clamp;
+    p.halfway = c.halfway;
+    p.has_lid = h->lv[level].has_lid ? 1 : 0;
     p.stats_on = c.velav;
     p.start_av = c.start_av;
     p.start_fluc = c.start_fluc;
@@ -605,8 +650,8 @@ int one_step(lbm_handle* h) {
     }
     if (p.force_on)
         CUDA_TRY(launch_force(C.L, C.f[C.cur], C.body, C.nbody, C.fpart, C.done, h->force_hist + 3LL * fidx,
-                              h->stream));
-    CUDA_TRY(launch_stream_collide(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, h->mom, h->stream));
+                              h->stream, C.mask, c.halfway));
+    CUDA_TRY(launch_stream_collide(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, h->mom, h->stream, C.links));
     C.cur = 1 - C.cur;
     if (c.refinement) {
         LevelState& Fn = h->lv[1];
@@ -621,9 +666,9 @@ int one_step(lbm_handle* h) {
             }
             if (pf.force_on)
                 CUDA_TRY(launch_force(Fn.L, Fn.f[Fn.cur], Fn.body, Fn.nbody, Fn.fpart, Fn.done,
-                                      h->force_hist + 3LL * fidx, h->stream));
+                                      h->force_hist + 3LL * fidx, h->stream, Fn.mask, c.halfway));
             CUDA_TRY(launch_stream_collide(Fn.L, pf, Fn.f[Fn.cur], Fn.f[1 - Fn.cur], Fn.mask, Fn.stats, nullptr,
-                                           h->stream));
+                                           h->stream, Fn.links));
             Fn.cur = 1 - Fn.cur;
         }
         CUDA_TRY(launch_interp_cf(h->rp, Fn.L, h->mom, Fn.f[Fn.cur], Fn.mask, h->stream));
@@ -994,7 +1039,8 @@ int lbm_time_stream_collide(lbm_handle* h, int level, int n, float* ms) {
     p.stats_on = 0;
     CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
     for (int i = 0; i < n; ++i) {
-        CUDA_TRY(launch_stream_collide(s.L, p, s.f[s.cur], s.f[1 - s.cur], s.mask, nullptr, nullptr, h->stream));
+        CUDA_TRY(launch_stream_collide(s.L, p, s.f[s.cur], s.f[1 - s.cur], s.mask, nullptr, nullptr, h->stream,
+                                       s.links));
         s.cur = 1 - s.cur;
     }
     CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
@@ -1158,6 +1204,7 @@ int lbm_stream_collide_f32(const float* fA, float* fB, const uint8_t* mask, int 
     p.rho_out = rho_out;
     p.t = t;
     p.stats_weight = 1.f;
+    p.has_lid = 1; /* the caller's mask may hold any node type */
     CUDA_TRY(launch_stream_collide(L, p, fA, fB, mask, nullptr, nullptr, (cudaStream_t)cuda_stream));
     return LBM_OK;
 }

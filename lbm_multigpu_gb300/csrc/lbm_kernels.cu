@@ -53,12 +53,17 @@ template <> struct Fmt<__nv_bfloat16> {
     }
 };
 
-template <class S>
+/* FEAT: compile-time features, chosen at launch from the configuration and
+ * the node types present, so a channel kernel carries no lid code (whose
+ * 19-entry temporaries would otherwise set every variant's register count) */
+constexpr int FEAT_HALFWAY = 1, FEAT_LID = 2, FEAT_CLAMP = 4;
+template <class S, int FEAT>
 __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, const StepParams p,
                                                                   const S* __restrict__ fA, S* __restrict__ fB,
                                                                   const uint8_t* __restrict__ mask,
                                                                   float* __restrict__ stats,
-                                                                  float* __restrict__ mom_export) {
+                                                                  float* __restrict__ mom_export,
+                                                                  const uint32_t* __restrict__ links) {
     using F = Fmt<S>;
     using T = typename F::T;
     const int x = blockIdx.x * SC_BX + threadIdx.x;
@@ -70,10 +75,14 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
     const unsigned qs = unsigned(L.qstride);
     const unsigned plane = unsigned(L.plane), pitch = unsigned(L.pitch);
     const unsigned c = z * plane + y * pitch + x;
-    const int type = mask[c];
+    const int mbyte = mask[c];
+    const int type = mbyte & TYPE_MASK;
+    /* half-way bounce-back leaves solid nodes untouched: nothing pulls from them */
+    constexpr bool HALFWAY = (FEAT & FEAT_HALFWAY) != 0;
+    if (HALFWAY && (type == WALL || type == BODY)) return;
     /* periodic neighbours; only boundary nodes, whose pulled values the
      * reference discards or bounces, ever wrap in x or y */
-    const bool cl = p.pull_clamp != 0;
+    constexpr bool cl = (FEAT & FEAT_CLAMP) != 0;
     const unsigned xm = (x == 0) ? (cl ? 0 : L.nx - 1) : x - 1;
     const unsigned xp = (x == L.nx - 1) ? (cl ? x : 0) : x + 1;
     const unsigned ym = (y == 0) ? (cl ? 0 : L.ny - 1) : y - 1;
@@ -90,6 +99,15 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
         /* pull: the value arriving from x - c_q */
         const unsigned src = q * qs + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)];
         f[q] = F::ld(fA + src, L.off[q]);
+    }
+    if (HALFWAY && (mbyte & NEAR_SOLID)) {
+        /* a population that would come from a solid node is the node's own
+         * post-collision population of the opposite direction, reflected
+         * half-way to the solid; links has bit q set for those q */
+        const uint32_t lk = links[c];
+#pragma unroll
+        for (int q = 1; q < 19; ++q)
+            if (lk & (1u << q)) f[q] = F::ld(fA + opp(q) * qs + c, L.off[opp(q)]);
     }
 
     if (type == WALL || type == BODY) {
@@ -114,7 +132,7 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
                 uin = uin + T(p.u_in) * T(p.noise_amp) * (T(2) * T(xi) - T(1));
             }
             extrap<T>(type, f, T(p.rho_out), uin);
-        } else if (type == LID) {
+        } else if ((FEAT & FEAT_LID) && type == LID) {
             lid<T>(f, p.lid_face, T(p.lid_u[0]), T(p.lid_u[1]), T(p.lid_u[2]), p.lid_quirk != 0);
         }
         collide<T>(p.model, f, T(p.omega), p.les != 0, T(p.cs), T(p.dpdy));
@@ -177,7 +195,8 @@ template <class S>
 __global__ void __launch_bounds__(FORCE_THREADS) k_force_list(const Level L, const S* __restrict__ fA,
                                                               const unsigned* __restrict__ body, int nbody,
                                                               double* __restrict__ part, unsigned* __restrict__ done,
-                                                              double* __restrict__ out3) {
+                                                              double* __restrict__ out3,
+                                                              const uint8_t* __restrict__ mask, int halfway) {
     using F = Fmt<S>;
     using T = typename F::T;
     double s[3] = {0.0, 0.0, 0.0};
@@ -193,12 +212,26 @@ __global__ void __launch_bounds__(FORCE_THREADS) k_force_list(const Level L, con
         const unsigned yb[3] = {ym * pitch, y * pitch, yp * pitch};
         const unsigned xs[3] = {xm, x, xp};
         T a[3] = {0, 0, 0};
+        if (halfway) {
+            /* link-wise exchange at a fluid node next to the body: each
+             * population heading into a BODY node (opp(q), arriving back as q)
+             * hands over 2 c_opp(q) f*_opp(q) */
 #pragma unroll
-        for (int q = 1; q < 19; ++q) {
-            const T v = T(2) * F::ld(fA + q * qs + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)], L.off[q]);
-            if (cx(q)) a[0] += T(cx(q)) * v;
-            if (cy(q)) a[1] += T(cy(q)) * v;
-            if (cz(q)) a[2] += T(cz(q)) * v;
+            for (int q = 1; q < 19; ++q) {
+                if ((mask[zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)]] & TYPE_MASK) != BODY) continue;
+                const T v = T(2) * F::ld(fA + opp(q) * qs + c, L.off[opp(q)]);
+                if (cx(q)) a[0] -= T(cx(q)) * v;
+                if (cy(q)) a[1] -= T(cy(q)) * v;
+                if (cz(q)) a[2] -= T(cz(q)) * v;
+            }
+        } else {
+#pragma unroll
+            for (int q = 1; q < 19; ++q) {
+                const T v = T(2) * F::ld(fA + q * qs + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)], L.off[q]);
+                if (cx(q)) a[0] += T(cx(q)) * v;
+                if (cy(q)) a[1] += T(cy(q)) * v;
+                if (cz(q)) a[2] += T(cz(q)) * v;
+            }
         }
 #pragma unroll
         for (int k = 0; k < 3; ++k) s[k] += double(a[k]);
@@ -270,7 +303,7 @@ __global__ void k_init(const Level L, const uint8_t* __restrict__ mask, S* __res
     const int x = blockIdx.x * SC_BX + threadIdx.x, y = blockIdx.y * SC_BY + threadIdx.y, z = blockIdx.z;
     if (x >= L.nx || y >= L.ny) return;
     const long long c = z * L.plane + (long long)y * L.pitch + x;
-    const int type = mask[c];
+    const int type = mask[c] & TYPE_MASK;
     const T u = (kind != 2 && (type == WALL || type == BODY)) ? T(0) : T(u0);
     T g[19];
     if (kind == 0) {
@@ -345,7 +378,7 @@ __global__ void __launch_bounds__(256) k_audit(const Level L, const S* __restric
         const int y = int(r % L.ny), z = int(r / L.ny);
         for (int x = lane; x < L.nx; x += 32) {
             const long long c = z * L.plane + (long long)y * L.pitch + x;
-            const int t = mask[c];
+            const int t = mask[c] & TYPE_MASK;
             if (t == WALL || t == BODY) continue;
             typename F::T m[4] = {0, 0, 0, 0};
 #pragma unroll
@@ -453,7 +486,7 @@ __global__ void k_interp_cf(const RefineParams r, const Level F, const float* __
         yf = b < L ? b : r.fny - 2 * L + b;
     }
     const long long cf = k * F.plane + (long long)yf * F.pitch + xf;
-    const int t = mask_f[cf];
+    const int t = mask_f[cf] & TYPE_MASK;
     if (t == WALL || t == BODY) return;
     const float xr = xf * r.lrfactor + r.lrfactor * 0.5f, yr = yf * r.lrfactor + r.lrfactor * 0.5f;
     const int xm = int(xr), ym = int(yr);
@@ -513,7 +546,7 @@ __global__ void k_interp_fc(const RefineParams r, const Level C, const Level F, 
     if (xi >= nxi || yi >= nyi) return;
     const int x = x0 + xi, y = y0 + yi;
     const long long cc = z * C.plane + (long long)y * C.pitch + x;
-    const int t = mask_c[cc];
+    const int t = mask_c[cc] & TYPE_MASK;
     if (t == WALL || t == BODY) return;
     const int L = r.lrlevel;
     const int xm = int(L * (x - r.lrx0)), ym = int(L * (y - r.lry0));
@@ -581,20 +614,35 @@ __global__ void k_interp_fc(const RefineParams r, const Level C, const Level F, 
     }
 
 cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const void* fA, void* fB, const uint8_t* mask,
-                                  float* stats, float* mom_export, cudaStream_t s) {
+                                  float* stats, float* mom_export, cudaStream_t s, const uint32_t* links) {
+    if (p.halfway && !links) return cudaErrorInvalidValue;
     const dim3 block(SC_BX, SC_BY), grid = sc_grid(L);
-    LBM_DISPATCH(L.storage, (k_stream_collide<S><<<grid, block, 0, s>>>(L, p, (const S*)fA, (S*)fB, mask, stats,
-                                                                         mom_export)));
+    const int feat = (p.halfway ? FEAT_HALFWAY : 0) | (p.has_lid ? FEAT_LID : 0) | (p.pull_clamp ? FEAT_CLAMP : 0);
+#define LBM_SC(FT) \
+    LBM_DISPATCH(L.storage, (k_stream_collide<S, FT><<<grid, block, 0, s>>>(L, p, (const S*)fA, (S*)fB, mask, stats, \
+                                                                             mom_export, links)))
+    switch (feat) {
+        case 0: LBM_SC(0); break;
+        case 1: LBM_SC(1); break;
+        case 2: LBM_SC(2); break;
+        case 3: LBM_SC(3); break;
+        case 4: LBM_SC(4); break;
+        case 5: LBM_SC(5); break;
+        case 6: LBM_SC(6); break;
+        default: LBM_SC(7); break;
+    }
+#undef LBM_SC
     return cudaGetLastError();
 }
 
 int force_partials() { return FORCE_BLOCKS; }
 
 cudaError_t launch_force(const Level& L, const void* fA, const unsigned* body, int nbody, double* partials,
-                         unsigned* done, double* out3, cudaStream_t s) {
+                         unsigned* done, double* out3, cudaStream_t s, const uint8_t* mask, int halfway) {
     if (nbody <= 0) return cudaSuccess;
     LBM_DISPATCH(L.storage, (k_force_list<S><<<FORCE_BLOCKS, FORCE_THREADS, 0, s>>>(L, (const S*)fA, body, nbody,
-                                                                                    partials, done, out3)));
+                                                                                    partials, done, out3, mask,
+                                                                                    halfway)));
     return cudaGetLastError();
 }
 
@@ -611,7 +659,7 @@ __global__ void __launch_bounds__(256) k_force_scan(const Level L, const S* __re
     for (long long r = (long long)blockIdx.x * 8 + warp; r < rows; r += (long long)gridDim.x * 8) {
         const int y = int(r % L.ny), z = int(r / L.ny);
         for (int x = lane; x < L.nx; x += 32) {
-            if (mask[z * L.plane + (long long)y * L.pitch + x] != BODY) continue;
+            if ((mask[z * L.plane + (long long)y * L.pitch + x] & TYPE_MASK) != BODY) continue;
             const int xm = (x == 0) ? L.nx - 1 : x - 1, xp = (x == L.nx - 1) ? 0 : x + 1;
             const int ym = (y == 0) ? L.ny - 1 : y - 1, yp = (y == L.ny - 1) ? 0 : y + 1;
             const int zm = (z == 0) ? L.nz - 1 : z - 1, zp = (z == L.nz - 1) ? 0 : z + 1;

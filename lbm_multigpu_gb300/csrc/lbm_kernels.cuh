@@ -9,7 +9,10 @@
 
 namespace lbm {
 
-/* node types of the one-byte mask; numbering shared with include/lbm_gb300.h */
+/* node types of the one-byte mask; numbering shared with include/lbm_gb300.h.
+ * In the device copy bit 7 (NEAR_SOLID) marks non-solid nodes with a solid
+ * neighbour; the type is mask & TYPE_MASK. */
+constexpr uint8_t NEAR_SOLID = 0x80, TYPE_MASK = 0x7F;
 enum NodeType : uint8_t {
     FLUID = 0,
     WALL = 1,
@@ -47,6 +50,9 @@ struct StepParams {
     int lid_face;
     int lid_quirk;         /* CPU_3D's regularised lid as written (CPU:1010-1023) */
     int pull_clamp;        /* pulls from outside the domain clamp to the edge (CPU:1369-1388) instead of wrapping */
+    int halfway;           /* half-way bounce-back: a pull from a solid node returns the node's own
+                            * opposite post-collision population; solids are not updated */
+    int has_lid;           /* the level's mask contains LID nodes */
     int force_on;          /* accumulate momentum exchange at BODY nodes */
     int t;                 /* time step index (stats, noise) */
     int stats_on, start_av, start_fluc;
@@ -67,11 +73,15 @@ inline int sc_blocks(const Level& L) {
 }
 
 /* kernel launchers (lbm_kernels.cu) */
+/* links: per node, bit q set when the pull source of population q is a solid
+ * node (read only by NEAR_SOLID nodes; needed for half-way bounce-back) */
 cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const void* fA, void* fB,
-                                  const uint8_t* mask, float* stats, float* mom_export, cudaStream_t s);
+                                  const uint8_t* mask, float* stats, float* mom_export, cudaStream_t s,
+                                  const uint32_t* links = nullptr);
 /* FP64 momentum exchange over a list of BODY nodes (pitched indices), ADDED to out3 */
 cudaError_t launch_force(const Level& L, const void* fA, const unsigned* body, int nbody, double* partials,
-                         unsigned* done, double* out3, cudaStream_t s);
+                         unsigned* done, double* out3, cudaStream_t s, const uint8_t* mask = nullptr,
+                         int halfway = 0);
 int force_partials();
 /* the same sum found by scanning the mask; partials holds force_scan_partials()*3 doubles */
 cudaError_t launch_force_scan(const Level& L, const void* fA, const uint8_t* mask, double* partials, double* out3,

@@ -438,6 +438,8 @@ void step_impl(const orc_params* p, const uint8_t* mask, const T* fA, T* fB, dou
             for (int x = 0; x < nx; ++x) {
                 const long c = (long(z) * ny + y) * nx + x;
                 const int im = mask[c];
+                /* half-way bounce-back: solid nodes are not updated */
+                if (p->halfway && (im == ORC_WALL || im == ORC_BODY)) continue;
                 T f[Q];
                 /* pull (LR7:1445-1491); the reference's z halo planes become a
                  * periodic wrap, x/y wrap only reaches boundary nodes whose
@@ -446,6 +448,20 @@ void step_impl(const orc_params* p, const uint8_t* mask, const T* fA, T* fB, dou
                     const int cl = p->pull_clamp;
                     int xs = edge(x - CX[q], nx, cl), ys = edge(y - CY[q], ny, cl), zs = edge(z - CZ[q], nz, cl);
                     f[q] = fA[q * N + (long(zs) * ny + ys) * nx + xs];
+                    if (p->halfway && q > 0) {
+                        const int nt = mask[(long(zs) * ny + ys) * nx + xs];
+                        if (nt == ORC_WALL || nt == ORC_BODY) {
+                            /* the node's own opposite population, reflected half-way */
+                            f[q] = fA[OPP[q] * N + c];
+                            if (nt == ORC_BODY && p->force_on) {
+                                /* link-wise momentum exchange: 2 c_opp(q) f*_opp(q) */
+                                const double v = 2.0 * double(f[q]);
+                                fx -= CX[q] * v;
+                                fy -= CY[q] * v;
+                                fz -= CZ[q] * v;
+                            }
+                        }
+                    }
                 }
                 if (im == ORC_WALL || im == ORC_BODY) {
                     /* full-way bounce-back + momentum exchange (LR7:1493-1526) */

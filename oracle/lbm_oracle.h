@@ -73,6 +73,8 @@ typedef struct {
      * (dmin/dmax, CPU:1369-1388); the lid as written (CPU:1010-1023) */
     int pull_clamp;
     int lid_quirk;
+    /* half-way bounce-back (extension; the reference is full-way) */
+    int halfway;
 } orc_params;
 
 typedef struct {

@@ -161,6 +161,28 @@ def test_lid_cavity_bgk_vs_oracle(product):
 # FP16 / BF16 store f minus the equilibrium at the inlet velocity; on this
 # small channel (tau0 0.515, 200 steps) the velocity error against the FP64
 # twin is 1.4e-3 (FP16, 11-bit mantissa) and 3.5e-2 (BF16, 8 bits)
+@pytest.mark.parametrize("model,les", [("MRT", 1), ("BGK", 0)])
+def test_halfway_bounceback_vs_oracle(product, model, les):
+    """half-way bounce-back (the channel configuration's wall treatment; the
+    reference is full-way): velocity and the link-wise drag/lift"""
+    lbm = product
+    steps = 200
+    with lbm.Solver(_chan_inputs(lbm, steps, model=model, les=les, bounceback="halfway")) as s:
+        s.step(steps)
+        f, mask, om, F = s.populations(), s.mask(), s.params()["omega"], s.forces()
+    o = OracleRun(NX, NY, NZ, mask, om, model=lbm.MODELS[model], les=les, cs=0.01,
+                  init_kind=1 if model == "BGK" else 0, init_u=0.05, halfway=1)
+    o.step(steps)
+    err, drho = _compare(f, o.fa, mask)
+    assert err < RTOL and drho < 1e-5, (err, drho)
+    Fo = np.array(o.forces)[: len(F)]
+    assert rel_l2(F[:, 0], Fo[:, 0]) < FTOL and F[-1, 0] > 0
+    with lbm.Solver(_chan_inputs(lbm, steps, model=model, les=les)) as s:
+        s.step(steps)
+        F_full = s.forces()
+    assert abs(F_full[-1, 0] - F[-1, 0]) > 1e-3 * abs(F[-1, 0])   # a different wall position, a different drag
+
+
 def test_reference_cpu_program_cavity(product, golden):
     """CPU_3D semantics on the GPU against the reference CPU program's output"""
     lbm = product
