@@ -9,6 +9,7 @@
  *   pull streaming (LR7:1445-1491) with the z halo planes replaced by a
  *   periodic index wrap inside one domain,
  *   full-way bounce-back + momentum exchange (LR7:1493-1526, 1607-1626),
+ *   or half-way bounce-back through per-node link masks,
  *   inlet/outlet rebuilds (LR7:1531-1561), the moving lid,
  *   MRT/BGK collision with Smagorinsky (LR7:583-711, DI3:599-832),
  *   running statistics (LR7:1567-1584),
@@ -77,9 +78,10 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
     const unsigned c = z * plane + y * pitch + x;
     const int mbyte = mask[c];
     const int type = mbyte & TYPE_MASK;
-    /* half-way bounce-back leaves solid nodes untouched: nothing pulls from them */
+    /* under half-way bounce-back nothing pulls from a solid node, which still
+     * runs the full-way branch below: an early return here would make the
+     * population loads of every warp wait for the mask byte */
     constexpr bool HALFWAY = (FEAT & FEAT_HALFWAY) != 0;
-    if (HALFWAY && (type == WALL || type == BODY)) return;
     /* periodic neighbours; only boundary nodes, whose pulled values the
      * reference discards or bounces, ever wrap in x or y */
     constexpr bool cl = (FEAT & FEAT_CLAMP) != 0;

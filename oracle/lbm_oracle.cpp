@@ -438,8 +438,9 @@ void step_impl(const orc_params* p, const uint8_t* mask, const T* fA, T* fB, dou
             for (int x = 0; x < nx; ++x) {
                 const long c = (long(z) * ny + y) * nx + x;
                 const int im = mask[c];
-                /* half-way bounce-back: solid nodes are not updated */
-                if (p->halfway && (im == ORC_WALL || im == ORC_BODY)) continue;
+                /* half-way bounce-back: solid nodes keep the full-way update
+                 * (their values are never pulled by a fluid node) */
+                const bool hw = p->halfway && im != ORC_WALL && im != ORC_BODY;
                 T f[Q];
                 /* pull (LR7:1445-1491); the reference's z halo planes become a
                  * periodic wrap, x/y wrap only reaches boundary nodes whose
@@ -448,7 +449,7 @@ void step_impl(const orc_params* p, const uint8_t* mask, const T* fA, T* fB, dou
                     const int cl = p->pull_clamp;
                     int xs = edge(x - CX[q], nx, cl), ys = edge(y - CY[q], ny, cl), zs = edge(z - CZ[q], nz, cl);
                     f[q] = fA[q * N + (long(zs) * ny + ys) * nx + xs];
-                    if (p->halfway && q > 0) {
+                    if (hw && q > 0) {
                         const int nt = mask[(long(zs) * ny + ys) * nx + xs];
                         if (nt == ORC_WALL || nt == ORC_BODY) {
                             /* the node's own opposite population, reflected half-way */
@@ -465,7 +466,7 @@ void step_impl(const orc_params* p, const uint8_t* mask, const T* fA, T* fB, dou
                 }
                 if (im == ORC_WALL || im == ORC_BODY) {
                     /* full-way bounce-back + momentum exchange (LR7:1493-1526) */
-                    if (im == ORC_BODY && p->force_on) {
+                    if (im == ORC_BODY && p->force_on && !p->halfway) {
                         double sx = 0, sy = 0, sz = 0;
                         for (int q = 1; q < Q; ++q) {
                             sx += 2.0 * CX[q] * double(f[q]);
