@@ -128,24 +128,27 @@ def time_precision(precision: str, steps: int, warmup: int, world: int, dist, wi
     if dist:
         dist.barrier()
     clocks = None
+    n0 = s.launch_count()
     if with_clocks:
         with ClockSampler(gpu) as cs:
             ms = s.step_timed(steps)
         clocks = cs.summary()
     else:
         ms = s.step_timed(steps)
+    launches = s.launch_count() - n0
     if dist:
         dist.barrier()
     kernel_ms = s.time_stream_collide(20)
     audit = s.audit()
     s.close()
-    return ms, kernel_ms, clocks, audit
+    return ms, kernel_ms, clocks, audit, launches
 
 
 def time_e2e(steps: int, world: int, dist) -> dict:
     """the same workload through the public API with host buffers in the
-    timed region: pinned initial populations in, each step's force out,
-    final populations out"""
+    timed region: pinned initial populations in, each step's force out
+    (queued into pinned memory, read once the loop has drained), final
+    populations out"""
     import numpy as np
     import torch
 
@@ -156,7 +159,7 @@ def time_e2e(steps: int, world: int, dist) -> dict:
     host_in = torch.empty(f0.shape, dtype=torch.float32, pin_memory=True).numpy()
     host_in[...] = f0
     host_out = torch.empty(f0.shape, dtype=torch.float32, pin_memory=True).numpy()
-    force = np.zeros((steps, 3))
+    force = torch.zeros((steps, 3), dtype=torch.float64, pin_memory=True).numpy()
     s.init_equilibrium()
     if dist:
         dist.barrier()
@@ -164,7 +167,7 @@ def time_e2e(steps: int, world: int, dist) -> dict:
     s.set_populations(host_in)
     for i in range(steps):
         s.step(1)
-        force[i] = s.last_force()
+        s.last_force_async(force[i])
     host_out[...] = s.populations()
     t1 = time.perf_counter()
     if dist:
@@ -295,15 +298,15 @@ def main():
 
     # FP32 Smagorinsky (the reference point), then the FP16 / BF16 stores
     main_prec = "fp32" if args.precision == "all" else args.precision
-    ms32, kms32, clocks, audit = time_precision(main_prec, args.steps, args.warmup, world, dist, True, local)
+    ms32, kms32, clocks, audit, launches = time_precision(main_prec, args.steps, args.warmup, world, dist, True, local)
     res = {}
     for prec in (("fp16", "bf16") if args.precision == "all" else ()):
-        ms, kms, _, _ = time_precision(prec, args.steps, args.warmup, world, dist, False, local)
+        ms, kms, _, _, _ = time_precision(prec, args.steps, args.warmup, world, dist, False, local)
         res[prec] = (ms, kms)
     full = None
     if args.precision == "all":
         # the reference's own wall treatment (full-way, on-node bounce-back)
-        msf, kmsf, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, "fullway")
+        msf, kmsf, _, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, "fullway")
         full = (msf, kmsf)
 
     def worst(ms):
@@ -347,7 +350,7 @@ def main():
         e2e=None if not e2e else dict(value=world * CELLS * min(args.steps, 2000) / e2e_sec / 1e6, unit="MLUPS",
                                       h2d_bytes_per_step=e2e["h2d"], d2h_bytes_per_step=e2e["d2h"],
                                       steps=min(args.steps, 2000)),
-        gpu_launches=args.steps * 3,
+        gpu_launches=launches * world,
         clocks=clocks,
         audit=dict(mass=float(audit[0]), momentum=[float(a) for a in audit[1:]]),
     )

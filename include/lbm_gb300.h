@@ -122,6 +122,18 @@ int lbm_get_forces(lbm_handle* h, double* fxyz, int max_steps, int* n);
 /* the force of the last step (3 doubles; zeros before STARTF) */
 int lbm_get_last_force(lbm_handle* h, double* f3);
 
+/* the same copy queued on the handle's stream without waiting: f3 (pinned
+ * host memory for a truly asynchronous copy) holds the force once
+ * lbm_synchronize returns; lets a monitor read every step's drag without
+ * stalling the step loop.  No reference counterpart (the reference copies its
+ * force arrays once, after the loop, LR7:2970-2980) */
+int lbm_get_last_force_async(lbm_handle* h, double* f3);
+
+/* number of kernels the handle has launched since lbm_create (all levels,
+ * every entry point that takes the handle); instrumentation with no
+ * counterpart in the reference */
+int lbm_get_launch_count(const lbm_handle* h, long long* n);
+
 /* FP64 mass and momentum of the non-solid nodes of a level: out4 = {M, Jx, Jy, Jz} */
 int lbm_audit(lbm_handle* h, int level, double* out4);
 

@@ -58,6 +58,8 @@ SIGNATURES = [
     ("lbm_get_stats", _I, [_P, _I, _P]),
     ("lbm_get_forces", _I, [_P, _P, _I, ctypes.POINTER(_I)]),
     ("lbm_get_last_force", _I, [_P, _P]),
+    ("lbm_get_last_force_async", _I, [_P, _P]),
+    ("lbm_get_launch_count", _I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     ("lbm_time_stream_collide", _I, [_P, _I, _I, ctypes.POINTER(_F)]),
     ("lbm_audit", _I, [_P, _I, _P]),
     ("lbm_write_inputs", _I, [_P, ctypes.c_char_p, _SZ, ctypes.POINTER(_SZ)]),
@@ -328,6 +330,19 @@ class Solver:
         f = np.zeros(3, np.float64)
         _check(self._lib.lbm_get_last_force(self._h, _ptr(f)))
         return f
+
+    def last_force_async(self, out: np.ndarray) -> None:
+        """queue the copy of the last step's force into out (3 float64,
+        ideally pinned); valid after synchronize()"""
+        if out.dtype != np.float64 or out.size < 3 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a contiguous float64 array of 3")
+        _check(self._lib.lbm_get_last_force_async(self._h, _ptr(out)))
+
+    def launch_count(self) -> int:
+        """kernels launched by this solver so far"""
+        n = ctypes.c_longlong()
+        _check(self._lib.lbm_get_launch_count(self._h, ctypes.byref(n)))
+        return int(n.value)
 
     def time_stream_collide(self, n: int, level: int = 0) -> float:
         ms = _F()

@@ -454,6 +454,12 @@ struct lbm_handle {
     double* audit_out = nullptr;
     RefineParams rp{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    /* the drag/lift reduction of a step reads the populations the step's
+     * stream-collide reads, so it runs beside it on a high-priority side
+     * stream: forked after the previous step, joined before the next */
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    long long launches = 0;         /* kernels this handle has launched */
 };
 
 namespace {
@@ -619,6 +625,7 @@ int do_init(lbm_handle* h) {
     for (int l = 0; l < h->nlevels; ++l) {
         LevelState& s = h->lv[l];
         for (int i = 0; i < 2; ++i) CUDA_TRY(launch_init(s.L, s.mask, s.f[i], kind, u0, h->stream));
+        h->launches += 2;
         s.cur = 0;
         if (s.stats) CUDA_TRY(cudaMemsetAsync(s.stats, 0, size_t(s.L.qstride) * 4 * sizeof(float), h->stream));
     }
@@ -626,6 +633,21 @@ int do_init(lbm_handle* h) {
     h->t = 0;
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return LBM_OK;
+}
+
+/* Launch the drag/lift reduction of level s's current populations on the
+ * side stream, after everything queued so far on the main stream; the caller
+ * joins (waits for ev_join) once the step's stream-collide is queued.  The
+ * force kernel adds into `out` (3 doubles), which is zero or holds the other
+ * level's sum of the same step. */
+cudaError_t fork_force(lbm_handle* h, LevelState& s, double* out) {
+    cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->side, h->ev_fork, 0);
+    if (e == cudaSuccess)
+        e = launch_force(s.L, s.f[s.cur], s.body, s.nbody, s.fpart, s.done, out, h->side, s.mask, h->cfg.halfway);
+    if (e == cudaSuccess) e = cudaEventRecord(h->ev_join, h->side);
+    ++h->launches;
+    return e;
 }
 
 /* one base step and, with refinement, the patch sub-steps and the two
@@ -648,10 +670,10 @@ int one_step(lbm_handle* h) {
         int rc = ensure_force_cap(h, fidx + 1);
         if (rc) return rc;
     }
-    if (p.force_on)
-        CUDA_TRY(launch_force(C.L, C.f[C.cur], C.body, C.nbody, C.fpart, C.done, h->force_hist + 3LL * fidx,
-                              h->stream, C.mask, c.halfway));
+    if (p.force_on) CUDA_TRY(fork_force(h, C, h->force_hist + 3LL * fidx));
     CUDA_TRY(launch_stream_collide(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, h->mom, h->stream, C.links));
+    ++h->launches;
+    if (p.force_on) CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
     C.cur = 1 - C.cur;
     if (c.refinement) {
         LevelState& Fn = h->lv[1];
@@ -664,15 +686,16 @@ int one_step(lbm_handle* h) {
                 int rc = ensure_force_cap(h, fidx + 1);
                 if (rc) return rc;
             }
-            if (pf.force_on)
-                CUDA_TRY(launch_force(Fn.L, Fn.f[Fn.cur], Fn.body, Fn.nbody, Fn.fpart, Fn.done,
-                                      h->force_hist + 3LL * fidx, h->stream, Fn.mask, c.halfway));
+            if (pf.force_on) CUDA_TRY(fork_force(h, Fn, h->force_hist + 3LL * fidx));
             CUDA_TRY(launch_stream_collide(Fn.L, pf, Fn.f[Fn.cur], Fn.f[1 - Fn.cur], Fn.mask, Fn.stats, nullptr,
                                            h->stream, Fn.links));
+            ++h->launches;
+            if (pf.force_on) CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
             Fn.cur = 1 - Fn.cur;
         }
         CUDA_TRY(launch_interp_cf(h->rp, Fn.L, h->mom, Fn.f[Fn.cur], Fn.mask, h->stream));
         CUDA_TRY(launch_interp_fc(h->rp, C.L, Fn.L, Fn.f[Fn.cur], C.f[C.cur], C.mask, h->stream));
+        h->launches += 2;
     }
     h->t = t + 1;
     return LBM_OK;
@@ -816,6 +839,14 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
         return bail(fail(LBM_ERR_CUDA, "cannot create a CUDA stream"));
     cudaEventCreate(&h->ev0);
     cudaEventCreate(&h->ev1);
+    {
+        int lo = 0, hi = 0;
+        cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        if (cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, hi) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess)
+            return bail(fail(LBM_ERR_CUDA, "cannot create the force stream"));
+    }
     /* reference velocity of the FP16/BF16 offsets: the inlet velocity of a channel */
     const float u_ref = c.geometry.rfind("channel", 0) == 0 ? c.umax : 0.f;
     if ((rc = alloc_level(h->lv[0], c.nx, c.ny, c.nz, storage, c.velav != 0, u_ref))) return bail(rc);
@@ -863,6 +894,9 @@ int lbm_destroy(lbm_handle* h) {
     cudaFree(h->audit_out);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->side) cudaStreamDestroy(h->side);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return LBM_OK;
@@ -927,6 +961,7 @@ int lbm_get_populations(lbm_handle* h, int level, float* f) {
     float* d = nullptr;
     CUDA_TRY(cudaMallocAsync((void**)&d, n * sizeof(float), h->stream));
     cudaError_t e = launch_pack(s.L, s.f[s.cur], d, h->stream);
+    ++h->launches;
     if (e == cudaSuccess) e = cudaMemcpyAsync(f, d, n * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
     cudaFreeAsync(d, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -942,7 +977,7 @@ int lbm_set_populations(lbm_handle* h, int level, const float* f) {
     float* d = nullptr;
     CUDA_TRY(cudaMallocAsync((void**)&d, n * sizeof(float), h->stream));
     cudaError_t e = cudaMemcpyAsync(d, f, n * sizeof(float), cudaMemcpyHostToDevice, h->stream);
-    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = launch_unpack(s.L, d, s.f[i], h->stream);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i, ++h->launches) e = launch_unpack(s.L, d, s.f[i], h->stream);
     cudaFreeAsync(d, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "set_populations: %s", cudaGetErrorString(e));
@@ -980,6 +1015,7 @@ int lbm_get_fields(lbm_handle* h, int level, float* rho, float* u, float* v, flo
     float* d = nullptr;
     CUDA_TRY(cudaMallocAsync((void**)&d, 4 * n * sizeof(float), h->stream));
     cudaError_t e = launch_fields(s.L, s.f[s.cur], d, d + n, d + 2 * n, d + 3 * n, h->stream);
+    ++h->launches;
     float* outs[4] = {rho, u, v, w};
     for (int i = 0; i < 4 && e == cudaSuccess; ++i)
         if (outs[i]) e = cudaMemcpyAsync(outs[i], d + i * n, n * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
@@ -1018,6 +1054,12 @@ int lbm_get_forces(lbm_handle* h, double* fxyz, int max_steps, int* n) {
     return LBM_OK;
 }
 
+int lbm_get_launch_count(const lbm_handle* h, long long* n) {
+    if (!h || !n) return fail(LBM_ERR_ARG, "null argument");
+    *n = h->launches;
+    return LBM_OK;
+}
+
 int lbm_get_last_force(lbm_handle* h, double* f3) {
     if (!h || !f3) return fail(LBM_ERR_ARG, "null argument");
     const int i = h->t - 1 - h->cfg.startf;
@@ -1027,6 +1069,17 @@ int lbm_get_last_force(lbm_handle* h, double* f3) {
     }
     CUDA_TRY(cudaMemcpyAsync(f3, h->force_hist + 3LL * i, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return LBM_OK;
+}
+
+int lbm_get_last_force_async(lbm_handle* h, double* f3) {
+    if (!h || !f3) return fail(LBM_ERR_ARG, "null argument");
+    const int i = h->t - 1 - h->cfg.startf;
+    if (i < 0 || i >= h->force_cap) {
+        f3[0] = f3[1] = f3[2] = 0.0;
+        return LBM_OK;
+    }
+    CUDA_TRY(cudaMemcpyAsync(f3, h->force_hist + 3LL * i, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     return LBM_OK;
 }
 
@@ -1041,6 +1094,7 @@ int lbm_time_stream_collide(lbm_handle* h, int level, int n, float* ms) {
     for (int i = 0; i < n; ++i) {
         CUDA_TRY(launch_stream_collide(s.L, p, s.f[s.cur], s.f[1 - s.cur], s.mask, nullptr, nullptr, h->stream,
                                        s.links));
+        ++h->launches;
         s.cur = 1 - s.cur;
     }
     CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
@@ -1056,6 +1110,7 @@ int lbm_audit(lbm_handle* h, int level, double* out4) {
     if (!out4) return fail(LBM_ERR_ARG, "out4 is null");
     LevelState& s = h->lv[level];
     CUDA_TRY(launch_audit(s.L, s.f[s.cur], s.mask, h->audit_part, audit_partials(s.L), h->audit_out, h->stream));
+    h->launches += 2;
     CUDA_TRY(cudaMemcpyAsync(out4, h->audit_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return LBM_OK;

@@ -158,9 +158,6 @@ def test_lid_cavity_bgk_vs_oracle(product):
     assert np.isfinite(audit).all()
 
 
-# FP16 / BF16 store f minus the equilibrium at the inlet velocity; on this
-# small channel (tau0 0.515, 200 steps) the velocity error against the FP64
-# twin is 1.4e-3 (FP16, 11-bit mantissa) and 3.5e-2 (BF16, 8 bits)
 @pytest.mark.parametrize("model,les", [("MRT", 1), ("BGK", 0)])
 def test_halfway_bounceback_vs_oracle(product, model, les):
     """half-way bounce-back (the channel configuration's wall treatment; the
@@ -239,6 +236,9 @@ def test_c1_cavity_axis_permutation(product):
     assert rel_l2(mapped, ja) < 1e-5
 
 
+# FP16 / BF16 store f minus the equilibrium at the inlet velocity; on this
+# small channel (tau0 0.515, 200 steps) the velocity error against the FP64
+# twin is 1.4e-3 (FP16, 11-bit mantissa) and 3.5e-2 (BF16, 8 bits)
 @pytest.mark.parametrize("prec,tol", [("fp16", 2e-3), ("bf16", 5e-2), ("fp32", 1e-5)])
 def test_storage_precision_vs_fp64(product, prec, tol):
     lbm = product
@@ -278,6 +278,34 @@ def test_deterministic_runs(product):
             res.append((s.populations(), s.forces()))
     np.testing.assert_array_equal(res[0][0], res[1][0])
     np.testing.assert_array_equal(res[0][1], res[1][1])
+
+
+def test_force_side_stream_and_launch_count(product):
+    """the per-step force runs on a side stream beside the stream-collide:
+    every step's force read asynchronously equals the recorded history, the
+    history equals a run that reads it synchronously after each step, and a
+    step is exactly two kernels (force + stream-collide; the first step,
+    t = STARTF = 0, records no force)"""
+    lbm = product
+    steps = 40
+    text = _chan_inputs(lbm, steps)
+    with lbm.Solver(text) as s:
+        n0 = s.launch_count()
+        got = np.zeros((steps, 3))
+        for i in range(steps):
+            s.step(1)
+            s.last_force_async(got[i])
+        s.synchronize()
+        assert s.launch_count() - n0 == 2 * steps - 1
+        hist = s.forces()
+    with lbm.Solver(text) as s:
+        sync = np.zeros((steps, 3))
+        for i in range(steps):
+            s.step(1)
+            sync[i] = s.last_force()
+    np.testing.assert_array_equal(got, hist[:steps])
+    np.testing.assert_array_equal(got, sync)
+    assert np.abs(got[-1, 0]) > 0
 
 
 def test_kernel_level_api_matches_handle(product):
