@@ -191,6 +191,33 @@ size_t lbm_body_force_scratch_doubles(void);
 int lbm_body_force_f32_noalloc(const float* fA, const uint8_t* mask, int nx, int ny, int nz, int pitch,
                                double* force_out, void* cuda_stream);
 
+/* ------------------------------------------------------------------------
+ * Learned subgrid closure.  No counterpart in the reference (its LES is the
+ * constant-Cs Smagorinsky model, LR7:683-685): a per-node MLP
+ * 16 -> 64 -> 64 -> 1 (GELU, softplus output) gives the eddy viscosity from
+ * the node's non-equilibrium stress.  Parameters are a float vector of
+ * lbm_mlp_param_count() entries: W1[64][16] (column 15 = bias), W2[64][64],
+ * b2[64], w3[64], b3.  Samples are X[n][16] features and T[n] target eddy
+ * viscosities (lattice units).
+ * ------------------------------------------------------------------------ */
+int lbm_mlp_param_count(void);
+/* Glorot-uniform weights, zero biases, from a seed (host memory) */
+int lbm_mlp_init_params(uint32_t seed, float* params);
+/* gradient of the mean squared error of nu_t / 1e-4 over n samples, and the
+ * loss; device pointers, synchronous on stream */
+int lbm_mlp_grad(const float* d_params, const float* d_X, const float* d_T, int n, float* d_grad, float* d_loss,
+                 void* stream);
+/* nu_t of n samples (FP32 forward on CUDA cores); device pointers, async */
+int lbm_mlp_predict(const float* d_params, const float* d_X, int n, float* d_nu, void* stream);
+/* Adam (beta 0.9 / 0.999) over seeded shuffled mini-batches of device
+ * samples; params (host) in and out, loss_hist[steps] (host, may be NULL) */
+int lbm_mlp_train(const float* d_X, const float* d_T, int n, int batch, int steps, float lr, uint32_t seed,
+                  float* params, float* loss_hist, void* stream);
+/* tensor-core self-check: D[128][64] = A[128][16 kc] * B[64][16 kc]^T with
+ * BF16 operands (raw 16-bit patterns) and an FP32 accumulator, through
+ * tcgen05.mma; kc = 1..4; host pointers */
+int lbm_tc_selftest(int kc, const uint16_t* A, const uint16_t* B, float* D);
+
 #ifdef __cplusplus
 }
 #endif

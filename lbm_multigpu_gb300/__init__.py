@@ -59,6 +59,12 @@ SIGNATURES = [
     ("lbm_get_forces", _I, [_P, _P, _I, ctypes.POINTER(_I)]),
     ("lbm_get_last_force", _I, [_P, _P]),
     ("lbm_get_last_force_async", _I, [_P, _P]),
+    ("lbm_mlp_param_count", _I, []),
+    ("lbm_mlp_init_params", _I, [ctypes.c_uint32, _P]),
+    ("lbm_mlp_grad", _I, [_P, _P, _P, _I, _P, _P, _P]),
+    ("lbm_mlp_predict", _I, [_P, _P, _I, _P, _P]),
+    ("lbm_mlp_train", _I, [_P, _P, _I, _I, _I, _F, ctypes.c_uint32, _P, _P, _P]),
+    ("lbm_tc_selftest", _I, [_I, _P, _P, _P]),
     ("lbm_get_launch_count", _I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     ("lbm_time_stream_collide", _I, [_P, _I, _I, ctypes.POINTER(_F)]),
     ("lbm_audit", _I, [_P, _I, _P]),

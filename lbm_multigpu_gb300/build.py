@@ -1,9 +1,10 @@
 """Build liblbm_gb300.so in-tree (lbm_multigpu_gb300/_build/) with nvcc for sm_103a.
 
-Three translation units compiled in parallel and linked into one shared
-library: the CUDA kernels (csrc/lbm_kernels.cu), the C ABI host side
-(csrc/lbm_host.cpp) and the allocation-free force entry point
-(csrc/lbm_noalloc.cu).  Host code is built with -ffp-contract=off so geometry
+Translation units compiled in parallel and linked into one shared library:
+the CUDA kernels (csrc/lbm_kernels.cu), the C ABI host side
+(csrc/lbm_host.cpp), the allocation-free force entry point
+(csrc/lbm_noalloc.cu), and the learned subgrid closure (csrc/sgs_mlp.cu
+kernels, csrc/lbm_sgs.cpp host side).  Host code is built with -ffp-contract=off so geometry
 masks and the text writers give identical results on x86 and aarch64 hosts.
 """
 from __future__ import annotations
@@ -32,7 +33,8 @@ def nvcc() -> str:
 
 
 def sources() -> list[Path]:
-    return [CSRC / "lbm_kernels.cu", CSRC / "lbm_host.cpp", CSRC / "lbm_noalloc.cu"]
+    return [CSRC / "lbm_kernels.cu", CSRC / "lbm_host.cpp", CSRC / "lbm_noalloc.cu", CSRC / "sgs_mlp.cu",
+            CSRC / "lbm_sgs.cpp"]
 
 
 def _stale(out: Path, deps: list[Path]) -> bool:

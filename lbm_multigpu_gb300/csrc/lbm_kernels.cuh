@@ -116,4 +116,15 @@ cudaError_t launch_interp_cf(const RefineParams& r, const Level& F, const float*
 cudaError_t launch_interp_fc(const RefineParams& r, const Level& C, const Level& F, const void* f_f, void* f_c,
                              const uint8_t* mask_c, cudaStream_t s);
 
+/* learned subgrid closure (sgs_mlp.cu) */
+int mlp_grad_blocks(int n);
+/* per-block partial gradients (+ loss) of the mean loss over n samples */
+cudaError_t launch_mlp_grad(const float* params, const float* X, const float* T, const int* idx, int n,
+                            float* grad_part, int nblocks, cudaStream_t s);
+/* sums the partials; with step > 0 also one Adam step on params (m, v state) */
+cudaError_t launch_mlp_adam(const float* grad_part, int nblocks, float* params, float* m, float* v, float* grad_out,
+                            float* loss_out, float lr, int step, cudaStream_t s);
+cudaError_t launch_mlp_predict(const float* params, const float* X, int n, float* nu, cudaStream_t s);
+cudaError_t launch_tc_selftest(const void* A, const void* B, int kc, float* D, int* err, cudaStream_t s);
+
 }  // namespace lbm

@@ -1,0 +1,51 @@
+/* The learned subgrid closure: a per-cell MLP 15 -> 64 -> 64 -> 1 (GELU,
+ * softplus output) giving the eddy viscosity nu_t that replaces the
+ * constant-Cs Smagorinsky model in the collision.
+ *
+ * Inputs, all local to a node (what the collide kernel has in registers):
+ * with the non-equilibrium stress Pi_neq of the pulled populations,
+ *   p_ij = -3/2 Pi_neq_ij / rho  (= tau_eff S_ij by Chapman-Enskog),
+ *   x0..x5   p_xx, p_yy, p_zz, p_xy, p_xz, p_yz            (/ P_REF)
+ *   x6..x11  the same over tau0: the strain the grid resolves
+ *            before any eddy viscosity                      (/ S_REF)
+ *   x12      |p| = sqrt(2 p:p)                              (/ P_REF)
+ *   x13      tr(p^3) / (p:p)^(3/2), 0 for p = 0
+ *   x14      (tau0 - 1/2) * 100, the molecular viscosity
+ *   x15      1 (carries the first layer's bias)
+ * Output: nu_t = NU_SCALE * softplus(y), and tau_eff = tau0 + 3 nu_t.
+ *
+ * Parameter vector (FP32 master copy, PyTorch Linear order [out][in]):
+ *   W1[64][16] (column 15 = b1) | W2[64][64] | b2[64] | w3[64] | b3
+ */
+#pragma once
+#include <cstdint>
+
+namespace lbm {
+namespace sgs {
+
+constexpr int NIN = 16, NH = 64;
+constexpr int OFF_W1 = 0, OFF_W2 = OFF_W1 + NH * NIN, OFF_B2 = OFF_W2 + NH * NH, OFF_W3 = OFF_B2 + NH,
+              OFF_B3 = OFF_W3 + NH, NPARAM = OFF_B3 + 1;
+constexpr float P_REF = 0.01f, S_REF = 0.01f, NU_SCALE = 1e-4f;
+constexpr float GELU_A = 0.7978845608f, GELU_B = 0.044715f;
+
+/* features of one node from p_ij (xx, yy, zz, xy, xz, yz) and tau0 */
+template <class T> __host__ __device__ inline void features(const T p[6], T tau0, T x[NIN]) {
+    const T pp = p[0] * p[0] + p[1] * p[1] + p[2] * p[2] + T(2) * (p[3] * p[3] + p[4] * p[4] + p[5] * p[5]);
+    /* tr(p^3) of the symmetric tensor */
+    const T xx = p[0], yy = p[1], zz = p[2], xy = p[3], xz = p[4], yz = p[5];
+    const T tr3 = xx * xx * xx + yy * yy * yy + zz * zz * zz + T(3) * xx * (xy * xy + xz * xz) +
+                  T(3) * yy * (xy * xy + yz * yz) + T(3) * zz * (xz * xz + yz * yz) + T(6) * xy * xz * yz;
+    const T inv_t0 = T(1) / tau0;
+    for (int i = 0; i < 6; ++i) {
+        x[i] = p[i] * T(1.0 / P_REF);
+        x[6 + i] = p[i] * inv_t0 * T(1.0 / S_REF);
+    }
+    x[12] = sqrt(T(2) * pp) * T(1.0 / P_REF);
+    x[13] = pp > T(1e-30) ? tr3 / (pp * sqrt(pp)) : T(0);
+    x[14] = (tau0 - T(0.5)) * T(100);
+    x[15] = T(1);
+}
+
+}  // namespace sgs
+}  // namespace lbm

@@ -3,7 +3,7 @@
 TEST INFRASTRUCTURE ONLY.  Nothing here is part of the product path.
 
 * ``build_oracle()`` compiles this directory's CPU restatement
-  (lbm_oracle.cpp) into ``oracle/_build/liblbm_oracle.so``.
+  (lbm_oracle.cpp, sgs_oracle.cpp) into ``oracle/_build/liblbm_oracle.so``.
 * ``stage()`` reads the reference sources from ``$LBM_REFERENCE``
   (default /root/reference, present only in the development container) and
   writes copies of the code paths the tests need into ``oracle/_ref/``, which is
@@ -140,12 +140,12 @@ def oracle_lib_path() -> Path:
 
 def build_oracle(force: bool = False) -> Path:
     out = oracle_lib_path()
-    src = HERE / "lbm_oracle.cpp"
-    if force or not out.exists() or out.stat().st_mtime < max(src.stat().st_mtime,
-                                                              (HERE / "lbm_oracle.h").stat().st_mtime):
+    srcs = [HERE / "lbm_oracle.cpp", HERE / "sgs_oracle.cpp"]
+    newest = max(p.stat().st_mtime for p in srcs + [HERE / "lbm_oracle.h"])
+    if force or not out.exists() or out.stat().st_mtime < newest:
         BUILD_DIR.mkdir(parents=True, exist_ok=True)
         tmp = out.with_suffix(f".{os.getpid()}.tmp")
-        _run([CXX, *ORACLE_FLAGS, "-o", str(tmp), str(src)])
+        _run([CXX, *ORACLE_FLAGS, "-o", str(tmp), *map(str, srcs)])
         os.replace(tmp, out)
     return out
 

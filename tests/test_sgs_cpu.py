@@ -1,0 +1,107 @@
+"""The learned-closure oracle on the CPU: its MLP gradient against central
+finite differences of its own loss, its features against an independent
+numpy restatement, and the box filter / subgrid-stress target on fields
+with known answers."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from oracle_bindings import oracle, ptr
+
+NIN, NH = 16, 64
+NPARAM = NH * NIN + NH * NH + NH + NH + 1
+
+
+def _params(seed=3, scale=0.3):
+    rng = np.random.default_rng(seed)
+    return (rng.standard_normal(NPARAM) * scale).astype(np.float32)
+
+
+def _samples(n, seed=4):
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((n, NIN)).astype(np.float32)
+    X[:, 15] = 1
+    T = (rng.random(n) * 3e-4).astype(np.float32)
+    return X, T
+
+
+def _loss(o, P, X, T):
+    g = np.zeros(NPARAM)
+    L = ctypes.c_double()
+    o.orc_mlp_grad(ptr(P), ptr(X), ptr(T), len(T), ptr(g), ctypes.byref(L))
+    return L.value, g
+
+
+def test_oracle_gradient_matches_finite_differences():
+    o = oracle()
+    assert o.orc_mlp_nparam() == NPARAM
+    P = _params()
+    X, T = _samples(24)
+    L0, g = _loss(o, P, X, T)
+    rng = np.random.default_rng(9)
+    # a spread of parameters from every block: W1, W1 bias column, W2, b2, w3, b3
+    picks = list(rng.choice(NH * NIN, 8, replace=False)) + [15, 16 * 7 + 15]
+    picks += list(NH * NIN + rng.choice(NH * NH, 8, replace=False))
+    picks += [NH * NIN + NH * NH + 5, NH * NIN + NH * NH + NH + 9, NPARAM - 1]
+    for p in picks:
+        h = 1e-3 * max(1.0, abs(float(P[p])))
+        Pp, Pm = P.copy(), P.copy()
+        Pp[p] += h
+        Pm[p] -= h
+        h = (float(Pp[p]) - float(Pm[p])) / 2  # the step the float32 params really took
+        fd = (_loss(o, Pp, X, T)[0] - _loss(o, Pm, X, T)[0]) / (2 * h)
+        assert abs(fd - g[p]) <= 2e-4 * max(1.0, abs(g[p])), (p, fd, g[p])
+    assert L0 > 0
+
+
+def _features_np(p, tau0):
+    m = np.array([[p[0], p[3], p[4]], [p[3], p[1], p[5]], [p[4], p[5], p[2]]])
+    pp = float((m * m).sum())
+    x = np.zeros(16)
+    x[:6] = np.asarray(p) / 0.01
+    x[6:12] = np.asarray(p) / tau0 / 0.01
+    x[12] = np.sqrt(2 * pp) / 0.01
+    x[13] = np.trace(m @ m @ m) / pp ** 1.5 if pp > 1e-30 else 0.0
+    x[14] = (tau0 - 0.5) * 100
+    x[15] = 1
+    return x
+
+
+def test_oracle_features():
+    o = oracle()
+    rng = np.random.default_rng(1)
+    for _ in range(20):
+        p = rng.standard_normal(6) * 1e-3
+        tau0 = 0.5 + rng.random() * 0.1
+        x = np.zeros(16)
+        o.orc_sgs_features(ptr(p), ctypes.c_double(tau0), ptr(x))
+        np.testing.assert_allclose(x, _features_np(p, tau0), rtol=1e-12, atol=1e-12)
+    x = np.zeros(16)
+    o.orc_sgs_features(ptr(np.zeros(6)), ctypes.c_double(0.55), ptr(x))
+    assert x[13] == 0 and x[15] == 1
+
+
+def test_oracle_box_filter_and_target():
+    o = oracle()
+    fx = fy = fz = 16
+    z, y, x = np.meshgrid(np.arange(fz), np.arange(fy), np.arange(fx), indexing="ij")
+    # a field constant over each 2x2x2 block has no subgrid stress
+    blk = np.sin(2 * np.pi * (x // 2) / 8) * 0.01
+    u = np.stack([blk, 0 * blk, 0 * blk]).astype(np.float32)
+    ub = np.zeros((3, 8, 8, 8))
+    uu = np.zeros((6, 8, 8, 8))
+    o.orc_box_filter(ptr(u), fx, fy, fz, ptr(ub), ptr(uu))
+    np.testing.assert_allclose(ub[0], blk[::2, ::2, ::2], atol=1e-9)
+    X = np.zeros((512, 16), np.float32)
+    T = np.zeros(512, np.float32)
+    o.orc_sgs_targets(ptr(ub), ptr(uu), 8, 8, 8, ctypes.c_double(0.52), ptr(X), ptr(T))
+    assert np.abs(T).max() < 1e-12
+    assert np.all(X[:, 15] == 1)
+    # a random field that varies inside the blocks: non-negative eddy
+    # viscosity, positive where the subgrid stress drains the resolved strain
+    u2 = (np.random.default_rng(5).standard_normal((3, fz, fy, fx)) * 0.01).astype(np.float32)
+    o.orc_box_filter(ptr(u2), fx, fy, fz, ptr(ub), ptr(uu))
+    o.orc_sgs_targets(ptr(ub), ptr(uu), 8, 8, 8, ctypes.c_double(0.52), ptr(X), ptr(T))
+    assert T.min() >= 0 and T.max() > 0

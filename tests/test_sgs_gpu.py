@@ -1,0 +1,115 @@
+"""GPU tests of the learned subgrid closure through the C ABI: the
+tensor-core self-check (tcgen05.mma, BF16 in, FP32 accumulate) against an
+FP64 product, the fused training gradient and the forward pass against the
+CPU oracle, and a short training run."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle_bindings import oracle, ptr
+
+pytestmark = pytest.mark.gpu
+
+NIN, NH = 16, 64
+NPARAM = NH * NIN + NH * NH + NH + NH + 1
+
+
+def bf16_bits(a: np.ndarray) -> np.ndarray:
+    """float32 -> bfloat16 bit patterns, round to nearest even"""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+    return r
+
+
+def bf16_val(b: np.ndarray) -> np.ndarray:
+    return (b.astype(np.uint32) << 16).view(np.float32)
+
+
+@pytest.mark.parametrize("kc", [1, 4])
+def test_tensor_core_selftest(product, kc):
+    lib = product.library()
+    K = 16 * kc
+    rng = np.random.default_rng(kc)
+    A = bf16_bits(rng.standard_normal((128, K)))
+    B = bf16_bits(rng.standard_normal((64, K)))
+    D = np.zeros((128, 64), np.float32)
+    assert lib.lbm_tc_selftest(kc, ptr(A), ptr(B), ptr(D)) == 0, lib.lbm_last_error()
+    want = bf16_val(A).astype(np.float64) @ bf16_val(B).astype(np.float64).T
+    np.testing.assert_allclose(D, want, rtol=1e-5, atol=1e-4)
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _data(n, seed):
+    rng = np.random.default_rng(seed)
+    X = (rng.standard_normal((n, NIN)) * 0.7).astype(np.float32)
+    X[:, 15] = 1
+    T = (1e-4 * np.log1p(np.exp(1.5 * X[:, 12] - 0.5 * X[:, 3] - 1))).astype(np.float32)
+    return X, T
+
+
+def _params(lib, seed):
+    P = np.zeros(NPARAM, np.float32)
+    assert lib.lbm_mlp_init_params(seed, ptr(P)) == 0
+    return P
+
+
+def test_mlp_gradient_matches_oracle(product):
+    torch = pytest.importorskip("torch")
+    lib = product.library()
+    assert lib.lbm_mlp_param_count() == NPARAM
+    P = _params(lib, 7)
+    P[NH * NIN + NH * NH: NH * NIN + NH * NH + NH] = 0.05   # non-zero b2
+    P[-1] = -0.3
+    X, T = _data(1000, 2)
+    dP, dX, dT = _dev(torch, P), _dev(torch, X), _dev(torch, T)
+    g = torch.zeros(NPARAM, dtype=torch.float32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    P_ = ctypes.c_void_p
+    assert lib.lbm_mlp_grad(P_(dP.data_ptr()), P_(dX.data_ptr()), P_(dT.data_ptr()), len(T), P_(g.data_ptr()),
+                            P_(loss.data_ptr()), None) == 0, lib.lbm_last_error()
+    go = np.zeros(NPARAM)
+    lo = ctypes.c_double()
+    oracle().orc_mlp_grad(ptr(P), ptr(X), ptr(T), len(T), ptr(go), ctypes.byref(lo))
+    gg = g.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(gg - go) <= 1e-4 * np.linalg.norm(go)
+    np.testing.assert_allclose(gg, go, rtol=1e-3, atol=1e-5 * np.abs(go).max())
+    assert abs(float(loss.item()) - lo.value) <= 1e-5 * lo.value
+
+
+def test_mlp_predict_matches_oracle(product):
+    torch = pytest.importorskip("torch")
+    lib = product.library()
+    P = _params(lib, 11)
+    X, _ = _data(5000, 3)
+    nu = torch.zeros(len(X), dtype=torch.float32, device="cuda")
+    dP, dX = _dev(torch, P), _dev(torch, X)
+    assert lib.lbm_mlp_predict(ctypes.c_void_p(dP.data_ptr()), ctypes.c_void_p(dX.data_ptr()), len(X),
+                               ctypes.c_void_p(nu.data_ptr()), None) == 0
+    torch.cuda.synchronize()
+    want = np.zeros(len(X))
+    oracle().orc_mlp_forward(ptr(P), ptr(X), len(X), ptr(want))
+    np.testing.assert_allclose(nu.cpu().numpy(), want, rtol=2e-5, atol=1e-10)
+
+
+def test_training_reduces_loss(product):
+    torch = pytest.importorskip("torch")
+    lib = product.library()
+    P = _params(lib, 5)
+    X, T = _data(20000, 4)
+    dX, dT = _dev(torch, X), _dev(torch, T)
+    steps = 400
+    hist = np.zeros(steps, np.float32)
+    assert lib.lbm_mlp_train(ctypes.c_void_p(dX.data_ptr()), ctypes.c_void_p(dT.data_ptr()), len(T), 1024, steps,
+                             ctypes.c_float(3e-3), 1, ptr(P), ptr(hist), None) == 0, lib.lbm_last_error()
+    assert np.isfinite(hist).all()
+    assert hist[-20:].mean() < 0.1 * hist[:5].mean()
+    # the trained parameters reproduce the targets on the CPU oracle too
+    nu = np.zeros(len(T))
+    oracle().orc_mlp_forward(ptr(P), ptr(X), len(X), ptr(nu))
+    assert np.sqrt(np.mean((nu - T) ** 2)) < 0.3 * np.sqrt(np.mean(T ** 2))
