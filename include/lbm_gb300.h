@@ -213,10 +213,57 @@ int lbm_mlp_predict(const float* d_params, const float* d_X, int n, float* d_nu,
  * samples; params (host) in and out, loss_hist[steps] (host, may be NULL) */
 int lbm_mlp_train(const float* d_X, const float* d_T, int n, int batch, int steps, float lr, uint32_t seed,
                   float* params, float* loss_hist, void* stream);
+/* nu_t of n samples through the tensor-core path the collide kernels use:
+ * BF16 weights and activations, FP32 accumulation (tcgen05.mma), GELU by
+ * tanh.approx; params in host memory, samples and output on the device;
+ * synchronous on stream */
+int lbm_mlp_predict_tc(const float* params, const float* d_X, int n, float* d_nu, void* stream);
 /* tensor-core self-check: D[128][64] = A[128][16 kc] * B[64][16 kc]^T with
  * BF16 operands (raw 16-bit patterns) and an FP32 accumulator, through
  * tcgen05.mma; kc = 1..4; host pointers */
 int lbm_tc_selftest(int kc, const uint16_t* A, const uint16_t* B, float* D);
+
+/* ------------------------------------------------------------------------
+ * Ensemble of periodic D3Q19 boxes (decaying turbulence), the data source of
+ * the learned closure.  No counterpart in the reference, which runs one
+ * domain per program; each member uses the reference's MRT collision
+ * (LR7:583-711) with periodic streaming.  All members advance together: one
+ * persistent kernel launch per step over the tiles of every member, replayed
+ * from a captured CUDA graph.  sgs: 0 none, 1 Smagorinsky (cs = Cs^2, as the
+ * reference's CS), 2 the learned MLP (lbm_ensemble_set_mlp).
+ * ------------------------------------------------------------------------ */
+typedef struct lbm_ensemble lbm_ensemble;
+/* count members of side sizes[m] (even, 8..1024) and relaxation time tau0[m] */
+int lbm_ensemble_create(int count, const int* sizes, const float* tau0, int sgs, float cs, lbm_ensemble** out);
+int lbm_ensemble_destroy(lbm_ensemble* e);
+/* seeded random-phase solenoidal velocity, E(k) ~ k^-5/3 for k = 1..n/kmax_div
+ * with up to per_shell wavevectors per shell, rms u_rms per component;
+ * populations at the rho = 1 equilibrium */
+int lbm_ensemble_init_turbulence(lbm_ensemble* e, uint32_t seed, float u_rms, int kmax_div, int per_shell);
+/* the modes of a member: k3[3n] integer wavevectors, phase[n] (in units of
+ * pi), a3[3n] amplitude vectors; *n = count (up to cap written) */
+int lbm_ensemble_modes(const lbm_ensemble* e, int member, int* k3, double* phase, double* a3, int cap, int* n);
+/* coarse members (half the fine sides) start from the 2x2x2 box filter of
+ * the fine members' current velocity */
+int lbm_ensemble_init_filtered(lbm_ensemble* coarse, lbm_ensemble* fine);
+int lbm_ensemble_set_mlp(lbm_ensemble* e, const float* params);
+/* picks tile height and grid size by timing candidates on a copy of the
+ * state (the state is unchanged); results are cached per device and shape */
+int lbm_ensemble_autotune(lbm_ensemble* e, int* ty, int* grid, float* ms_per_step);
+int lbm_ensemble_step(lbm_ensemble* e, int nsteps);
+int lbm_ensemble_step_timed(lbm_ensemble* e, int nsteps, float* ms);
+int lbm_ensemble_info(const lbm_ensemble* e, int* ty, int* grid, long long* cells, long long* steps);
+/* kinetic energy 1/2 <|u|^2> per member (FP64) */
+int lbm_ensemble_energy(lbm_ensemble* e, double* E);
+/* velocity u[3][n][n][n] of a member */
+int lbm_ensemble_velocity(lbm_ensemble* e, int member, float* u3);
+/* compact populations f[19][n][n][n] of a member, out and in */
+int lbm_ensemble_populations(lbm_ensemble* e, int member, float* f);
+int lbm_ensemble_set_populations(lbm_ensemble* e, int member, const float* f);
+/* training samples of every member filtered 2x2x2 (features X[.][16] and
+ * target nu T[.] on the device, appended at *n, capacity cap); tau0_coarse
+ * <= 1/2 takes each member's coarse relaxation time by acoustic scaling */
+int lbm_ensemble_samples(lbm_ensemble* e, float tau0_coarse, float* d_X, float* d_T, long long cap, long long* n);
 
 #ifdef __cplusplus
 }

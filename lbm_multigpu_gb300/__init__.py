@@ -65,6 +65,22 @@ SIGNATURES = [
     ("lbm_mlp_predict", _I, [_P, _P, _I, _P, _P]),
     ("lbm_mlp_train", _I, [_P, _P, _I, _I, _I, _F, ctypes.c_uint32, _P, _P, _P]),
     ("lbm_tc_selftest", _I, [_I, _P, _P, _P]),
+    ("lbm_mlp_predict_tc", _I, [_P, _P, _I, _P, _P]),
+    ("lbm_ensemble_create", _I, [_I, _P, _P, _I, _F, _P]),
+    ("lbm_ensemble_destroy", _I, [_P]),
+    ("lbm_ensemble_init_turbulence", _I, [_P, ctypes.c_uint32, _F, _I, _I]),
+    ("lbm_ensemble_modes", _I, [_P, _I, _P, _P, _P, _I, _P]),
+    ("lbm_ensemble_init_filtered", _I, [_P, _P]),
+    ("lbm_ensemble_set_mlp", _I, [_P, _P]),
+    ("lbm_ensemble_autotune", _I, [_P, _P, _P, _P]),
+    ("lbm_ensemble_step", _I, [_P, _I]),
+    ("lbm_ensemble_step_timed", _I, [_P, _I, _P]),
+    ("lbm_ensemble_info", _I, [_P, _P, _P, _P, _P]),
+    ("lbm_ensemble_energy", _I, [_P, _P]),
+    ("lbm_ensemble_velocity", _I, [_P, _I, _P]),
+    ("lbm_ensemble_populations", _I, [_P, _I, _P]),
+    ("lbm_ensemble_set_populations", _I, [_P, _I, _P]),
+    ("lbm_ensemble_samples", _I, [_P, _F, _P, _P, ctypes.c_longlong, _P]),
     ("lbm_get_launch_count", _I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     ("lbm_time_stream_collide", _I, [_P, _I, _I, ctypes.POINTER(_F)]),
     ("lbm_audit", _I, [_P, _I, _P]),
@@ -369,3 +385,101 @@ class Solver:
 
     def write_outputs(self, casename: str) -> None:
         _check(self._lib.lbm_write_outputs(self._h, casename.encode()))
+
+
+SGS = {"none": 0, "smagorinsky": 1, "mlp": 2}
+
+
+class Ensemble:
+    """Periodic D3Q19 boxes of uneven sizes advanced together (one persistent
+    launch per step, replayed from a CUDA graph); the data source and test bed
+    of the learned subgrid closure."""
+
+    def __init__(self, sizes, tau0, sgs: str = "none", cs: float = 0.01):
+        self._lib = library()
+        self.sizes = [int(n) for n in sizes]
+        t = np.asarray(tau0 if np.ndim(tau0) else [tau0] * len(self.sizes), np.float32)
+        self.tau0 = t
+        sz = np.asarray(self.sizes, np.int32)
+        h = _P()
+        _check(self._lib.lbm_ensemble_create(len(sz), _ptr(sz), _ptr(t), SGS[sgs], _F(cs), ctypes.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.lbm_ensemble_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def init_turbulence(self, seed: int, u_rms: float = 0.04, kmax_div: int = 8, per_shell: int = 24) -> None:
+        _check(self._lib.lbm_ensemble_init_turbulence(self._h, seed, _F(u_rms), kmax_div, per_shell))
+
+    def modes(self, member: int):
+        n = _I()
+        _check(self._lib.lbm_ensemble_modes(self._h, member, None, None, None, 0, ctypes.byref(n)))
+        k = np.zeros((n.value, 3), np.int32)
+        ph = np.zeros(n.value)
+        a = np.zeros((n.value, 3))
+        _check(self._lib.lbm_ensemble_modes(self._h, member, _ptr(k), _ptr(ph), _ptr(a), n.value, ctypes.byref(n)))
+        return k, ph, a
+
+    def init_filtered(self, fine: "Ensemble") -> None:
+        _check(self._lib.lbm_ensemble_init_filtered(self._h, fine._h))
+
+    def set_mlp(self, params: np.ndarray) -> None:
+        p = np.ascontiguousarray(params, np.float32)
+        _check(self._lib.lbm_ensemble_set_mlp(self._h, _ptr(p)))
+
+    def autotune(self):
+        ty, g, ms = _I(), _I(), _F()
+        _check(self._lib.lbm_ensemble_autotune(self._h, ctypes.byref(ty), ctypes.byref(g), ctypes.byref(ms)))
+        return ty.value, g.value, ms.value
+
+    def step(self, n: int = 1) -> None:
+        _check(self._lib.lbm_ensemble_step(self._h, n))
+
+    def step_timed(self, n: int) -> float:
+        ms = _F()
+        _check(self._lib.lbm_ensemble_step_timed(self._h, n, ctypes.byref(ms)))
+        return float(ms.value)
+
+    def info(self) -> dict:
+        ty, g, c, st = _I(), _I(), ctypes.c_longlong(), ctypes.c_longlong()
+        _check(self._lib.lbm_ensemble_info(self._h, ctypes.byref(ty), ctypes.byref(g), ctypes.byref(c),
+                                           ctypes.byref(st)))
+        return dict(ty=ty.value, grid=g.value, cells=c.value, steps=st.value)
+
+    def energy(self) -> np.ndarray:
+        e = np.zeros(len(self.sizes))
+        _check(self._lib.lbm_ensemble_energy(self._h, _ptr(e)))
+        return e
+
+    def velocity(self, member: int) -> np.ndarray:
+        n = self.sizes[member]
+        u = np.zeros((3, n, n, n), np.float32)
+        _check(self._lib.lbm_ensemble_velocity(self._h, member, _ptr(u)))
+        return u
+
+    def populations(self, member: int) -> np.ndarray:
+        n = self.sizes[member]
+        f = np.zeros((19, n, n, n), np.float32)
+        _check(self._lib.lbm_ensemble_populations(self._h, member, _ptr(f)))
+        return f
+
+    def set_populations(self, member: int, f: np.ndarray) -> None:
+        g = np.ascontiguousarray(f, np.float32)
+        _check(self._lib.lbm_ensemble_set_populations(self._h, member, _ptr(g)))
+
+    def samples_into(self, X_ptr: int, T_ptr: int, cap: int, n: int = 0, tau0_coarse: float = 0.0) -> int:
+        """append the filtered training samples of every member at device
+        pointers X (float [cap][16]) and T (float [cap]); returns the new count"""
+        c = ctypes.c_longlong(n)
+        _check(self._lib.lbm_ensemble_samples(self._h, _F(tau0_coarse), _P(X_ptr), _P(T_ptr), cap, ctypes.byref(c)))
+        return int(c.value)

@@ -268,6 +268,41 @@ template <class T> __host__ __device__ __forceinline__ void collide_bgk(T f[19],
     }
 }
 
+/* density and non-equilibrium stress Pi_neq = sum c c f - rho/3 I - j j
+ * (xx, yy, zz, xy, xz, yz) of the pulled populations: the input of the
+ * learned subgrid closure (the quantity the Smagorinsky model takes the norm
+ * of) */
+template <class T> __host__ __device__ __forceinline__ void pi_neq(const T f[19], T& rho, T p[6]) {
+    T r = 0, jx = 0, jy = 0, jz = 0, xx = 0, yy = 0, zz = 0, xy = 0, xz = 0, yz = 0;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        r += f[q];
+        if (cx(q)) {
+            jx += T(cx(q)) * f[q];
+            xx += f[q];
+        }
+        if (cy(q)) {
+            jy += T(cy(q)) * f[q];
+            yy += f[q];
+        }
+        if (cz(q)) {
+            jz += T(cz(q)) * f[q];
+            zz += f[q];
+        }
+        if (cx(q) * cy(q)) xy += T(cx(q) * cy(q)) * f[q];
+        if (cx(q) * cz(q)) xz += T(cx(q) * cz(q)) * f[q];
+        if (cy(q) * cz(q)) yz += T(cy(q) * cz(q)) * f[q];
+    }
+    const T third = r * T(1.0 / 3.0);
+    rho = r;
+    p[0] = xx - third - jx * jx;
+    p[1] = yy - third - jy * jy;
+    p[2] = zz - third - jz * jz;
+    p[3] = xy - jx * jy;
+    p[4] = xz - jx * jz;
+    p[5] = yz - jy * jz;
+}
+
 template <class T>
 __host__ __device__ __forceinline__ void collide(int model, T f[19], T omega, bool les, T cs, T dpdy) {
     switch (model) {

@@ -126,5 +126,10 @@ cudaError_t launch_mlp_adam(const float* grad_part, int nblocks, float* params, 
                             float* loss_out, float lr, int step, cudaStream_t s);
 cudaError_t launch_mlp_predict(const float* params, const float* X, int n, float* nu, cudaStream_t s);
 cudaError_t launch_tc_selftest(const void* A, const void* B, int kc, float* D, int* err, cudaStream_t s);
+/* tensor-core inference of n samples from a weight blob (sgs::BLOB_BYTES, see
+ * mlp_make_blob); err gets 2 when an MMA completion wait ran out */
+cudaError_t launch_mlp_predict_tc(const void* blob, const float* X, int n, float* nu, int* err, cudaStream_t s);
+/* host: the device weight blob of a parameter vector (lbm_sgs.cpp) */
+void mlp_make_blob(const float* params, unsigned char* blob);
 
 }  // namespace lbm

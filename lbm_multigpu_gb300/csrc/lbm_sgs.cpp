@@ -16,7 +16,9 @@
 
 #include "../../include/lbm_gb300.h"
 #include "lbm_kernels.cuh"
+#include "sgs_infer.cuh"
 #include "sgs_mlp.cuh"
+#include "tc_sm103.cuh"
 
 using namespace lbm;
 
@@ -49,7 +51,37 @@ template <class T> struct DevBuf {
     cudaError_t alloc(size_t n) { return cudaMalloc(&p, n * sizeof(T)); }
 };
 
+uint16_t bf16_rne(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    if ((u & 0x7F800000u) == 0x7F800000u) return uint16_t(u >> 16); /* inf / nan kept */
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return uint16_t(u >> 16);
+}
+
 }  // namespace
+
+namespace lbm {
+void mlp_make_blob(const float* P, unsigned char* blob) {
+    std::memset(blob, 0, sgs::BLOB_BYTES);
+    for (int j = 0; j < sgs::NH; ++j)
+        for (int k = 0; k < sgs::NIN; ++k) {
+            const uint16_t b = bf16_rne(P[sgs::OFF_W1 + j * sgs::NIN + k]);
+            std::memcpy(blob + tc::core_off(j, k, sgs::W1_LBO, sgs::W1_SBO), &b, 2);
+        }
+    for (int j = 0; j < sgs::NH; ++j)
+        for (int k = 0; k < sgs::NH; ++k) {
+            const uint16_t b = bf16_rne(P[sgs::OFF_W2 + j * sgs::NH + k]);
+            std::memcpy(blob + sgs::W1_BYTES + tc::core_off(j, k, sgs::W2_LBO, sgs::W2_SBO), &b, 2);
+        }
+    float* fp = reinterpret_cast<float*>(blob + sgs::W1_BYTES + sgs::W2_BYTES);
+    for (int j = 0; j < sgs::NH; ++j) {
+        fp[j] = P[sgs::OFF_B2 + j];
+        fp[sgs::NH + j] = P[sgs::OFF_W3 + j];
+    }
+    fp[2 * sgs::NH] = P[sgs::OFF_B3];
+}
+}  // namespace lbm
 
 extern "C" {
 
@@ -132,6 +164,26 @@ int lbm_mlp_train(const float* d_X, const float* d_T, int n, int batch, int step
         SGS_TRY(cudaMemcpyAsync(loss_hist, loss.p, size_t(steps) * sizeof(float), cudaMemcpyDeviceToHost, s),
                 "loss read");
     SGS_TRY(cudaStreamSynchronize(s), "training");
+    return LBM_OK;
+}
+
+int lbm_mlp_predict_tc(const float* params, const float* d_X, int n, float* d_nu, void* stream) {
+    if (!params || !d_X || !d_nu || n < 0) return set_error(LBM_ERR_ARG, "bad argument", cudaSuccess);
+    if (n == 0) return LBM_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<unsigned char> blob(sgs::BLOB_BYTES);
+    mlp_make_blob(params, blob.data());
+    DevBuf<unsigned char> d;
+    DevBuf<int> err;
+    SGS_TRY(d.alloc(blob.size()), "cudaMalloc");
+    SGS_TRY(err.alloc(1), "cudaMalloc");
+    SGS_TRY(cudaMemcpyAsync(d.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, s), "blob upload");
+    SGS_TRY(cudaMemsetAsync(err.p, 0, sizeof(int), s), "memset");
+    SGS_TRY(launch_mlp_predict_tc(d.p, d_X, n, d_nu, err.p, s), "tensor-core predict launch");
+    int e = 0;
+    SGS_TRY(cudaMemcpyAsync(&e, err.p, sizeof(int), cudaMemcpyDeviceToHost, s), "read");
+    SGS_TRY(cudaStreamSynchronize(s), "tensor-core predict");
+    if (e) return set_error(LBM_ERR_CUDA, "tensor-core inference: an MMA completion wait ran out", cudaSuccess);
     return LBM_OK;
 }
 

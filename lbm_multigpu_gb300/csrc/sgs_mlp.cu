@@ -14,6 +14,7 @@
 #include <cuda_bf16.h>
 
 #include "lbm_kernels.cuh"
+#include "sgs_infer.cuh"
 #include "sgs_mlp.cuh"
 #include "tc_sm103.cuh"
 
@@ -263,6 +264,26 @@ __global__ void __launch_bounds__(128) k_tc_selftest(const __nv_bfloat16* __rest
 #endif
 }
 
+/* nu_t of n samples through the tensor-core inference path (the one the
+ * collide kernels use): persistent blocks of 128 rows */
+__global__ void __launch_bounds__(128) k_mlp_predict_tc(const unsigned char* __restrict__ blob,
+                                                        const float* __restrict__ X, int n, float* __restrict__ nu,
+                                                        int* __restrict__ err) {
+    __shared__ InferSmem<128> s;
+#if defined(__CUDA_ARCH__)
+    infer_setup<128>(s, blob);
+    for (int base = blockIdx.x * 128; base < n; base += gridDim.x * 128) {
+        const int i = base + threadIdx.x;
+        float x[NIN];
+#pragma unroll
+        for (int k = 0; k < NIN; ++k) x[k] = i < n ? X[size_t(i) * NIN + k] : 0.f;
+        const float v = infer_nu<128>(s, x, err);
+        if (i < n) nu[i] = v;
+    }
+    infer_teardown<128>(s);
+#endif
+}
+
 }  // namespace sgs
 
 /* ---- launchers */
@@ -298,6 +319,14 @@ cudaError_t launch_mlp_predict(const float* params, const float* X, int n, float
     if (b > 152 * 8) b = 152 * 8;
     if (b < 1) b = 1;
     sgs::k_mlp_predict<<<b, sgs::GT, 0, s>>>(params, X, n, nu);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_predict_tc(const void* blob, const float* X, int n, float* nu, int* err, cudaStream_t s) {
+    int b = (n + 127) / 128;
+    if (b > 152 * 4) b = 152 * 4;
+    if (b < 1) b = 1;
+    sgs::k_mlp_predict_tc<<<b, 128, 0, s>>>((const unsigned char*)blob, X, n, nu, err);
     return cudaGetLastError();
 }
 

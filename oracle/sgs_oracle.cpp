@@ -117,6 +117,50 @@ void orc_mlp_grad(const float* params, const float* X, const float* T, int n, do
     *loss = L;
 }
 
+void orc_collide_d(int model, int les, double omega, double cs, double dpdy, double* f, int n);
+
+/* density and Pi_neq = sum c c f - rho/3 I - j j (xx, yy, zz, xy, xz, yz) */
+void orc_pi_neq(const double* f, double* rho, double* p) {
+    static const int CX[19] = {0, 1, 0, -1, 0, 1, -1, -1, 1, 0, 1, 0, -1, 0, 0, 1, 0, -1, 0};
+    static const int CY[19] = {0, 0, 1, 0, -1, 1, 1, -1, -1, 0, 0, 1, 0, -1, 0, 0, 1, 0, -1};
+    static const int CZ[19] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, -1, -1, -1, -1, -1};
+    double r = 0, j[3] = {0, 0, 0}, m[6] = {0, 0, 0, 0, 0, 0};
+    for (int q = 0; q < 19; ++q) {
+        const double c[3] = {double(CX[q]), double(CY[q]), double(CZ[q])};
+        r += f[q];
+        for (int a = 0; a < 3; ++a) j[a] += c[a] * f[q];
+        m[0] += c[0] * c[0] * f[q], m[1] += c[1] * c[1] * f[q], m[2] += c[2] * c[2] * f[q];
+        m[3] += c[0] * c[1] * f[q], m[4] += c[0] * c[2] * f[q], m[5] += c[1] * c[2] * f[q];
+    }
+    *rho = r;
+    p[0] = m[0] - r / 3 - j[0] * j[0];
+    p[1] = m[1] - r / 3 - j[1] * j[1];
+    p[2] = m[2] - r / 3 - j[2] * j[2];
+    p[3] = m[3] - j[0] * j[1];
+    p[4] = m[4] - j[0] * j[2];
+    p[5] = m[5] - j[1] * j[2];
+}
+
+/* the learned closure in the collision: per node (AoS f[n][19]) Pi_neq ->
+ * p = -3/2 Pi_neq / rho -> features -> MLP -> nu_t, then the LR7 MRT
+ * collision (model 0, no Smagorinsky) at 1 / (tau0 + 3 nu_t); nu_out[n] */
+void orc_collide_mlp(const float* params, double tau0, double* f, int n, double* nu_out) {
+    for (int i = 0; i < n; ++i) {
+        double* g = f + 19L * i;
+        double rho, p[6], x[16];
+        orc_pi_neq(g, &rho, p);
+        for (double& v : p) v *= -1.5 / rho;
+        orc_sgs_features(p, tau0, x);
+        float xf[16];
+        for (int k = 0; k < 16; ++k) xf[k] = float(x[k]);
+        Fwd a;
+        forward(params, xf, a);
+        const double nu = NU_SCALE * softplus(a.y);
+        if (nu_out) nu_out[i] = nu;
+        orc_collide_d(0, 0, 1 / (tau0 + 3 * nu), 0, 0, g, 1);
+    }
+}
+
 /* 2x2x2 box filter of a fine periodic velocity field (u[3][fz][fy][fx]) onto
  * the coarse grid: ubar[3][cz][cy][cx], and the filtered products
  * uu[6][...] (xx, yy, zz, xy, xz, yz) */

@@ -1,0 +1,161 @@
+"""GPU tests of the ensemble of periodic boxes through the C ABI: the seeded
+turbulence initialisation against its mode table, the batched persistent
+step against the CPU oracle (no model, Smagorinsky, and the learned closure
+through the tensor cores), graph / autotuner invariance, and the filtered
+training samples against the oracle's filter."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle_bindings import CX, CY, CZ, OracleRun, oracle, ptr, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [16, 24, 32]  # 24: rows padded to a pitch of 32
+
+
+def _field(n, k, ph, a):
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    u = np.zeros((3, n, n, n))
+    for kk, p, aa in zip(k, ph, a):
+        c = np.cos(np.pi * (((kk[0] * x + kk[1] * y + kk[2] * z) % n) * 2.0 / n + p))
+        for d in range(3):
+            u[d] += aa[d] * c
+    return u
+
+
+def test_turbulence_init_matches_modes(product):
+    lbm = product
+    with lbm.Ensemble(SIZES, 0.52) as e:
+        e.init_turbulence(seed=7, u_rms=0.04, kmax_div=4, per_shell=12)
+        for m, n in enumerate(SIZES):
+            k, ph, a = e.modes(m)
+            assert len(k) > 0
+            kn = np.linalg.norm(k, axis=1)
+            assert np.abs((k * a).sum(1)).max() <= 1e-12 * np.abs(a).max()   # solenoidal
+            want = _field(n, k, ph, a)
+            np.testing.assert_allclose(e.velocity(m), want, atol=2e-7)
+            assert abs(np.sqrt((want ** 2).mean()) - 0.04) < 1e-6             # rms per component
+            # shell energies follow k^-5/3
+            ks = np.unique(np.round(kn))
+            Ek = np.array([(a[np.round(kn) == s] ** 2).sum() for s in ks])
+            slope = np.polyfit(np.log(ks), np.log(Ek), 1)[0]
+            assert abs(slope + 5 / 3) < 0.05, slope
+
+
+@pytest.mark.parametrize("sgs,les", [("none", 0), ("smagorinsky", 1)])
+def test_ensemble_step_matches_oracle(product, sgs, les):
+    lbm = product
+    tau = [0.52, 0.55, 0.6]
+    steps = 6
+    with lbm.Ensemble(SIZES, tau, sgs=sgs, cs=0.01) as e:
+        e.init_turbulence(seed=3, u_rms=0.04, kmax_div=4, per_shell=12)
+        f0 = [e.populations(m) for m in range(len(SIZES))]
+        e.step(steps)
+        for m, n in enumerate(SIZES):
+            o = OracleRun(n, n, n, np.zeros((n, n, n), np.uint8), 1 / tau[m], model=0, les=les, cs=0.01, f0=f0[m])
+            o.step(steps)
+            got = e.populations(m)
+            assert rel_l2(got - f0[m], o.fa - f0[m]) < 1e-5, m
+
+
+def _pull(f):
+    g = np.empty_like(f)
+    for q in range(19):
+        g[q] = np.roll(f[q], shift=(CZ[q], CY[q], CX[q]), axis=(0, 1, 2))
+    return g
+
+
+def test_ensemble_mlp_collision_matches_oracle(product):
+    """one step of the learned closure: pull, Pi_neq, features, tensor-core
+    MLP, MRT at tau0 + 3 nu_t; the GPU update agrees with the FP64 oracle to
+    5% of what the eddy viscosity changes (BF16 inference)"""
+    lbm = product
+    lib = lbm.library()
+    P = np.zeros(lib.lbm_mlp_param_count(), np.float32)
+    lib.lbm_mlp_init_params(21, ptr(P))
+    P *= 3
+    P[-1] = 40.0            # nu_t around 4e-3: a visible change of tau
+    sizes, tau0 = [16, 24], 0.51
+    rng = np.random.default_rng(0)
+    with lbm.Ensemble(sizes, tau0, sgs="mlp") as e:
+        e.init_turbulence(seed=5, u_rms=0.04, kmax_div=4, per_shell=12)
+        e.step(3)
+        e.set_mlp(P)
+        for m, n in enumerate(sizes):
+            f = e.populations(m).astype(np.float64)
+            f *= 1 + 0.002 * rng.standard_normal(f.shape)   # stress the closure
+            e.set_populations(m, f.astype(np.float32))
+        f_in = [e.populations(m).astype(np.float64) for m in range(len(sizes))]
+        e.step(1)
+        for m, n in enumerate(sizes):
+            pulled = _pull(f_in[m])
+            aos = np.ascontiguousarray(pulled.reshape(19, -1).T)
+            nu = np.zeros(aos.shape[0])
+            oracle().orc_collide_mlp(ptr(P), ctypes.c_double(tau0), ptr(aos), aos.shape[0], ptr(nu))
+            want = aos.T.reshape(pulled.shape)
+            plain = np.ascontiguousarray(pulled.reshape(19, -1).T)
+            oracle().orc_collide_d(0, 0, ctypes.c_double(1 / tau0), ctypes.c_double(0), ctypes.c_double(0), ptr(plain),
+                                   plain.shape[0])
+            plain = plain.T.reshape(pulled.shape)
+            got = e.populations(m).astype(np.float64)
+            closure = np.linalg.norm(want - plain)     # what the eddy viscosity changed
+            assert closure > 5e-3 * np.linalg.norm(want - pulled)
+            assert np.linalg.norm(got - want) <= 0.05 * closure, np.linalg.norm(got - want) / closure
+            assert nu.min() > 0
+
+
+def test_graph_and_autotune_keep_results(product):
+    lbm = product
+    a = lbm.Ensemble(SIZES, 0.53, sgs="smagorinsky")
+    b = lbm.Ensemble(SIZES, 0.53, sgs="smagorinsky")
+    for e in (a, b):
+        e.init_turbulence(seed=11, kmax_div=4, per_shell=12)
+    a.step(16)                  # two graph replays of 8 steps
+    for _ in range(16):
+        b.step(1)               # single launches
+    for m in range(len(SIZES)):
+        np.testing.assert_array_equal(a.populations(m), b.populations(m))
+    E0 = a.energy()
+    ty, grid, ms = a.autotune()
+    assert ty in (4, 8) and grid > 0 and ms > 0
+    np.testing.assert_array_equal(a.energy(), E0)      # the trials ran on a copy
+    a.step(10)
+    b.step(10)
+    for m in range(len(SIZES)):
+        np.testing.assert_array_equal(a.populations(m), b.populations(m))
+    assert a.info()["steps"] == 26
+    a.close()
+    b.close()
+
+
+def test_training_samples_match_oracle(product):
+    torch = pytest.importorskip("torch")
+    lbm = product
+    sizes, tau0 = [16, 32], 0.506
+    with lbm.Ensemble(sizes, tau0) as e:
+        e.init_turbulence(seed=2, kmax_div=4, per_shell=12)
+        e.step(10)
+        cap = sum((n // 2) ** 3 for n in sizes)
+        X = torch.zeros((cap, 16), dtype=torch.float32, device="cuda")
+        T = torch.zeros(cap, dtype=torch.float32, device="cuda")
+        n = e.samples_into(X.data_ptr(), T.data_ptr(), cap)
+        assert n == cap
+        Xg, Tg = X.cpu().numpy(), T.cpu().numpy()
+        pos = 0
+        for m, N in enumerate(sizes):
+            u = e.velocity(m)
+            nc = N // 2
+            ub = np.zeros((3, nc, nc, nc))
+            uu = np.zeros((6, nc, nc, nc))
+            oracle().orc_box_filter(ptr(u), N, N, N, ptr(ub), ptr(uu))
+            Xo = np.zeros((nc ** 3, 16), np.float32)
+            To = np.zeros(nc ** 3, np.float32)
+            oracle().orc_sgs_targets(ptr(ub), ptr(uu), nc, nc, nc, ctypes.c_double(0.503), ptr(Xo), ptr(To))
+            np.testing.assert_allclose(Xg[pos:pos + nc ** 3], Xo, rtol=1e-5, atol=1e-6)
+            np.testing.assert_allclose(Tg[pos:pos + nc ** 3], To, rtol=1e-5, atol=1e-12)
+            assert (To > 0).mean() > 0.2
+            pos += nc ** 3

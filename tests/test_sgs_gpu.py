@@ -113,3 +113,24 @@ def test_training_reduces_loss(product):
     nu = np.zeros(len(T))
     oracle().orc_mlp_forward(ptr(P), ptr(X), len(X), ptr(nu))
     assert np.sqrt(np.mean((nu - T) ** 2)) < 0.3 * np.sqrt(np.mean(T ** 2))
+
+
+def test_tensor_core_inference_matches_oracle(product):
+    """the inference path of the collide kernels: BF16 weights and
+    activations through tcgen05.mma, FP32 accumulation, GELU by tanh.approx;
+    against the FP64 oracle forward.  Tolerance: 2% relative L2 over the
+    samples (BF16 keeps 8 mantissa bits)"""
+    torch = pytest.importorskip("torch")
+    lib = product.library()
+    P = _params(lib, 13)
+    P[NH * NIN + NH * NH: NH * NIN + NH * NH + NH] = 0.1
+    X, _ = _data(3000, 8)   # not a multiple of 128: a partial last tile
+    dX = _dev(torch, X)
+    nu = torch.full((len(X),), -1.0, dtype=torch.float32, device="cuda")
+    assert lib.lbm_mlp_predict_tc(ptr(P), ctypes.c_void_p(dX.data_ptr()), len(X), ctypes.c_void_p(nu.data_ptr()),
+                                  None) == 0, lib.lbm_last_error()
+    got = nu.cpu().numpy().astype(np.float64)
+    want = np.zeros(len(X))
+    oracle().orc_mlp_forward(ptr(P), ptr(X), len(X), ptr(want))
+    assert (got >= 0).all()
+    assert np.linalg.norm(got - want) <= 2e-2 * np.linalg.norm(want), np.linalg.norm(got - want) / np.linalg.norm(want)
