@@ -223,6 +223,12 @@ int lbm_mlp_predict_tc(const float* params, const float* d_X, int n, float* d_nu
  * tcgen05.mma; kc = 1..4; host pointers */
 int lbm_tc_selftest(int kc, const uint16_t* A, const uint16_t* B, float* D);
 
+/* weights of the learned closure for a handle whose record selects
+ * "SGS: mlp" (the record may instead name a float32 file in "SGS weights:");
+ * the stream-collide then takes its eddy viscosity from the MLP on the
+ * tensor cores instead of the Smagorinsky model.  n = lbm_mlp_param_count() */
+int lbm_set_sgs_mlp(lbm_handle* h, const float* params, int n);
+
 /* ------------------------------------------------------------------------
  * Ensemble of periodic D3Q19 boxes (decaying turbulence), the data source of
  * the learned closure.  No counterpart in the reference, which runs one

@@ -66,6 +66,7 @@ SIGNATURES = [
     ("lbm_mlp_train", _I, [_P, _P, _I, _I, _I, _F, ctypes.c_uint32, _P, _P, _P]),
     ("lbm_tc_selftest", _I, [_I, _P, _P, _P]),
     ("lbm_mlp_predict_tc", _I, [_P, _P, _I, _P, _P]),
+    ("lbm_set_sgs_mlp", _I, [_P, _P, _I]),
     ("lbm_ensemble_create", _I, [_I, _P, _P, _I, _F, _P]),
     ("lbm_ensemble_destroy", _I, [_P]),
     ("lbm_ensemble_init_turbulence", _I, [_P, ctypes.c_uint32, _F, _I, _I]),
@@ -189,7 +190,8 @@ def make_inputs(nx: int, ny: int, nz: int, *, obst1=(0.0, 0.0, 0.0), r1=1.0, obs
     names = {"geometry": "GEOMETRY:", "precision": "PRECISION:", "tau": "TAU:", "lid_velocity": "LID velocity:",
              "lid_face": "LID face:", "inlet_noise": "Inlet noise:", "seed": "Seed:", "velav": "VELAV:",
              "init": "Init:", "init_velocity": "Init velocity:", "order": "ORDER:", "fc_top_zflip": "FC top zflip:",
-             "edge_pull": "EDGE PULL:", "lid_bc": "LID BC:", "bounceback": "BOUNCEBACK:"}
+             "edge_pull": "EDGE PULL:", "lid_bc": "LID BC:", "bounceback": "BOUNCEBACK:", "sgs": "SGS:",
+             "sgs_weights": "SGS weights:"}
     for k, v in ext.items():
         if k not in names:
             raise KeyError(f"unknown .inputs extension key {k!r}")
@@ -359,6 +361,11 @@ class Solver:
         if out.dtype != np.float64 or out.size < 3 or not out.flags["C_CONTIGUOUS"]:
             raise ValueError("out must be a contiguous float64 array of 3")
         _check(self._lib.lbm_get_last_force_async(self._h, _ptr(out)))
+
+    def set_sgs_mlp(self, params: np.ndarray) -> None:
+        """weights of the learned closure (the record must select sgs="mlp")"""
+        p = np.ascontiguousarray(params, np.float32)
+        _check(self._lib.lbm_set_sgs_mlp(self._h, _ptr(p), p.size))
 
     def launch_count(self) -> int:
         """kernels launched by this solver so far"""

@@ -282,7 +282,7 @@ __global__ void k_d2f(const double* __restrict__ a, float* __restrict__ b, size_
 
 /* ---- launchers */
 template <int TY, int SGS> static size_t step_smem() {
-    return SGS == ens::SGS_MLP ? sizeof(sgs::InferSmem<32 * TY>) + 1024 : 0;
+    return SGS == ens::SGS_MLP ? sgs::infer_dyn_smem<32 * TY>() : 0;
 }
 
 template <int TY, int SGS> static cudaError_t step_attr() {
@@ -337,8 +337,6 @@ int ens_step_occupancy(int ty, int sgs) {
                                                               step_smem<8, ens::SGS_MLP>());
     }
     if (e != cudaSuccess) return 1;
-    /* TMEM: each resident block of the MLP variant holds 32 * ty columns of 512 */
-    if (sgs == ens::SGS_MLP && nb * 16 * ty > 512) nb = 512 / (16 * ty);
     return nb < 1 ? 1 : nb;
 }
 

@@ -26,6 +26,7 @@
 
 #include "../../include/lbm_gb300.h"
 #include "lbm_kernels.cuh"
+#include "sgs_infer.cuh"
 
 using namespace lbm;
 
@@ -90,6 +91,8 @@ struct Config {
     int pull_clamp = 0;             /* "EDGE PULL: clamp" (CPU_3D) or "wrap" */
     int halfway = 0;                /* "BOUNCEBACK: halfway" or "fullway" (the reference) */
     int lid_quirk = 0;              /* "LID BC: cpu3d" reproduces CPU_3D's lid as written */
+    int sgs_mlp = 0;                /* "SGS: mlp": the learned closure replaces Smagorinsky */
+    std::string sgs_weights;        /* "SGS weights: <file>" of float32 parameters */
     /* older records spell the LES line "Smagorinski LES: YES/NO"; DynInlet
      * records add "KP" (the inlet P-control gain, MRTtest/DynInlet3.cu:26) */
     bool les_yesno = false;
@@ -195,6 +198,11 @@ int parse_inputs(const char* text, Config& c) {
             ok = (val == "halfway" || val == "fullway");
             c.halfway = val == "halfway";
         }
+        else if (key == "SGS") {
+            ok = (val == "mlp" || val == "smagorinsky");
+            c.sgs_mlp = val == "mlp";
+        }
+        else if (key == "SGS weights") c.sgs_weights = val;
         else if (key == "LID BC") {
             ok = (val == "cpu3d" || val == "regularized");
             c.lid_quirk = val == "cpu3d";
@@ -289,6 +297,8 @@ std::string value_of(const Config& c, const std::string& key, float omega, float
     else if (key == "EDGE PULL") o << (c.pull_clamp ? "clamp" : "wrap");
     else if (key == "LID BC") o << (c.lid_quirk ? "cpu3d" : "regularized");
     else if (key == "BOUNCEBACK") o << (c.halfway ? "halfway" : "fullway");
+    else if (key == "SGS") o << (c.sgs_mlp ? "mlp" : "smagorinsky");
+    else if (key == "SGS weights") o << c.sgs_weights;
     return o.str();
 }
 
@@ -345,6 +355,8 @@ std::string write_inputs(const Config& c, float omega, float omegaLR) {
     if (c.pull_clamp) line("EDGE PULL: ", "EDGE PULL");
     if (c.lid_quirk) line("LID BC: ", "LID BC");
     if (c.halfway) line("BOUNCEBACK: ", "BOUNCEBACK");
+    if (c.sgs_mlp) line("SGS: ", "SGS");
+    if (!c.sgs_weights.empty()) line("SGS weights: ", "SGS weights");
     return o.str();
 }
 
@@ -460,6 +472,10 @@ struct lbm_handle {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     long long launches = 0;         /* kernels this handle has launched */
+    /* learned subgrid closure: device weight blob and its error flag */
+    unsigned char* mlp_blob = nullptr;
+    int* mlp_err = nullptr;
+    bool mlp_ready = false;
 };
 
 namespace {
@@ -670,8 +686,15 @@ int one_step(lbm_handle* h) {
         int rc = ensure_force_cap(h, fidx + 1);
         if (rc) return rc;
     }
+    if (c.sgs_mlp && !h->mlp_ready)
+        return fail(LBM_ERR_STATE, "SGS mlp: no weights (SGS weights record line or lbm_set_sgs_mlp)");
     if (p.force_on) CUDA_TRY(fork_force(h, C, h->force_hist + 3LL * fidx));
-    CUDA_TRY(launch_stream_collide(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, h->mom, h->stream, C.links));
+    if (c.sgs_mlp)
+        CUDA_TRY(launch_stream_collide_mlp(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, C.links, h->mlp_blob,
+                                           h->mlp_err, h->stream));
+    else
+        CUDA_TRY(launch_stream_collide(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, h->mom, h->stream,
+                                       C.links));
     ++h->launches;
     if (p.force_on) CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
     C.cur = 1 - C.cur;
@@ -823,6 +846,16 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
             return fail(LBM_ERR_CONFIG, "refinement patch does not fit in the base grid");
         if (c.lrx < 2 * lev + 2 || c.lry < 2 * lev + 2) return fail(LBM_ERR_CONFIG, "refinement patch too small");
     }
+    if (c.sgs_mlp && (c.refinement || c.geometry == "cavity" || c.pull_clamp || storage == STORE_F64))
+        return fail(LBM_ERR_CONFIG, "SGS mlp runs on channel and periodic levels without refinement, FP32/FP16/BF16");
+    std::vector<float> sgs_params;
+    if (!c.sgs_weights.empty()) {
+        std::ifstream in(c.sgs_weights, std::ios::binary);
+        sgs_params.resize(sgs::NPARAM);
+        if (!in.read(reinterpret_cast<char*>(sgs_params.data()), sgs::NPARAM * sizeof(float)))
+            return fail(LBM_ERR_CONFIG, "SGS weights: cannot read %d float32 values from '%s'", sgs::NPARAM,
+                        c.sgs_weights.c_str());
+    }
     int dev = 0;
     CUDA_TRY(cudaGetDevice(&dev));
     lbm_handle* h = new lbm_handle();
@@ -879,6 +912,7 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
         cudaMalloc(&h->audit_out, 4 * sizeof(double)) != cudaSuccess)
         return bail(fail(LBM_ERR_NOMEM, "cannot allocate audit scratch"));
     if ((rc = ensure_force_cap(h, std::max(1, c.tmax - c.startf)))) return bail(rc);
+    if (!sgs_params.empty() && (rc = lbm_set_sgs_mlp(h, sgs_params.data(), sgs::NPARAM))) return bail(rc);
     if ((rc = do_init(h))) return bail(rc);
     *out = h;
     return LBM_OK;
@@ -894,6 +928,8 @@ int lbm_destroy(lbm_handle* h) {
     cudaFree(h->audit_out);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    cudaFree(h->mlp_blob);
+    cudaFree(h->mlp_err);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->side) cudaStreamDestroy(h->side);
@@ -1005,6 +1041,31 @@ int lbm_step_timed(lbm_handle* h, int nsteps, float* ms) {
 int lbm_synchronize(lbm_handle* h) {
     if (!h) return fail(LBM_ERR_ARG, "null handle");
     CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (h->mlp_err) {
+        int e = 0;
+        CUDA_TRY(cudaMemcpy(&e, h->mlp_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (e) {
+            cudaMemset(h->mlp_err, 0, sizeof(int));
+            return fail(LBM_ERR_CUDA, "SGS mlp: a tensor-core completion wait ran out");
+        }
+    }
+    return LBM_OK;
+}
+
+int lbm_set_sgs_mlp(lbm_handle* h, const float* params, int n) {
+    if (!h || !params) return fail(LBM_ERR_ARG, "null argument");
+    if (n != sgs::NPARAM) return fail(LBM_ERR_ARG, "SGS mlp: %d parameters, expected %d", n, sgs::NPARAM);
+    if (!h->cfg.sgs_mlp) return fail(LBM_ERR_STATE, "SGS mlp: the record does not select 'SGS: mlp'");
+    std::vector<unsigned char> blob(sgs::BLOB_BYTES);
+    mlp_make_blob(params, blob.data());
+    if (!h->mlp_blob) CUDA_TRY(cudaMalloc(&h->mlp_blob, sgs::BLOB_BYTES));
+    if (!h->mlp_err) {
+        CUDA_TRY(cudaMalloc(&h->mlp_err, sizeof(int)));
+        CUDA_TRY(cudaMemset(h->mlp_err, 0, sizeof(int)));
+    }
+    CUDA_TRY(cudaMemcpyAsync(h->mlp_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->mlp_ready = true;
     return LBM_OK;
 }
 
@@ -1090,10 +1151,15 @@ int lbm_time_stream_collide(lbm_handle* h, int level, int n, float* ms) {
     StepParams p = base_params(h, level);
     p.t = h->t;
     p.stats_on = 0;
+    if (h->cfg.sgs_mlp && !h->mlp_ready) return fail(LBM_ERR_STATE, "SGS mlp: no weights");
     CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
     for (int i = 0; i < n; ++i) {
-        CUDA_TRY(launch_stream_collide(s.L, p, s.f[s.cur], s.f[1 - s.cur], s.mask, nullptr, nullptr, h->stream,
-                                       s.links));
+        if (h->cfg.sgs_mlp)
+            CUDA_TRY(launch_stream_collide_mlp(s.L, p, s.f[s.cur], s.f[1 - s.cur], s.mask, nullptr, s.links,
+                                               h->mlp_blob, h->mlp_err, h->stream));
+        else
+            CUDA_TRY(launch_stream_collide(s.L, p, s.f[s.cur], s.f[1 - s.cur], s.mask, nullptr, nullptr, h->stream,
+                                           s.links));
         ++h->launches;
         s.cur = 1 - s.cur;
     }

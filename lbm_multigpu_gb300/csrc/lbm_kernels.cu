@@ -22,6 +22,7 @@
 
 #include "d3q19.cuh"
 #include "lbm_kernels.cuh"
+#include "sgs_infer.cuh"
 
 namespace lbm {
 
@@ -183,6 +184,124 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
             for (int i = 0; i < 9; ++i) mom_export[i * ne + ce] = mom[i];
         }
     }
+}
+
+/* The stream-collide step with the learned subgrid closure in place of the
+ * Smagorinsky model: the node update of k_stream_collide (pull, half-way or
+ * full-way bounce-back, inlet/outlet rebuild with inlet noise, running
+ * statistics; no lid, no clamped edges, no refinement export), with the
+ * eddy viscosity of every node from the MLP evaluated on the tensor cores
+ * for the whole 32 x 8 tile at once.  Persistent blocks walk the tiles so
+ * that each block stages the weights and allocates its TMEM once per launch.
+ * MRT collision (LR7:583-711) at tau_eff = tau0 + 3 nu_t; FP32 arithmetic. */
+template <class S, bool HALFWAY>
+__global__ void __launch_bounds__(SC_BX* SC_BY, 2) k_stream_collide_mlp(const Level L, const StepParams p,
+                                                                      const S* __restrict__ fA, S* __restrict__ fB,
+                                                                      const uint8_t* __restrict__ mask,
+                                                                      float* __restrict__ stats,
+                                                                      const uint32_t* __restrict__ links,
+                                                                      const unsigned char* __restrict__ blob,
+                                                                      int* __restrict__ err) {
+    using F = Fmt<S>;
+    constexpr int ROWS = SC_BX * SC_BY;
+    extern __shared__ unsigned char dsm[];
+    sgs::InferSmem<ROWS>& sm = *reinterpret_cast<sgs::InferSmem<ROWS>*>(
+        (reinterpret_cast<uintptr_t>(dsm) + 1023) & ~uintptr_t(1023));
+#if defined(__CUDA_ARCH__)
+    sgs::infer_setup<ROWS>(sm, blob);
+    const unsigned qs = unsigned(L.qstride);
+    const unsigned plane = unsigned(L.plane), pitch = unsigned(L.pitch);
+    const int tiles_x = L.pitch / SC_BX, tiles_y = (L.ny + SC_BY - 1) / SC_BY;
+    const int ntiles = tiles_x * tiles_y * L.nz;
+    const float tau0 = 1.f / p.omega;
+    for (int g = blockIdx.x; g < ntiles; g += gridDim.x) {
+        const int z = g / (tiles_x * tiles_y), r = g - z * tiles_x * tiles_y;
+        const int x = (r % tiles_x) * SC_BX + int(threadIdx.x), y = (r / tiles_x) * SC_BY + int(threadIdx.y);
+        const bool live = x < L.nx && y < L.ny;
+        float f[19];
+        int type = FLUID;
+        unsigned c = 0;
+        if (live) {
+            c = unsigned(z) * plane + unsigned(y) * pitch + unsigned(x);
+            const int mbyte = mask[c];
+            type = mbyte & TYPE_MASK;
+            const unsigned xm = (x == 0) ? L.nx - 1 : x - 1, xp = (x == L.nx - 1) ? 0 : x + 1;
+            const unsigned ym = (y == 0) ? L.ny - 1 : y - 1, yp = (y == L.ny - 1) ? 0 : y + 1;
+            const unsigned zm = (z == 0) ? L.nz - 1 : z - 1, zp = (z == L.nz - 1) ? 0 : z + 1;
+            const unsigned zb[3] = {zm * plane, z * plane, zp * plane};
+            const unsigned yb[3] = {ym * pitch, y * pitch, yp * pitch};
+            const unsigned xs[3] = {xm, unsigned(x), xp};
+#pragma unroll
+            for (int q = 0; q < 19; ++q)
+                f[q] = F::ld(fA + q * qs + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)], L.off[q]);
+            if (HALFWAY && (mbyte & NEAR_SOLID)) {
+                const uint32_t lk = links[c];
+#pragma unroll
+                for (int q = 1; q < 19; ++q)
+                    if (lk & (1u << q)) f[q] = F::ld(fA + opp(q) * qs + c, L.off[opp(q)]);
+            }
+            if (type >= WEST_INLET && type <= NORTH_OUTLET) {
+                unsigned nb;
+                if (type == WEST_INLET) nb = zb[1] + yb[1] + xp;
+                else if (type == EAST_OUTLET) nb = zb[1] + yb[1] + xm;
+                else if (type == SOUTH_INLET) nb = zb[1] + yb[2] + x;
+                else nb = zb[1] + yb[0] + x;
+#pragma unroll
+                for (int q = 0; q < 19; ++q) f[q] = F::ld(fA + q * qs + nb, L.off[q]);
+                float uin = p.u_in;
+                if (p.noise_amp != 0.f) {
+                    const uint32_t cell = uint32_t((z * L.ny + y) * L.nx + x);
+                    const float xi = philox_uniform(p.noise_seed, cell, uint32_t(p.t));
+                    uin = uin + p.u_in * p.noise_amp * (2.f * xi - 1.f);
+                }
+                extrap<float>(type, f, p.rho_out, uin);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) f[q] = wq(q);
+        }
+        /* the closure for the whole tile */
+        float rho, p6[6], xf[sgs::NIN];
+        pi_neq<float>(f, rho, p6);
+        const float sc = -1.5f / rho;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) p6[k] *= sc;
+        sgs::features<float>(p6, tau0, xf);
+        const float nu = sgs::infer_nu<ROWS>(sm, xf, err);
+        if (!live) continue;
+        if (type == WALL || type == BODY) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) F::st(fB + q * qs + c, f[opp(q)], L.off[q]);
+            continue;
+        }
+        collide_mrt<MRT>(f, 1.f / (tau0 + 3.f * nu), false, 0.f, 0.f);
+        if (p.stats_on && p.t >= p.start_av) {
+            float u = 0, v = 0;
+#pragma unroll
+            for (int q = 0; q < 19; ++q) {
+                if (cx(q)) u += float(cx(q)) * f[q];
+                if (cy(q)) v += float(cy(q)) * f[q];
+            }
+            float* au = stats;
+            float* av = stats + qs;
+            const float w = p.stats_weight;
+            if (p.t < p.start_fluc) {
+                const float n = float(p.t - p.start_av);
+                au[c] = (au[c] * n + u * w) / (n + w);
+                av[c] = (av[c] * n + v * w) / (n + w);
+            } else {
+                float* fu = stats + 2 * (size_t)qs;
+                float* fv = stats + 3 * (size_t)qs;
+                const float n = float(p.t - p.start_fluc);
+                fu[c] = (fu[c] * n + (u - au[c]) * (u - au[c]) * w) / (n + w);
+                fv[c] = (fv[c] * n + (v - av[c]) * (v - av[c]) * w) / (n + w);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 19; ++q) F::st(fB + q * qs + c, f[q], L.off[q]);
+    }
+    sgs::infer_teardown<ROWS>(sm);
+#endif
 }
 
 /* Momentum exchange at BODY nodes (LR7:1494-1502, reduced per block at
@@ -635,6 +754,51 @@ cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const voi
     }
 #undef LBM_SC
     return cudaGetLastError();
+}
+
+template <class S, bool HW> static cudaError_t sc_mlp_t(const Level& L, const StepParams& p, const void* fA, void* fB,
+                                                        const uint8_t* mask, float* stats, const uint32_t* links,
+                                                        const void* blob, int* err, cudaStream_t s) {
+    const size_t smem = sgs::infer_dyn_smem<SC_BX * SC_BY>();
+    static cudaError_t attr = cudaErrorNotReady;
+    static int grid = 0;
+    if (attr == cudaErrorNotReady) {
+        attr = cudaFuncSetAttribute(k_stream_collide_mlp<S, HW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    int(smem));
+        int nb = 0, dev = 0, sms = 0;
+        if (attr == cudaSuccess)
+            attr = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stream_collide_mlp<S, HW>, SC_BX * SC_BY, smem);
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        /* the shared-memory request already keeps TMEM (128 columns per
+         * block, 512 per SM) from being over-subscribed */
+        nb = nb < 1 ? 1 : nb;
+        grid = (sms > 0 ? sms : 152) * nb;
+    }
+    if (attr != cudaSuccess) return attr;
+    const int ntiles = (L.pitch / SC_BX) * ((L.ny + SC_BY - 1) / SC_BY) * L.nz;
+    k_stream_collide_mlp<S, HW><<<grid < ntiles ? grid : ntiles, dim3(SC_BX, SC_BY), smem, s>>>(
+        L, p, (const S*)fA, (S*)fB, mask, stats, links, (const unsigned char*)blob, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_collide_mlp(const Level& L, const StepParams& p, const void* fA, void* fB,
+                                      const uint8_t* mask, float* stats, const uint32_t* links, const void* blob,
+                                      int* err, cudaStream_t s) {
+    if ((p.halfway && !links) || !blob || !err || p.has_lid || p.pull_clamp || p.exp_nx > 0)
+        return cudaErrorInvalidValue;
+    switch (L.storage) {
+        case STORE_F32:
+            return p.halfway ? sc_mlp_t<float, true>(L, p, fA, fB, mask, stats, links, blob, err, s)
+                             : sc_mlp_t<float, false>(L, p, fA, fB, mask, stats, links, blob, err, s);
+        case STORE_F16:
+            return p.halfway ? sc_mlp_t<__half, true>(L, p, fA, fB, mask, stats, links, blob, err, s)
+                             : sc_mlp_t<__half, false>(L, p, fA, fB, mask, stats, links, blob, err, s);
+        case STORE_BF16:
+            return p.halfway ? sc_mlp_t<__nv_bfloat16, true>(L, p, fA, fB, mask, stats, links, blob, err, s)
+                             : sc_mlp_t<__nv_bfloat16, false>(L, p, fA, fB, mask, stats, links, blob, err, s);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 int force_partials() { return FORCE_BLOCKS; }

@@ -78,6 +78,13 @@ inline int sc_blocks(const Level& L) {
 cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const void* fA, void* fB,
                                   const uint8_t* mask, float* stats, float* mom_export, cudaStream_t s,
                                   const uint32_t* links = nullptr);
+/* the same step with the learned closure (tensor-core MLP) in place of the
+ * Smagorinsky model; blob = weights (sgs::BLOB_BYTES), err = device flag set
+ * to 2 when an MMA completion wait ran out.  Channel features only: no lid,
+ * no clamped edges, no refinement export; FP32 / FP16 / BF16 storage */
+cudaError_t launch_stream_collide_mlp(const Level& L, const StepParams& p, const void* fA, void* fB,
+                                      const uint8_t* mask, float* stats, const uint32_t* links, const void* blob,
+                                      int* err, cudaStream_t s);
 /* FP64 momentum exchange over a list of BODY nodes (pitched indices), ADDED to out3 */
 cudaError_t launch_force(const Level& L, const void* fA, const unsigned* body, int nbody, double* partials,
                          unsigned* done, double* out3, cudaStream_t s, const uint8_t* mask = nullptr,

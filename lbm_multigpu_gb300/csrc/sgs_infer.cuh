@@ -17,6 +17,7 @@
  */
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_runtime.h>
 
 #include "sgs_mlp.cuh"
 #include "tc_sm103.cuh"
@@ -31,6 +32,14 @@ constexpr uint32_t W1_BYTES = NH * NIN * 2, W2_BYTES = NH * NH * 2;
 /* device weight blob: W1 and W2 already in the core-matrix layout as bf16,
  * then b2[64], w3[64], b3 as FP32 */
 constexpr uint32_t BLOB_BYTES = W1_BYTES + W2_BYTES + (2 * NH + 4) * 4;
+constexpr int SM_SMEM_BYTES = 228 * 1024; /* shared memory per SM */
+
+template <int ROWS> struct InferSmem;
+
+/* dynamic shared memory for a block of ROWS rows that holds InferSmem (plus
+ * 1 KB of alignment slack) and is large enough that no more blocks than TMEM
+ * can serve (512 columns) fit on one SM */
+template <int ROWS> inline size_t infer_dyn_smem();
 
 template <int ROWS> struct InferSmem {
     alignas(1024) unsigned char w1[W1_BYTES];
@@ -43,12 +52,38 @@ template <int ROWS> struct InferSmem {
     uint32_t phase;
 };
 
+/* TMEM columns a block holds: 64 per 128 rows */
+template <int ROWS> __host__ __device__ constexpr int tmem_cols() { return ROWS / 2 < 32 ? 32 : ROWS / 2; }
+
+template <int ROWS> inline size_t infer_dyn_smem() {
+    static size_t v = 0;
+    if (!v) {
+        int dev = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+            per_sm <= 0)
+            per_sm = SM_SMEM_BYTES;
+        const int max_blocks = 512 / tmem_cols<ROWS>();
+        const size_t need = sizeof(InferSmem<ROWS>) + 1024;
+        const size_t floor = size_t(per_sm) / size_t(max_blocks + 1) + 1;
+        v = need > floor ? need : floor;
+    }
+    return v;
+}
+
 #if defined(__CUDA_ARCH__)
 
-/* once per block: weights into shared memory, the mbarrier, TMEM columns
- * (64 per 128 rows) */
+/* linear thread index (blocks may be 1-D or 2-D): row of the block's tile */
+__device__ __forceinline__ int row_index() {
+    return int(threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z));
+}
+
+/* once per block: weights into shared memory, the mbarrier, TMEM columns.
+ * tcgen05.alloc waits until the columns are free, so a launch must never
+ * make more blocks resident on an SM than 512 / tmem_cols<ROWS>() (the
+ * launchers size dynamic shared memory to guarantee it) */
 template <int ROWS> __device__ __forceinline__ void infer_setup(InferSmem<ROWS>& s, const unsigned char* blob) {
-    const int t = threadIdx.x;
+    const int t = row_index();
     const uint4* src = reinterpret_cast<const uint4*>(blob);
     for (int i = t; i < int(W1_BYTES / 16); i += ROWS) reinterpret_cast<uint4*>(s.w1)[i] = src[i];
     for (int i = t; i < int(W2_BYTES / 16); i += ROWS)
@@ -63,7 +98,7 @@ template <int ROWS> __device__ __forceinline__ void infer_setup(InferSmem<ROWS>&
         tc::mbar_init(&s.mbar, 1);
         s.phase = 0;
     }
-    if (t < 32) tc::tmem_alloc(&s.tmem, ROWS / 2 < 32 ? 32 : ROWS / 2);
+    if (t < 32) tc::tmem_alloc(&s.tmem, tmem_cols<ROWS>());
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
@@ -73,7 +108,7 @@ template <int ROWS> __device__ __forceinline__ void infer_setup(InferSmem<ROWS>&
 template <int ROWS> __device__ __forceinline__ void infer_teardown(InferSmem<ROWS>& s) {
     tc::fence_before_sync();
     __syncthreads();
-    if (threadIdx.x < 32) tc::tmem_dealloc(s.tmem, ROWS / 2 < 32 ? 32 : ROWS / 2);
+    if (row_index() < 32) tc::tmem_dealloc(s.tmem, tmem_cols<ROWS>());
 }
 
 __device__ __forceinline__ float gelu_fast(float z) {
@@ -93,7 +128,7 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
  * returns false when a completion wait ran out */
 template <int ROWS> __device__ __forceinline__ bool infer_mma_wait(InferSmem<ROWS>& s) {
     /* block-uniform verdict: tcgen05.ld below is warp-collective */
-    const bool ok = __syncthreads_and(tc::mbar_wait(&s.mbar, s.phase, 1u << 22));
+    const bool ok = __syncthreads_and(tc::mbar_wait(&s.mbar, s.phase, 1u << 20));
     tc::fence_after_sync();
     return ok;
 }
@@ -101,7 +136,7 @@ template <int ROWS> __device__ __forceinline__ bool infer_mma_wait(InferSmem<ROW
 /* nu_t of this thread's row; x[16] are its features (FP32) */
 template <int ROWS> __device__ __forceinline__ float infer_nu(InferSmem<ROWS>& s, const float x[NIN], int* err) {
     static_assert(ROWS == 128 || ROWS == 256, "one or two M=128 MMAs per block");
-    const int t = threadIdx.x, warp = t >> 5;
+    const int t = row_index(), warp = t >> 5;
     /* A of layer 1 */
     {
         uint4 v0, v1;
@@ -126,23 +161,26 @@ template <int ROWS> __device__ __forceinline__ float infer_nu(InferSmem<ROWS>& s
     }
     bool ok = infer_mma_wait(s);
     const uint32_t ta = s.tmem + (uint32_t((warp & 3) * 32) << 16) + uint32_t(warp >> 2) * 64;
-    uint32_t r[64];
-    if (ok) {
+    /* accumulator columns in chunks of 16 (few live registers):
+     * GELU -> bf16 -> A of layer 2 */
 #pragma unroll
-        for (int c = 0; c < 4; ++c) tc::tmem_ld16(ta + 16 * c, r + 16 * c);
-        tc::tmem_wait_ld();
-        tc::tmem_fence_regs<64>(r);
-    }
-    /* GELU -> bf16 -> A of layer 2 */
+    for (int c = 0; c < 4; ++c) {
+        uint32_t r[16];
+        if (ok) {
+            tc::tmem_ld16(ta + 16 * c, r);
+            tc::tmem_wait_ld();
+            tc::tmem_fence_regs<16>(r);
+        }
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        uint4 v;
-        float g[8];
+        for (int h = 0; h < 2; ++h) {
+            float g[8];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) g[k] = ok ? gelu_fast(__uint_as_float(r[8 * c + k])) : 0.f;
-        v.x = pack_bf16(g[0], g[1]), v.y = pack_bf16(g[2], g[3]), v.z = pack_bf16(g[4], g[5]),
-        v.w = pack_bf16(g[6], g[7]);
-        *reinterpret_cast<uint4*>(s.a2 + tc::core_off(t, 8 * c, W2_LBO, W2_SBO)) = v;
+            for (int k = 0; k < 8; ++k) g[k] = ok ? gelu_fast(__uint_as_float(r[8 * h + k])) : 0.f;
+            uint4 v;
+            v.x = pack_bf16(g[0], g[1]), v.y = pack_bf16(g[2], g[3]), v.z = pack_bf16(g[4], g[5]),
+            v.w = pack_bf16(g[6], g[7]);
+            *reinterpret_cast<uint4*>(s.a2 + tc::core_off(t, 16 * c + 8 * h, W2_LBO, W2_SBO)) = v;
+        }
     }
     tc::fence_async_smem();
     tc::fence_before_sync();
@@ -161,15 +199,19 @@ template <int ROWS> __device__ __forceinline__ float infer_nu(InferSmem<ROWS>& s
     }
     __syncthreads(); /* every thread sees the flipped phase */
     ok = infer_mma_wait(s) && ok;
-    if (ok) {
-#pragma unroll
-        for (int c = 0; c < 4; ++c) tc::tmem_ld16(ta + 16 * c, r + 16 * c);
-        tc::tmem_wait_ld();
-        tc::tmem_fence_regs<64>(r);
-    }
     float y = s.b3;
 #pragma unroll
-    for (int k = 0; k < NH; ++k) y = fmaf(s.w3[k], gelu_fast(__uint_as_float(r[k]) + s.b2[k]), y);
+    for (int c = 0; c < 4; ++c) {
+        uint32_t r[16];
+        if (ok) {
+            tc::tmem_ld16(ta + 16 * c, r);
+            tc::tmem_wait_ld();
+            tc::tmem_fence_regs<16>(r);
+        }
+#pragma unroll
+        for (int k = 0; k < 16; ++k)
+            y = ok ? fmaf(s.w3[16 * c + k], gelu_fast(__uint_as_float(r[k]) + s.b2[16 * c + k]), y) : y;
+    }
     tc::fence_before_sync();
     __syncthreads();
     if (t == 0) s.phase ^= 1;

@@ -269,7 +269,9 @@ __global__ void __launch_bounds__(128) k_tc_selftest(const __nv_bfloat16* __rest
 __global__ void __launch_bounds__(128) k_mlp_predict_tc(const unsigned char* __restrict__ blob,
                                                         const float* __restrict__ X, int n, float* __restrict__ nu,
                                                         int* __restrict__ err) {
-    __shared__ InferSmem<128> s;
+    extern __shared__ unsigned char dsm[];
+    InferSmem<128>& s =
+        *reinterpret_cast<InferSmem<128>*>((reinterpret_cast<uintptr_t>(dsm) + 1023) & ~uintptr_t(1023));
 #if defined(__CUDA_ARCH__)
     infer_setup<128>(s, blob);
     for (int base = blockIdx.x * 128; base < n; base += gridDim.x * 128) {
@@ -326,7 +328,12 @@ cudaError_t launch_mlp_predict_tc(const void* blob, const float* X, int n, float
     int b = (n + 127) / 128;
     if (b > 152 * 4) b = 152 * 4;
     if (b < 1) b = 1;
-    sgs::k_mlp_predict_tc<<<b, 128, 0, s>>>((const unsigned char*)blob, X, n, nu, err);
+    const size_t smem = sgs::infer_dyn_smem<128>();
+    static cudaError_t attr = cudaErrorNotReady;
+    if (attr == cudaErrorNotReady)
+        attr = cudaFuncSetAttribute(sgs::k_mlp_predict_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (attr != cudaSuccess) return attr;
+    sgs::k_mlp_predict_tc<<<b, 128, smem, s>>>((const unsigned char*)blob, X, n, nu, err);
     return cudaGetLastError();
 }
 

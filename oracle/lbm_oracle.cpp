@@ -500,7 +500,14 @@ void step_impl(const orc_params* p, const uint8_t* mask, const T* fA, T* fB, dou
                     } else if (im == ORC_LID) {
                         lid<T>(f, p->lid_face, T(p->lid_u[0]), T(p->lid_u[1]), T(p->lid_u[2]), p->lid_quirk);
                     }
-                    collide<T>(p->model, f, T(p->omega), p->les, T(p->cs), T(p->dpdy));
+                    if (p->mlp) {
+                        double g[Q];
+                        for (int q = 0; q < Q; ++q) g[q] = double(f[q]);
+                        orc_collide_mlp(p->mlp, 1.0 / double(p->omega), g, 1, nullptr);
+                        for (int q = 0; q < Q; ++q) f[q] = T(g[q]);
+                    } else {
+                        collide<T>(p->model, f, T(p->omega), p->les, T(p->cs), T(p->dpdy));
+                    }
                     if (p->stats_on && av_u) {
                         /* vel_av / vel_fluc (LR7:1018-1058) */
                         float u = 0, v = 0;

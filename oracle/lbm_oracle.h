@@ -75,6 +75,10 @@ typedef struct {
     int lid_quirk;
     /* half-way bounce-back (extension; the reference is full-way) */
     int halfway;
+    /* learned subgrid closure (sgs_oracle.cpp): when non-null, the collision
+     * of fluid and boundary nodes takes nu_t from this MLP parameter vector
+     * (MRT at tau0 + 3 nu_t) instead of the model / LES settings */
+    const float* mlp;
 } orc_params;
 
 typedef struct {
@@ -123,6 +127,8 @@ double orc_mass(const float* f, const uint8_t* mask, int ncell);
 uint32_t orc_noise_hash(uint32_t seed, uint32_t cell, uint32_t step);
 float orc_noise_uniform(uint32_t seed, uint32_t cell, uint32_t step);
 int orc_num_threads(void);
+/* learned subgrid closure (sgs_oracle.cpp) */
+void orc_collide_mlp(const float* params, double tau0, double* f, int n, double* nu_out);
 void orc_set_num_threads(int n);
 
 #ifdef __cplusplus

@@ -37,7 +37,7 @@ class Params(ctypes.Structure):
                 ("start_fluc", ctypes.c_int), ("stats_weight", _F), ("exp_x0", ctypes.c_int),
                 ("exp_y0", ctypes.c_int), ("exp_nx", ctypes.c_int), ("exp_ny", ctypes.c_int),
                 ("noise_amp", _F), ("noise_seed", ctypes.c_uint32), ("pull_clamp", ctypes.c_int),
-                ("lid_quirk", ctypes.c_int), ("halfway", ctypes.c_int)]
+                ("lid_quirk", ctypes.c_int), ("halfway", ctypes.c_int), ("mlp", ctypes.c_void_p)]
 
 
 class Refine(ctypes.Structure):
@@ -87,11 +87,14 @@ class OracleRun:
 
     def __init__(self, nx, ny, nz, mask, omega, *, model=0, les=0, cs=0.02, dpdy=0.0, u_in=0.05, init_kind=0,
                  init_u=0.05, lid_u=(0, 0, 0), lid_face=5, startf=0, refine=None, noise_amp=0.0, seed=12345,
-                 stats=None, f0=None, pull_clamp=0, lid_quirk=0, halfway=0):
+                 stats=None, f0=None, pull_clamp=0, lid_quirk=0, halfway=0, mlp=None):
         o = oracle()
         self.p = Params(nx=nx, ny=ny, nz=nz, model=model, les=les, omega=omega, cs=cs, dpdy=dpdy, u_in=u_in,
                         rho_out=1.0, lid_face=lid_face, stats_weight=1.0, noise_amp=noise_amp, noise_seed=seed,
                         pull_clamp=pull_clamp, lid_quirk=lid_quirk, halfway=halfway)
+        if mlp is not None:
+            self._mlp = np.ascontiguousarray(mlp, np.float32)
+            self.p.mlp = self._mlp.ctypes.data
         self.p.lid_u[:] = list(lid_u)
         if stats:
             self.p.stats_on, self.p.start_av, self.p.start_fluc = 1, stats[0], stats[1]

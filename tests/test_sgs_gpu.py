@@ -134,3 +134,48 @@ def test_tensor_core_inference_matches_oracle(product):
     oracle().orc_mlp_forward(ptr(P), ptr(X), len(X), ptr(want))
     assert (got >= 0).all()
     assert np.linalg.norm(got - want) <= 2e-2 * np.linalg.norm(want), np.linalg.norm(got - want) / np.linalg.norm(want)
+
+
+@pytest.mark.parametrize("bounceback", ["halfway", "fullway"])
+def test_channel_with_learned_closure_vs_oracle(product, bounceback):
+    """the channel stream-collide with the learned closure in place of
+    Smagorinsky (tensor-core MLP per 32 x 8 tile, persistent blocks) against
+    the oracle's step with the same closure in FP64; the BF16 inference error
+    stays under 5% of the closure's own effect (its distance to Smagorinsky)"""
+    from oracle_bindings import OracleRun, moments, rel_l2
+
+    lbm = product
+    lib = lbm.library()
+    P = _params(lib, 21) * 3
+    P[-1] = 40.0            # nu_t near 4e-3: tau_eff well above tau0
+    NX_, NY_, NZ_, steps = 64, 24, 6, 30
+    kw = dict(obst1=(20.5, 11.5, 0.0), r1=4.0, re=60.0, umax=0.05, tmax=steps, les=1, cs=0.01,
+              geometry="channel_square", bounceback=bounceback)
+    with lbm.Solver(lbm.make_inputs(NX_, NY_, NZ_, sgs="mlp", **kw)) as s:
+        s.set_sgs_mlp(P)
+        s.step(steps)
+        f, mask, om = s.populations(), s.mask(), s.params()["omega"]
+    with lbm.Solver(lbm.make_inputs(NX_, NY_, NZ_, **kw)) as s:
+        s.step(steps)
+        f_smag = s.populations()
+    o = OracleRun(NX_, NY_, NZ_, mask, om, model=0, les=0, init_kind=0, init_u=0.05,
+                  halfway=int(bounceback == "halfway"), mlp=P)
+    o.step(steps)
+    fl = (mask != 1) & (mask != 2)
+    j = moments(f)[1][:, fl]
+    jo = moments(o.fa)[1][:, fl]
+    js = moments(f_smag)[1][:, fl]
+    effect = rel_l2(js, jo)
+    assert effect > 1e-4
+    assert rel_l2(j, jo) < 0.05 * effect, (rel_l2(j, jo), effect)
+
+
+def test_closure_requires_weights(product):
+    lbm = product
+    text = lbm.make_inputs(64, 24, 6, obst1=(20.5, 11.5, 0.0), r1=4.0, re=60.0, umax=0.05, tmax=10, les=1,
+                           geometry="channel_square", sgs="mlp")
+    with lbm.Solver(text) as s:
+        with pytest.raises(lbm.LbmError):
+            s.step(1)
+        with pytest.raises(lbm.LbmError):
+            s.set_sgs_mlp(np.zeros(10, np.float32))
