@@ -233,10 +233,12 @@ __global__ void k_box_filter(const float* __restrict__ u, int n, double* __restr
     for (int k = 0; k < 6; ++k) uu[k * cn + o] = p[k] / 8;
 }
 
-/* training samples of the filtered member: features of p = (tau0 + 3 nu) S
- * and the least-squares eddy viscosity nu of the subgrid stress */
-__global__ void k_sgs_targets(const double* __restrict__ ubar, const double* __restrict__ uu, int nc, double tau0,
-                              float* __restrict__ X, float* __restrict__ T) {
+/* training samples of the filtered member, pass 1 per coarse cell: the
+ * filtered strain S (central differences, periodic) and the two
+ * contractions of the least-squares eddy viscosity, tau^d : S and S : S,
+ * with tau = uu - ubar ubar the filtered subgrid stress */
+__global__ void k_sgs_contract(const double* __restrict__ ubar, const double* __restrict__ uu, int nc,
+                               double* __restrict__ s8) {
     const size_t cn = size_t(nc) * nc * nc;
     const size_t o = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (o >= cn) return;
@@ -264,10 +266,31 @@ __global__ void k_sgs_targets(const double* __restrict__ ubar, const double* __r
         ts += w * tau[k] * S[k];
         ss += w * S[k] * S[k];
     }
+    for (int k = 0; k < 6; ++k) s8[k * cn + o] = S[k];
+    s8[6 * cn + o] = ts;
+    s8[7 * cn + o] = ss;
+}
+
+/* pass 2: nu = max(0, -<tau^d:S> / (2 <S:S>)) with <> the 3x3x3 box average
+ * (periodic), the features of p = (tau0 + 3 nu) S, and the target nu */
+__global__ void k_sgs_targets(const double* __restrict__ s8, int nc, double tau0, float* __restrict__ X,
+                              float* __restrict__ T) {
+    const size_t cn = size_t(nc) * nc * nc;
+    const size_t o = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (o >= cn) return;
+    const int x = int(o % nc), y = int((o / nc) % nc), z = int(o / (size_t(nc) * nc));
+    double ts = 0, ss = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                const size_t i = (size_t((z + dz + nc) % nc) * nc + (y + dy + nc) % nc) * nc + (x + dx + nc) % nc;
+                ts += s8[6 * cn + i];
+                ss += s8[7 * cn + i];
+            }
     double nu = ss > 1e-30 ? -ts / (2 * ss) : 0;
     if (nu < 0) nu = 0;
     double p[6], xf[sgs::NIN];
-    for (int k = 0; k < 6; ++k) p[k] = (tau0 + 3 * nu) * S[k];
+    for (int k = 0; k < 6; ++k) p[k] = (tau0 + 3 * nu) * s8[k * cn + o];
     sgs::features<double>(p, tau0, xf);
     for (int k = 0; k < sgs::NIN; ++k) X[o * sgs::NIN + k] = float(xf[k]);
     T[o] = float(nu);
@@ -367,10 +390,12 @@ cudaError_t launch_d2f(const double* a, float* b, size_t n, cudaStream_t s) {
     ens::k_d2f<<<unsigned((n + 255) / 256), 256, 0, s>>>(a, b, n);
     return cudaGetLastError();
 }
-cudaError_t launch_sgs_targets(const double* ubar, const double* uu, int nc, double tau0, float* X, float* T,
-                               cudaStream_t s) {
+cudaError_t launch_sgs_targets(const double* ubar, const double* uu, int nc, double tau0, double* s8, float* X,
+                               float* T, cudaStream_t s) {
     const size_t cn = size_t(nc) * nc * nc;
-    ens::k_sgs_targets<<<unsigned((cn + 255) / 256), 256, 0, s>>>(ubar, uu, nc, tau0, X, T);
+    const unsigned nb = unsigned((cn + 255) / 256);
+    ens::k_sgs_contract<<<nb, 256, 0, s>>>(ubar, uu, nc, s8);
+    ens::k_sgs_targets<<<nb, 256, 0, s>>>(s8, nc, tau0, X, T);
     return cudaGetLastError();
 }
 

@@ -49,7 +49,9 @@ cudaError_t launch_ens_velocity(const ens::Table& T, const float* f, float* u, c
 cudaError_t launch_ens_energy(const ens::Table& T, const float* u, double* out, cudaStream_t s);
 cudaError_t launch_box_filter(const float* u, int n, double* ubar, double* uu, cudaStream_t s);
 cudaError_t launch_d2f(const double* a, float* b, size_t n, cudaStream_t s);
-cudaError_t launch_sgs_targets(const double* ubar, const double* uu, int nc, double tau0, float* X, float* T,
-                               cudaStream_t s);
+/* two passes: per-cell strain and contractions into s8 (8 * nc^3 doubles),
+ * then the 3x3x3-averaged least-squares eddy viscosity and the features */
+cudaError_t launch_sgs_targets(const double* ubar, const double* uu, int nc, double tau0, double* s8, float* X,
+                               float* T, cudaStream_t s);
 
 }  // namespace lbm

@@ -40,6 +40,7 @@ struct lbm_ensemble {
     size_t nu = 0;
     double* ubar = nullptr; /* filter scratch, sized for the largest member */
     double* uu = nullptr;
+    double* s8 = nullptr;
     ens::Mode* modes = nullptr;
     unsigned char* blob = nullptr;
     int* err = nullptr;
@@ -249,6 +250,7 @@ int lbm_ensemble_create(int count, const int* sizes, const float* tau0, int sgs,
     if (cudaMalloc(&e->u, e->nu * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&e->ubar, maxc * 3 * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&e->uu, maxc * 6 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&e->s8, maxc * 8 * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&e->err, sizeof(int)) != cudaSuccess || cudaMalloc(&e->energy, ens::MAXM * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&e->blob, sgs::BLOB_BYTES) != cudaSuccess)
         return bail(set_error(LBM_ERR_CUDA, "ensemble: buffers", cudaGetLastError()));
@@ -273,6 +275,7 @@ int lbm_ensemble_destroy(lbm_ensemble* e) {
     cudaFree(e->u);
     cudaFree(e->ubar);
     cudaFree(e->uu);
+    cudaFree(e->s8);
     cudaFree(e->modes);
     cudaFree(e->blob);
     cudaFree(e->err);
@@ -490,7 +493,8 @@ int lbm_ensemble_samples(lbm_ensemble* e, float tau0_coarse, float* d_X, float* 
         ENS_TRY(launch_box_filter(e->u + M.uoff, M.n, e->ubar, e->uu, e->stream), "filter");
         /* acoustic scaling: half the lattice viscosity on the 2x coarser grid */
         const double t0 = tau0_coarse > 0.5f ? double(tau0_coarse) : 0.5 + (double(M.tau0) - 0.5) / 2;
-        ENS_TRY(launch_sgs_targets(e->ubar, e->uu, nc, t0, d_X + pos * sgs::NIN, d_T + pos, e->stream), "targets");
+        ENS_TRY(launch_sgs_targets(e->ubar, e->uu, nc, t0, e->s8, d_X + pos * sgs::NIN, d_T + pos, e->stream),
+                "targets");
         pos += cn;
     }
     *n = pos;

@@ -10,7 +10,8 @@
  *   (softplus(y) - nu_target / 1e-4)^2;
  *   features of p_ij = -3/2 Pi_neq_ij / rho and tau0 (x0..x15, x15 = 1);
  *   box filter of a fine velocity field onto the coarse grid and the
- *   least-squares eddy viscosity of the filtered subgrid stress.
+ *   least-squares eddy viscosity of the filtered subgrid stress, its
+ *   contractions averaged over 3x3x3 coarse cells.
  */
 #include <cmath>
 #include <cstdint>
@@ -183,9 +184,10 @@ void orc_box_filter(const float* u, int fx, int fy, int fz, double* ubar, double
             }
 }
 
-/* per coarse cell: filtered strain (central differences, periodic), the
- * least-squares eddy viscosity nu = max(0, -tau^d:S / (2 S:S)) of the
- * subgrid stress tau = uu - ubar ubar, the features of p = (tau0 + 3 nu) S
+/* per coarse cell: filtered strain S (central differences, periodic), the
+ * contractions tau^d:S and S:S of the subgrid stress tau = uu - ubar ubar,
+ * their 3x3x3 box averages (periodic), the least-squares eddy viscosity
+ * nu = max(0, -<tau^d:S> / (2 <S:S>)), the features of p = (tau0 + 3 nu) S
  * (X[n][16]) and the target nu (T[n]) */
 void orc_sgs_targets(const double* ubar, const double* uu, int cx, int cy, int cz, double tau0, float* X, float* T) {
     const size_t cn = size_t(cx) * cy * cz;
@@ -193,6 +195,7 @@ void orc_sgs_targets(const double* ubar, const double* uu, int cx, int cy, int c
         x = (x + cx) % cx, y = (y + cy) % cy, z = (z + cz) % cz;
         return ubar[k * cn + (size_t(z) * cy + y) * cx + x];
     };
+    std::vector<double> S6(6 * cn), TS(cn), SS(cn);
     for (int z = 0; z < cz; ++z)
         for (int y = 0; y < cy; ++y)
             for (int x = 0; x < cx; ++x) {
@@ -216,10 +219,27 @@ void orc_sgs_targets(const double* ubar, const double* uu, int cx, int cy, int c
                     ts += w * tau[k] * S[k];
                     ss += w * S[k] * S[k];
                 }
+                for (int k = 0; k < 6; ++k) S6[k * cn + o] = S[k];
+                TS[o] = ts;
+                SS[o] = ss;
+            }
+    for (int z = 0; z < cz; ++z)
+        for (int y = 0; y < cy; ++y)
+            for (int x = 0; x < cx; ++x) {
+                double ts = 0, ss = 0;
+                for (int dz = -1; dz <= 1; ++dz)
+                    for (int dy = -1; dy <= 1; ++dy)
+                        for (int dx = -1; dx <= 1; ++dx) {
+                            const size_t i = (size_t((z + dz + cz) % cz) * cy + (y + dy + cy) % cy) * cx +
+                                             (x + dx + cx) % cx;
+                            ts += TS[i];
+                            ss += SS[i];
+                        }
                 double nu = ss > 1e-30 ? -ts / (2 * ss) : 0;
                 if (nu < 0) nu = 0;
+                const size_t o = (size_t(z) * cy + y) * cx + x;
                 double p[6], x16[16];
-                for (int k = 0; k < 6; ++k) p[k] = (tau0 + 3 * nu) * S[k];
+                for (int k = 0; k < 6; ++k) p[k] = (tau0 + 3 * nu) * S6[k * cn + o];
                 orc_sgs_features(p, tau0, x16);
                 for (int k = 0; k < 16; ++k) X[o * 16 + k] = float(x16[k]);
                 T[o] = float(nu);
