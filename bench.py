@@ -43,12 +43,18 @@ WORKLOAD = ("D3Q19 MRT+Smagorinsky channel 512x128x128, square cylinder side 16 
             "drag/lift every step")
 
 
-def inputs_text(precision: str, tmax: int, bounceback: str = "halfway") -> str:
+SGS_WEIGHTS = ROOT / "lbm_multigpu_gb300" / "data" / "sgs_mlp.bin"
+# MLP 15(+1)->64->64->1 per cell: 2 (16*64 + 64*64 + 64) multiply-adds
+SGS_FLOP_PER_CELL = 2 * (16 * 64 + 64 * 64 + 64)
+
+
+def inputs_text(precision: str, tmax: int, bounceback: str = "halfway", sgs: str = "smagorinsky") -> str:
     import lbm_multigpu_gb300 as lbm
 
+    ext = dict(sgs="mlp", sgs_weights=str(SGS_WEIGHTS)) if sgs == "mlp" else {}
     return lbm.make_inputs(NX, NY, NZ, obst1=(128.5, 63.5, 0.0), r1=8.0, re=120.0, umax=0.05, tmax=tmax, les=1,
                            cs=0.01, model="MRT", geometry="channel_square", precision=precision, inlet_noise=0.01,
-                           seed=12345, bounceback=bounceback)
+                           seed=12345, bounceback=bounceback, **ext)
 
 
 def peaks() -> dict:
@@ -118,11 +124,11 @@ def dist_setup():
 
 
 def time_precision(precision: str, steps: int, warmup: int, world: int, dist, with_clocks: bool, gpu: int,
-                   bounceback: str = "halfway"):
+                   bounceback: str = "halfway", sgs: str = "smagorinsky"):
     """resident-in-HBM run of `steps` steps after `warmup`; returns (ms, clocks)"""
     import lbm_multigpu_gb300 as lbm
 
-    s = lbm.Solver(inputs_text(precision, warmup + steps + 10, bounceback))
+    s = lbm.Solver(inputs_text(precision, warmup + steps + 10, bounceback, sgs))
     s.step(warmup)
     s.synchronize()
     if dist:
@@ -303,7 +309,11 @@ def main():
     for prec in (("fp16", "bf16") if args.precision == "all" else ()):
         ms, kms, _, _, _ = time_precision(prec, args.steps, args.warmup, world, dist, False, local)
         res[prec] = (ms, kms)
-    full = None
+    full = sgsr = None
+    if args.precision == "all" and SGS_WEIGHTS.exists():
+        # the learned closure in place of Smagorinsky (tensor-core MLP per tile)
+        mss, kmss, _, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, sgs="mlp")
+        sgsr = (mss, kmss)
     if args.precision == "all":
         # the reference's own wall treatment (full-way, on-node bounce-back)
         msf, kmsf, _, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, "fullway")
@@ -364,6 +374,14 @@ def main():
         gbs = CELLS * BYTES_PER_CELL["fp32"] / (full[1] * 1e-3) / 1e9
         line["fp32_fullway_bounceback"] = dict(value=v, ms_per_step=worst(full[0]) / args.steps, kernel_ms=full[1],
                                                kernel_gbs=gbs, frac=gbs / pk["hbm_gbs"])
+    if sgsr:
+        v = world * CELLS * args.steps / (worst(sgsr[0]) * 1e-3) / 1e6
+        gbs = CELLS * BYTES_PER_CELL["fp32"] / (sgsr[1] * 1e-3) / 1e9
+        line["learned_sgs"] = dict(value=v, ratio_vs_smagorinsky=v / mlups, cost=1 - v / mlups,
+                                   ms_per_step=worst(sgsr[0]) / args.steps, kernel_ms=sgsr[1], kernel_gbs=gbs,
+                                   frac=gbs / pk["hbm_gbs"],
+                                   tensor_tflops=CELLS * SGS_FLOP_PER_CELL / (sgsr[1] * 1e-3) / 1e12,
+                                   kernel="k_stream_collide_mlp<fp32>", weights=str(SGS_WEIGHTS.relative_to(ROOT)))
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line))

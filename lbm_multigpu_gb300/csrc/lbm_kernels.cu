@@ -17,6 +17,8 @@
  * Forces are reduced per block in FP64 (warp shuffles, then shared memory)
  * into a scratch array and summed by a second, deterministic kernel.
  */
+#include <algorithm>
+
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -194,8 +196,9 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
  * for the whole 32 x 8 tile at once.  Persistent blocks walk the tiles so
  * that each block stages the weights and allocates its TMEM once per launch.
  * MRT collision (LR7:583-711) at tau_eff = tau0 + 3 nu_t; FP32 arithmetic. */
+constexpr int MLP_BY = 4; /* tile 32 x 4: one M = 128 MMA per layer */
 template <class S, bool HALFWAY>
-__global__ void __launch_bounds__(SC_BX* SC_BY, 2) k_stream_collide_mlp(const Level L, const StepParams p,
+__global__ void __launch_bounds__(SC_BX* MLP_BY, 6) k_stream_collide_mlp(const Level L, const StepParams p,
                                                                       const S* __restrict__ fA, S* __restrict__ fB,
                                                                       const uint8_t* __restrict__ mask,
                                                                       float* __restrict__ stats,
@@ -203,7 +206,7 @@ __global__ void __launch_bounds__(SC_BX* SC_BY, 2) k_stream_collide_mlp(const Le
                                                                       const unsigned char* __restrict__ blob,
                                                                       int* __restrict__ err) {
     using F = Fmt<S>;
-    constexpr int ROWS = SC_BX * SC_BY;
+    constexpr int ROWS = SC_BX * MLP_BY;
     extern __shared__ unsigned char dsm[];
     sgs::InferSmem<ROWS>& sm = *reinterpret_cast<sgs::InferSmem<ROWS>*>(
         (reinterpret_cast<uintptr_t>(dsm) + 1023) & ~uintptr_t(1023));
@@ -211,13 +214,26 @@ __global__ void __launch_bounds__(SC_BX* SC_BY, 2) k_stream_collide_mlp(const Le
     sgs::infer_setup<ROWS>(sm, blob);
     const unsigned qs = unsigned(L.qstride);
     const unsigned plane = unsigned(L.plane), pitch = unsigned(L.pitch);
-    const int tiles_x = L.pitch / SC_BX, tiles_y = (L.ny + SC_BY - 1) / SC_BY;
+    const int tiles_x = L.pitch / SC_BX, tiles_y = (L.ny + MLP_BY - 1) / MLP_BY;
     const int ntiles = tiles_x * tiles_y * L.nz;
-    const float tau0 = 1.f / p.omega;
+    const float tau0 = 1.f / p.omega, inv_t0 = p.omega;
     for (int g = blockIdx.x; g < ntiles; g += gridDim.x) {
         const int z = g / (tiles_x * tiles_y), r = g - z * tiles_x * tiles_y;
-        const int x = (r % tiles_x) * SC_BX + int(threadIdx.x), y = (r / tiles_x) * SC_BY + int(threadIdx.y);
+        const int x = (r % tiles_x) * SC_BX + int(threadIdx.x), y = (r / tiles_x) * MLP_BY + int(threadIdx.y);
         const bool live = x < L.nx && y < L.ny;
+        {
+            /* the next tile's population rows toward L2 while this one runs
+             * its MLP: one prefetch per (population, row), by lane q */
+            const int gn = g + int(gridDim.x);
+            if (gn < ntiles && threadIdx.x < 19) {
+                const int zn = gn / (tiles_x * tiles_y), rn = gn - zn * tiles_x * tiles_y;
+                const int yn = (rn / tiles_x) * MLP_BY + int(threadIdx.y), xn = (rn % tiles_x) * SC_BX;
+                if (yn < L.ny) {
+                    const S* row = fA + threadIdx.x * qs + unsigned(zn) * plane + unsigned(yn) * pitch + xn;
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(row));
+                }
+            }
+        }
         float f[19];
         int type = FLUID;
         unsigned c = 0;
@@ -266,7 +282,7 @@ __global__ void __launch_bounds__(SC_BX* SC_BY, 2) k_stream_collide_mlp(const Le
         const float sc = -1.5f / rho;
 #pragma unroll
         for (int k = 0; k < 6; ++k) p6[k] *= sc;
-        sgs::features<float>(p6, tau0, xf);
+        sgs::features<float>(p6, tau0, inv_t0, xf);
         const float nu = sgs::infer_nu<ROWS>(sm, xf, err);
         if (!live) continue;
         if (type == WALL || type == BODY) {
@@ -759,25 +775,38 @@ cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const voi
 template <class S, bool HW> static cudaError_t sc_mlp_t(const Level& L, const StepParams& p, const void* fA, void* fB,
                                                         const uint8_t* mask, float* stats, const uint32_t* links,
                                                         const void* blob, int* err, cudaStream_t s) {
-    const size_t smem = sgs::infer_dyn_smem<SC_BX * SC_BY>();
+    const size_t smem = sgs::infer_dyn_smem<SC_BX * MLP_BY>();
     static cudaError_t attr = cudaErrorNotReady;
     static int grid = 0;
     if (attr == cudaErrorNotReady) {
         attr = cudaFuncSetAttribute(k_stream_collide_mlp<S, HW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     int(smem));
-        int nb = 0, dev = 0, sms = 0;
+        /* all of the unified L1 / shared array as shared memory, so that the
+         * register limit (2 blocks of 256 threads at 128 registers) decides */
         if (attr == cudaSuccess)
-            attr = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stream_collide_mlp<S, HW>, SC_BX * SC_BY, smem);
+            attr = cudaFuncSetAttribute(k_stream_collide_mlp<S, HW>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                        100);
+        /* resident blocks per SM from the kernel's own limits: registers,
+         * shared memory, threads, and TMEM (128 columns of 512 per block) */
+        cudaFuncAttributes fa{};
+        int dev = 0, sms = 0, regs_sm = 0, smem_sm = 0;
+        if (attr == cudaSuccess) attr = cudaFuncGetAttributes(&fa, k_stream_collide_mlp<S, HW>);
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        /* the shared-memory request already keeps TMEM (128 columns per
-         * block, 512 per SM) from being over-subscribed */
+        cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        const int threads = SC_BX * MLP_BY;
+        const int regs_block = ((fa.numRegs > 0 ? fa.numRegs : 255) * 32 + 255) / 256 * 256 * (threads / 32);
+        int nb = regs_sm / (regs_block > 0 ? regs_block : 1);
+        nb = std::min(nb, int(smem_sm / (smem + fa.sharedSizeBytes + 1024)));
+        nb = std::min(nb, 2048 / threads);
+        nb = std::min(nb, 512 / sgs::tmem_cols<SC_BX * MLP_BY>());
         nb = nb < 1 ? 1 : nb;
         grid = (sms > 0 ? sms : 152) * nb;
     }
     if (attr != cudaSuccess) return attr;
-    const int ntiles = (L.pitch / SC_BX) * ((L.ny + SC_BY - 1) / SC_BY) * L.nz;
-    k_stream_collide_mlp<S, HW><<<grid < ntiles ? grid : ntiles, dim3(SC_BX, SC_BY), smem, s>>>(
+    const int ntiles = (L.pitch / SC_BX) * ((L.ny + MLP_BY - 1) / MLP_BY) * L.nz;
+    k_stream_collide_mlp<S, HW><<<grid < ntiles ? grid : ntiles, dim3(SC_BX, MLP_BY), smem, s>>>(
         L, p, (const S*)fA, (S*)fB, mask, stats, links, (const unsigned char*)blob, err);
     return cudaGetLastError();
 }

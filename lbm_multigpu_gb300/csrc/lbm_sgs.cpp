@@ -64,22 +64,19 @@ uint16_t bf16_rne(float f) {
 namespace lbm {
 void mlp_make_blob(const float* P, unsigned char* blob) {
     std::memset(blob, 0, sgs::BLOB_BYTES);
+    auto put = [&](unsigned char* base, uint32_t off, float v) {
+        const uint16_t b = bf16_rne(v);
+        std::memcpy(base + off, &b, 2);
+    };
     for (int j = 0; j < sgs::NH; ++j)
-        for (int k = 0; k < sgs::NIN; ++k) {
-            const uint16_t b = bf16_rne(P[sgs::OFF_W1 + j * sgs::NIN + k]);
-            std::memcpy(blob + tc::core_off(j, k, sgs::W1_LBO, sgs::W1_SBO), &b, 2);
-        }
+        for (int k = 0; k < sgs::NIN; ++k)
+            put(blob, tc::core_off(j, k, sgs::W1_LBO, sgs::W1_SBO), P[sgs::OFF_W1 + j * sgs::NIN + k]);
     for (int j = 0; j < sgs::NH; ++j)
-        for (int k = 0; k < sgs::NH; ++k) {
-            const uint16_t b = bf16_rne(P[sgs::OFF_W2 + j * sgs::NH + k]);
-            std::memcpy(blob + sgs::W1_BYTES + tc::core_off(j, k, sgs::W2_LBO, sgs::W2_SBO), &b, 2);
-        }
-    float* fp = reinterpret_cast<float*>(blob + sgs::W1_BYTES + sgs::W2_BYTES);
-    for (int j = 0; j < sgs::NH; ++j) {
-        fp[j] = P[sgs::OFF_B2 + j];
-        fp[sgs::NH + j] = P[sgs::OFF_W3 + j];
-    }
-    fp[2 * sgs::NH] = P[sgs::OFF_B3];
+        for (int k = 0; k < sgs::NH; ++k)
+            put(blob + sgs::W1_BYTES, tc::core_off(j, k, sgs::W2_LBO, sgs::W2_SBO), P[sgs::OFF_W2 + j * sgs::NH + k]);
+    std::memcpy(blob + sgs::BLOB_B2, &P[sgs::OFF_B2], sgs::NH * 4);
+    std::memcpy(blob + sgs::BLOB_B2 + sgs::NH * 4, &P[sgs::OFF_B3], 4);
+    std::memcpy(blob + sgs::BLOB_B2 + sgs::NH * 4 + 16, &P[sgs::OFF_W3], sgs::NH * 4);
 }
 }  // namespace lbm
 

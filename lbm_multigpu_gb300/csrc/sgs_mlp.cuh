@@ -29,14 +29,14 @@ constexpr int OFF_W1 = 0, OFF_W2 = OFF_W1 + NH * NIN, OFF_B2 = OFF_W2 + NH * NH,
 constexpr float P_REF = 0.01f, S_REF = 0.01f, NU_SCALE = 1e-4f;
 constexpr float GELU_A = 0.7978845608f, GELU_B = 0.044715f;
 
-/* features of one node from p_ij (xx, yy, zz, xy, xz, yz) and tau0 */
-template <class T> __host__ __device__ inline void features(const T p[6], T tau0, T x[NIN]) {
+/* features of one node from p_ij (xx, yy, zz, xy, xz, yz), tau0 and
+ * inv_t0 = 1 / tau0 (a kernel computes it once) */
+template <class T> __host__ __device__ inline void features(const T p[6], T tau0, T inv_t0, T x[NIN]) {
     const T pp = p[0] * p[0] + p[1] * p[1] + p[2] * p[2] + T(2) * (p[3] * p[3] + p[4] * p[4] + p[5] * p[5]);
     /* tr(p^3) of the symmetric tensor */
     const T xx = p[0], yy = p[1], zz = p[2], xy = p[3], xz = p[4], yz = p[5];
     const T tr3 = xx * xx * xx + yy * yy * yy + zz * zz * zz + T(3) * xx * (xy * xy + xz * xz) +
                   T(3) * yy * (xy * xy + yz * yz) + T(3) * zz * (xz * xz + yz * yz) + T(6) * xy * xz * yz;
-    const T inv_t0 = T(1) / tau0;
     for (int i = 0; i < 6; ++i) {
         x[i] = p[i] * T(1.0 / P_REF);
         x[6 + i] = p[i] * inv_t0 * T(1.0 / S_REF);
@@ -45,6 +45,10 @@ template <class T> __host__ __device__ inline void features(const T p[6], T tau0
     x[13] = pp > T(1e-30) ? tr3 / (pp * sqrt(pp)) : T(0);
     x[14] = (tau0 - T(0.5)) * T(100);
     x[15] = T(1);
+}
+
+template <class T> __host__ __device__ inline void features(const T p[6], T tau0, T x[NIN]) {
+    features<T>(p, tau0, T(1) / tau0, x);
 }
 
 }  // namespace sgs
