@@ -267,6 +267,118 @@ def reference_arm(args, world, rank):
     print(json.dumps(line))
 
 
+def workload_c3(steps: int, warmup: int) -> dict:
+    """two-level refinement: coarse 256x128x64 MRT-LES channel, circular
+    cylinder of diameter 12 coarse cells, ratio-2 patch spanning the periodic
+    z extent (96x64x128 fine, the reference's full-z layout), 2 fine steps per
+    coarse step; MLUPS by the reference's count (LR7:2956-2961): coarse nodes
+    + fine nodes x LRLEVEL per coarse step"""
+    import lbm_multigpu_gb300 as lbm
+
+    text = lbm.make_inputs(256, 128, 64, obst1=(64.5, 63.5, 0.0), r1=6.0, re=90.0, umax=0.05,
+                           tmax=steps + warmup + 10, les=1, cs=0.01, geometry="channel_circle", refinement=1,
+                           lr_dims=(96, 64, 128), lr_factor=0.5, lr_origin=(48.25, 47.25, -0.75), inlet_noise=0.01)
+    with lbm.Solver(text) as s:
+        s.step(warmup)
+        s.synchronize()
+        n0 = s.launch_count()
+        ms = s.step_timed(steps)
+        launches = s.launch_count() - n0
+        kc = s.time_stream_collide(20, 0)
+        kf = s.time_stream_collide(20, 1)
+        audit = s.audit(0)
+    nodes = 256 * 128 * 64 + 96 * 64 * 128 * 2
+    return dict(workload="C3 two-level refinement: coarse 256x128x64 + fine 96x64x128 (ratio 2, full z), "
+                         "MRT-LES, circular cylinder D=12, tau0=0.52 (RE=90), CS=0.01, 1% inlet noise",
+                metric="MLUPS (coarse + 2 x fine nodes per coarse step)", value=nodes * steps / (ms * 1e3),
+                unit="MLUPS", steps=steps, warmup=warmup, ms_per_coarse_step=ms / steps,
+                kernel_ms=dict(coarse_stream_collide=kc, fine_stream_collide=kf,
+                               interface_and_force=ms / steps - kc - 2 * kf),
+                gpu_launches=launches, audit_mass=float(audit[0]))
+
+
+def workload_c4(steps: int) -> dict:
+    """precision: the channel geometry scaled to 768x256x256 (square cylinder
+    side 24 at x=192, tau0=0.52) with populations stored as FP16 / BF16
+    (offset f - feq(1, u_in)), FP32 collide, beside FP32 and an FP64-storage
+    twin of the same kernels: max / RMS density and velocity error of each
+    against FP64, and MLUPS"""
+    import numpy as np
+
+    import lbm_multigpu_gb300 as lbm
+
+    nx, ny, nz = 768, 256, 256
+    out, ref, mask = {}, None, None
+    for prec in ("fp64", "fp32", "fp16", "bf16"):
+        text = lbm.make_inputs(nx, ny, nz, obst1=(192.5, 127.5, 0.0), r1=12.0, re=180.0, umax=0.05,
+                               tmax=steps + 10, les=1, cs=0.01, geometry="channel_square", precision=prec,
+                               bounceback="halfway")
+        with lbm.Solver(text) as s:
+            ms = s.step_timed(steps)
+            rho, u, v, w = s.fields()
+            if mask is None:
+                mask = s.mask()
+        fl = (mask != 1) & (mask != 2)
+        r = dict(mlups=nx * ny * nz * steps / (ms * 1e3), ms_per_step=ms / steps)
+        vel = np.stack([u[fl], v[fl], w[fl]]).astype(np.float64)
+        rh = rho[fl].astype(np.float64)
+        if ref is None:
+            ref = (rh, vel)
+        else:
+            dr, dv = rh - ref[0], np.linalg.norm(vel - ref[1], axis=0)
+            r.update(rho_err_max=float(np.abs(dr).max()), rho_err_rms=float(np.sqrt(np.mean(dr ** 2))),
+                     u_err_max=float(dv.max()), u_err_rms=float(np.sqrt(np.mean(dv ** 2))),
+                     u_rel_l2=float(np.linalg.norm(vel - ref[1]) / np.linalg.norm(ref[1])))
+        out[prec] = r
+    for prec in ("fp16", "bf16"):
+        out[prec]["mlups_vs_fp32"] = out[prec]["mlups"] / out["fp32"]["mlups"]
+    return dict(workload="C4 precision: 768x256x256 channel, square cylinder side 24, MRT-LES, half-way "
+                         "bounce-back; errors over fluid nodes against the FP64-storage twin",
+                steps=steps, results=out)
+
+
+def workload_sgs_channel(steps: int, warmup: int) -> dict:
+    """the learned closure deployed in the channel: MLUPS of the tensor-core
+    MLP stream-collide against Smagorinsky on the same 512x128x128 case"""
+    import lbm_multigpu_gb300 as lbm
+
+    res = {}
+    for sgs in ("smagorinsky", "mlp"):
+        with lbm.Solver(inputs_text("fp32", steps + warmup + 10, sgs=sgs)) as s:
+            s.step(warmup)
+            ms = s.step_timed(steps)
+            k = s.time_stream_collide(20)
+        res[sgs] = dict(mlups=CELLS * steps / (ms * 1e3), ms_per_step=ms / steps, kernel_ms=k)
+    res["cost"] = 1 - res["mlp"]["mlups"] / res["smagorinsky"]["mlups"]
+    res["tensor_tflops"] = CELLS * SGS_FLOP_PER_CELL / (res["mlp"]["kernel_ms"] * 1e-3) / 1e12
+    return dict(workload="C5 deployment: " + WORKLOAD.replace("MRT+Smagorinsky", "MRT + learned closure"),
+                steps=steps, results=res)
+
+
+def workload_ensemble(steps: int, warmup: int) -> dict:
+    """C5 batching: the 16-member decaying-turbulence ensemble of uneven box
+    sizes (64^3..160^3, seeded) advanced by one persistent launch per step
+    from a CUDA graph, tile height and grid from the autotuner; MRT, periodic;
+    MLUPS over all members and the fraction of the HBM roofline (152 B per
+    node update)"""
+    import lbm_multigpu_gb300 as lbm
+    from lbm_multigpu_gb300 import sgs_pipeline as sp
+
+    sizes = sp.ensemble_sizes(2024, 16)
+    with lbm.Ensemble(sizes, sp.TAU_F, sgs="none") as e:
+        e.init_turbulence(2024, kmax_div=8, per_shell=24)
+        ty, grid, tuned = e.autotune()
+        e.step(warmup)
+        ms = e.step_timed(steps)
+        cells = e.info()["cells"]
+    gbs = cells * 152 / (ms / steps * 1e-3) / 1e9
+    pk = peaks()
+    return dict(workload="C5 ensemble: 16 periodic MRT boxes, sides " + ",".join(map(str, sizes)),
+                metric="MLUPS", value=cells * steps / (ms * 1e3), unit="MLUPS", steps=steps, cells=cells,
+                ms_per_step=ms / steps, tile=f"32x{ty}", grid=grid, autotune_ms_per_step=tuned,
+                roofline=dict(bound="hbm", achieved=gbs, peak=pk["hbm_gbs"], unit="GB/s", frac=gbs / pk["hbm_gbs"]))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -277,6 +389,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--precision", default="all", choices=["all", "fp32", "fp16", "bf16"],
                     help="storage precisions to time (all: fp32 reference point, then fp16 and bf16)")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "sgs", "ensemble"],
+                    help="c2: the channel headline line (default); c3: two-level refinement; c4: storage "
+                         "precision against FP64 at 768x256x256; sgs: the learned closure against Smagorinsky; "
+                         "ensemble: the 16-member periodic-box ensemble")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
@@ -298,6 +414,19 @@ def main():
 
     if rank == 0 or not (ROOT / "lbm_multigpu_gb300" / "_build" / "liblbm_gb300.so").exists():
         __graft_entry__.build()
+    if args.workload != "c2":
+        if rank == 0:
+            steps = min(args.steps, 2000)
+            if args.workload == "c3":
+                line = workload_c3(steps, args.warmup)
+            elif args.workload == "c4":
+                line = workload_c4(steps)
+            elif args.workload == "ensemble":
+                line = workload_ensemble(steps, args.warmup)
+            else:
+                line = workload_sgs_channel(steps, args.warmup)
+            print(json.dumps(line))
+        return
     if dist:
         dist.barrier()
     import numpy as np
