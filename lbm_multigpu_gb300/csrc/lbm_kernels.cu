@@ -61,19 +61,15 @@ template <> struct Fmt<__nv_bfloat16> {
  * the node types present, so a channel kernel carries no lid code (whose
  * 19-entry temporaries would otherwise set every variant's register count) */
 constexpr int FEAT_HALFWAY = 1, FEAT_LID = 2, FEAT_CLAMP = 4;
+/* the node update of one node (x, y, z) inside the level; shared by the
+ * one-node-per-thread kernel and the slow path of the paired kernel */
 template <class S, int FEAT>
-__global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, const StepParams p,
-                                                                  const S* __restrict__ fA, S* __restrict__ fB,
-                                                                  const uint8_t* __restrict__ mask,
-                                                                  float* __restrict__ stats,
-                                                                  float* __restrict__ mom_export,
-                                                                  const uint32_t* __restrict__ links) {
+__device__ __forceinline__ void sc_node(const Level& L, const StepParams& p, const S* __restrict__ fA,
+                                        S* __restrict__ fB, const uint8_t* __restrict__ mask,
+                                        float* __restrict__ stats, float* __restrict__ mom_export,
+                                        const uint32_t* __restrict__ links, const int x, const int y, const int z) {
     using F = Fmt<S>;
     using T = typename F::T;
-    const int x = blockIdx.x * SC_BX + threadIdx.x;
-    const int y = blockIdx.y * SC_BY + threadIdx.y;
-    const int z = blockIdx.z;
-    if (x >= L.nx || y >= L.ny) return;
     /* 32-bit element offsets: a level holds fewer than 2^31 elements per
      * buffer (checked at allocation) */
     const unsigned qs = unsigned(L.qstride);
@@ -186,6 +182,20 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
             for (int i = 0; i < 9; ++i) mom_export[i * ne + ce] = mom[i];
         }
     }
+}
+
+template <class S, int FEAT>
+__global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, const StepParams p,
+                                                                  const S* __restrict__ fA, S* __restrict__ fB,
+                                                                  const uint8_t* __restrict__ mask,
+                                                                  float* __restrict__ stats,
+                                                                  float* __restrict__ mom_export,
+                                                                  const uint32_t* __restrict__ links) {
+    const int x = blockIdx.x * SC_BX + threadIdx.x;
+    const int y = blockIdx.y * SC_BY + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= L.nx || y >= L.ny) return;
+    sc_node<S, FEAT>(L, p, fA, fB, mask, stats, mom_export, links, x, y, z);
 }
 
 /* The stream-collide step with the learned subgrid closure in place of the
@@ -753,6 +763,7 @@ __global__ void k_interp_fc(const RefineParams r, const Level C, const Level F, 
 cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const void* fA, void* fB, const uint8_t* mask,
                                   float* stats, float* mom_export, cudaStream_t s, const uint32_t* links) {
     if (p.halfway && !links) return cudaErrorInvalidValue;
+
     const dim3 block(SC_BX, SC_BY), grid = sc_grid(L);
     const int feat = (p.halfway ? FEAT_HALFWAY : 0) | (p.has_lid ? FEAT_LID : 0) | (p.pull_clamp ? FEAT_CLAMP : 0);
 #define LBM_SC(FT) \
