@@ -271,6 +271,28 @@ int lbm_ensemble_set_populations(lbm_ensemble* e, int member, const float* f);
  * <= 1/2 takes each member's coarse relaxation time by acoustic scaling */
 int lbm_ensemble_samples(lbm_ensemble* e, float tau0_coarse, float* d_X, float* d_T, long long cap, long long* n);
 
+/* ------------------------------------------------------------------------
+ * Post-processing of the outputs (host only, no device)
+ * ------------------------------------------------------------------------ */
+/* ForceCalcs (bgk_channel1/Re3000_Cyl2/ForceCalcs.cpp): mean and RMS of each
+ * component of a force history fxyz[3 n] (the values of a .force file) over
+ * the lines t_start .. t_end - 1, with that program's FP32 running updates */
+int lbm_force_stats(const float* fxyz, int n, int t_start, int t_end, float* mean3, float* rms3);
+/* drag coefficient 2 <Fx> / (rho u^2 d lz), RMS lift coefficient, and the
+ * Strouhal number f d / u of the lift's dominant frequency, over lines
+ * t_start .. n - 1 of raw forces (not normalised); cd, cl_rms, st may be NULL */
+int lbm_force_coefficients(const double* fxyz, int n, int t_start, double u, double d, double lz, double rho,
+                           double* cd, double* cl_rms, double* st);
+/* VelProf (bgk_channel1/Re3000/VelProf.cpp): wall units of a wall-normal
+ * line of n nodes: y+ = (i - 1/2) u_tau / nu, v+ = v / u_tau, rms+ =
+ * sqrt(fluctuation) / u_tau; any output may be NULL */
+int lbm_wall_profile(const float* v_mean, const float* u_fluc, const float* v_fluc, const float* w_fluc, int n,
+                     float u_tau, float nu, float* yplus, float* vplus, float* urms, float* vrms, float* wrms);
+/* profiles along y at x of a level's statistics (lbm_get_stats layout
+ * float[4][nz][ny][nx]: velAv u, v, velFluc u, v), averaged over z:
+ * prof4[4][ny] */
+int lbm_stats_profiles(const float* stats4, int nx, int ny, int nz, int x, float* prof4);
+
 #ifdef __cplusplus
 }
 #endif

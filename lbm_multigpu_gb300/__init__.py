@@ -67,6 +67,11 @@ SIGNATURES = [
     ("lbm_tc_selftest", _I, [_I, _P, _P, _P]),
     ("lbm_mlp_predict_tc", _I, [_P, _P, _I, _P, _P]),
     ("lbm_set_sgs_mlp", _I, [_P, _P, _I]),
+    ("lbm_force_stats", _I, [_P, _I, _I, _I, _P, _P]),
+    ("lbm_force_coefficients", _I, [_P, _I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                    _P, _P, _P]),
+    ("lbm_wall_profile", _I, [_P, _P, _P, _P, _I, _F, _F, _P, _P, _P, _P, _P]),
+    ("lbm_stats_profiles", _I, [_P, _I, _I, _I, _I, _P]),
     ("lbm_ensemble_create", _I, [_I, _P, _P, _I, _F, _P]),
     ("lbm_ensemble_destroy", _I, [_P]),
     ("lbm_ensemble_init_turbulence", _I, [_P, ctypes.c_uint32, _F, _I, _I]),
@@ -490,3 +495,42 @@ class Ensemble:
         c = ctypes.c_longlong(n)
         _check(self._lib.lbm_ensemble_samples(self._h, _F(tau0_coarse), _P(X_ptr), _P(T_ptr), cap, ctypes.byref(c)))
         return int(c.value)
+
+
+def force_stats(fxyz, t_start: int, t_end: int | None = None):
+    """ForceCalcs: mean and RMS per component of a force history (n, 3) over
+    lines t_start .. t_end - 1, in the program's FP32 running arithmetic"""
+    f = np.ascontiguousarray(fxyz, np.float32).reshape(-1, 3)
+    n = f.shape[0]
+    mean = np.zeros(3, np.float32)
+    rms = np.zeros(3, np.float32)
+    _check(library().lbm_force_stats(_ptr(f), n, t_start, n if t_end is None else t_end, _ptr(mean), _ptr(rms)))
+    return mean, rms
+
+
+def force_coefficients(fxyz, t_start: int, u: float, d: float, lz: float, rho: float = 1.0) -> dict:
+    """C_D, RMS C_L and the Strouhal number of raw drag/lift histories (n, 3)"""
+    f = np.ascontiguousarray(fxyz, np.float64).reshape(-1, 3)
+    cd, cl, st = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    _check(library().lbm_force_coefficients(_ptr(f), f.shape[0], t_start, u, d, lz, rho, ctypes.byref(cd),
+                                            ctypes.byref(cl), ctypes.byref(st)))
+    return dict(cd=cd.value, cl_rms=cl.value, st=st.value)
+
+
+def wall_profile(v_mean, u_fluc, v_fluc, w_fluc, u_tau: float, nu: float) -> np.ndarray:
+    """VelProf: rows (y+, v+, urms+, vrms+, wrms+) of a wall-normal line"""
+    arrs = [np.ascontiguousarray(a, np.float32) for a in (v_mean, u_fluc, v_fluc, w_fluc)]
+    n = arrs[0].size
+    out = np.zeros((5, n), np.float32)
+    _check(library().lbm_wall_profile(*[_ptr(a) for a in arrs], n, _F(u_tau), _F(nu),
+                                      *[_ptr(out[k]) for k in range(5)]))
+    return out
+
+
+def stats_profiles(stats4: np.ndarray, x: int) -> np.ndarray:
+    """profiles along y at x of statistics float[4][nz][ny][nx], z-averaged"""
+    s = np.ascontiguousarray(stats4, np.float32)
+    _, nz, ny, nx = s.shape
+    out = np.zeros((4, ny), np.float32)
+    _check(library().lbm_stats_profiles(_ptr(s), nx, ny, nz, x, _ptr(out)))
+    return out

@@ -5,7 +5,8 @@ the CUDA kernels (csrc/lbm_kernels.cu), the C ABI host side
 (csrc/lbm_host.cpp), the allocation-free force entry point
 (csrc/lbm_noalloc.cu), and the learned subgrid closure (csrc/sgs_mlp.cu
 kernels, csrc/lbm_sgs.cpp host side), and the ensemble of periodic boxes
-(csrc/ensemble.cu, csrc/lbm_ensemble.cpp).  Host code is built with -ffp-contract=off so geometry
+(csrc/ensemble.cu, csrc/lbm_ensemble.cpp), and the post-processing of the
+outputs (csrc/lbm_post.cpp).  Host code is built with -ffp-contract=off so geometry
 masks and the text writers give identical results on x86 and aarch64 hosts.
 """
 from __future__ import annotations
@@ -35,7 +36,7 @@ def nvcc() -> str:
 
 def sources() -> list[Path]:
     return [CSRC / "lbm_kernels.cu", CSRC / "lbm_host.cpp", CSRC / "lbm_noalloc.cu", CSRC / "sgs_mlp.cu",
-            CSRC / "lbm_sgs.cpp", CSRC / "ensemble.cu", CSRC / "lbm_ensemble.cpp"]
+            CSRC / "lbm_sgs.cpp", CSRC / "ensemble.cu", CSRC / "lbm_ensemble.cpp", CSRC / "lbm_post.cpp"]
 
 
 def _stale(out: Path, deps: list[Path]) -> bool:

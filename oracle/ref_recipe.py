@@ -80,6 +80,20 @@ CPU3D_PROGRAMS = {
 CPU3D_KEEP_OUTPUT = {"cav24"}
 
 
+# the reference's post-processing programs, staged with small constants
+# (ForceCalcs reads lines tStart..tMax-1 of <casename>.force; VelProf reads
+# xDim/2 lines of <casename>_slice.dat; its output loop runs to xDim over
+# arrays of xDim/2 and is bounded to xDim/2 in the staged copy)
+POST_PROGRAMS = {
+    "forcecalcs": ("bgk_channel1/Re3000_Cyl2/ForceCalcs.cpp",
+                   [(r"int tMax = \d+;", "int tMax = 300;"), (r"int tStart = \d+;", "int tStart = 100;"),
+                    (r'string casename = "[^"]*";', 'string casename = "post";')]),
+    "velprof": ("bgk_channel1/Re3000/VelProf.cpp",
+                [(r'string casename = "[^"]*";', 'string casename = "post";'),
+                 (r"for\(i = 0; i<xDim; i\+\+\)\{\n\toutput", "for(i = 0; i<xDim/2; i++){\n\toutput")]),
+}
+
+
 def _cut(text: str, start_pat: str, stop_pat: str) -> str:
     lines = text.splitlines(keepends=True)
     i0 = next(i for i, l in enumerate(lines) if re.match(start_pat, l))
@@ -125,6 +139,16 @@ def stage(ref_root: Path = REF_ROOT) -> bool:
             # timing harness: the final tecplot dump of every node is not part of the loop
             s = s.replace('output.open ("output.dat");', "/* output.dat dump disabled for timing */")
         (REF_DIR / f"cpu3d_{name}.cpp").write_text(s)
+    for name, (rel, subs) in POST_PROGRAMS.items():
+        src = ref_root / rel
+        if not src.exists():
+            continue
+        s = src.read_text(errors="replace")
+        for pat, rep in subs:
+            s, n = re.subn(pat, rep, s, count=1)
+            if n != 1:
+                raise RuntimeError(f"staging {rel}: pattern {pat!r} not found")
+        (REF_DIR / f"{name}.cpp").write_text(s)
     return True
 
 
@@ -190,6 +214,10 @@ def build_ref(force: bool = False, jobs: int = 8) -> list[Path]:
         out = REF_DIR / f"cpu3d_{name}"
         if force or not out.exists():
             jobs_list.append([CXX, "-O3", "-march=native", "-w", "-o", str(out), str(REF_DIR / f"cpu3d_{name}.cpp")])
+    for name in POST_PROGRAMS:
+        src, out = REF_DIR / f"{name}.cpp", REF_DIR / name
+        if src.exists() and (force or not out.exists()):
+            jobs_list.append([CXX, "-O2", "-ffp-contract=off", "-w", "-o", str(out), str(src)])
     with ThreadPoolExecutor(jobs) as ex:
         list(ex.map(_run_cpu3d_fallback, jobs_list))
     return sorted(REF_DIR.glob("*.so"))
