@@ -129,6 +129,12 @@ int lbm_get_last_force(lbm_handle* h, double* f3);
  * force arrays once, after the loop, LR7:2970-2980) */
 int lbm_get_last_force_async(lbm_handle* h, double* f3);
 
+/* dynamic inlet (DI3, records with DYNY1): the P-control history, one
+ * entry {t, mean v of the plane DYNY1, dpdy after the update} per control
+ * step (DI3:3150-3170, its outputAvV file); *n = entries so far, up to
+ * max_entries written */
+int lbm_get_dyn_history(lbm_handle* h, float* hist3, int max_entries, int* n);
+
 /* number of kernels the handle has launched since lbm_create (all levels,
  * every entry point that takes the handle); instrumentation with no
  * counterpart in the reference */
@@ -228,6 +234,17 @@ int lbm_tc_selftest(int kc, const uint16_t* A, const uint16_t* B, float* D);
  * the stream-collide then takes its eddy viscosity from the MLP on the
  * tensor cores instead of the Smagorinsky model.  n = lbm_mlp_param_count() */
 int lbm_set_sgs_mlp(lbm_handle* h, const float* params, int n);
+
+/* Checkpoint and restart (no counterpart in the reference, which always
+ * starts from the equilibrium).  A checkpoint holds the run record, the time,
+ * every level's stored populations as they are (so FP16 / BF16 restart
+ * bit-exactly), the statistics, the force history and the closure weights.
+ * lbm_restore_state loads one into a handle made from an equivalent record;
+ * lbm_create_from_state makes the handle from the record inside the file.
+ * Continuing a restored run gives the same bits as never stopping. */
+int lbm_save_state(lbm_handle* h, const char* path);
+int lbm_restore_state(lbm_handle* h, const char* path);
+int lbm_create_from_state(const char* path, lbm_handle** out);
 
 /* ------------------------------------------------------------------------
  * Ensemble of periodic D3Q19 boxes (decaying turbulence), the data source of

@@ -67,6 +67,10 @@ SIGNATURES = [
     ("lbm_tc_selftest", _I, [_I, _P, _P, _P]),
     ("lbm_mlp_predict_tc", _I, [_P, _P, _I, _P, _P]),
     ("lbm_set_sgs_mlp", _I, [_P, _P, _I]),
+    ("lbm_save_state", _I, [_P, ctypes.c_char_p]),
+    ("lbm_get_dyn_history", _I, [_P, _P, _I, _P]),
+    ("lbm_restore_state", _I, [_P, ctypes.c_char_p]),
+    ("lbm_create_from_state", _I, [ctypes.c_char_p, _P]),
     ("lbm_force_stats", _I, [_P, _I, _I, _I, _P, _P]),
     ("lbm_force_coefficients", _I, [_P, _I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                     _P, _P, _P]),
@@ -196,7 +200,8 @@ def make_inputs(nx: int, ny: int, nz: int, *, obst1=(0.0, 0.0, 0.0), r1=1.0, obs
              "lid_face": "LID face:", "inlet_noise": "Inlet noise:", "seed": "Seed:", "velav": "VELAV:",
              "init": "Init:", "init_velocity": "Init velocity:", "order": "ORDER:", "fc_top_zflip": "FC top zflip:",
              "edge_pull": "EDGE PULL:", "lid_bc": "LID BC:", "bounceback": "BOUNCEBACK:", "sgs": "SGS:",
-             "sgs_weights": "SGS weights:"}
+             "sgs_weights": "SGS weights:", "dyny1": "DYNY1:", "dyn_every": "DYN every:",
+             "dyn_start": "DYN start:", "trip_end": "TRIP end:", "kp": "KP:"}
     for k, v in ext.items():
         if k not in names:
             raise KeyError(f"unknown .inputs extension key {k!r}")
@@ -366,6 +371,32 @@ class Solver:
         if out.dtype != np.float64 or out.size < 3 or not out.flags["C_CONTIGUOUS"]:
             raise ValueError("out must be a contiguous float64 array of 3")
         _check(self._lib.lbm_get_last_force_async(self._h, _ptr(out)))
+
+    def dyn_history(self) -> np.ndarray:
+        """the dynamic inlet's control history, rows (t, mean v, dpdy)"""
+        n = _I()
+        _check(self._lib.lbm_get_dyn_history(self._h, None, 0, ctypes.byref(n)))
+        h = np.zeros((n.value, 3), np.float32)
+        if n.value:
+            _check(self._lib.lbm_get_dyn_history(self._h, _ptr(h), n.value, ctypes.byref(n)))
+        return h
+
+    def save_state(self, path: str) -> None:
+        """checkpoint: record, time, stored populations, statistics, forces"""
+        _check(self._lib.lbm_save_state(self._h, str(path).encode()))
+
+    def restore_state(self, path: str) -> None:
+        _check(self._lib.lbm_restore_state(self._h, str(path).encode()))
+
+    @classmethod
+    def from_state(cls, path: str) -> "Solver":
+        """a solver made from the record inside a checkpoint, at its state"""
+        self = cls.__new__(cls)
+        self._lib = library()
+        h = _P()
+        _check(self._lib.lbm_create_from_state(str(path).encode(), ctypes.byref(h)))
+        self._h = h
+        return self
 
     def set_sgs_mlp(self, params: np.ndarray) -> None:
         """weights of the learned closure (the record must select sgs="mlp")"""

@@ -92,6 +92,12 @@ struct Config {
     int halfway = 0;                /* "BOUNCEBACK: halfway" or "fullway" (the reference) */
     int lid_quirk = 0;              /* "LID BC: cpu3d" reproduces CPU_3D's lid as written */
     int sgs_mlp = 0;                /* "SGS: mlp": the learned closure replaces Smagorinsky */
+    /* dynamic inlet (DI3): body force below DYNY1 (DI3:1358), P-control of
+     * the mean velocity of the plane DYNY1 every DYN every steps after DYN
+     * start (DI3:3150-3170), trip bodies (Obst2) until TRIP end (DI3:72-90) */
+    int dyny1 = -1;
+    int dyn_every = 100, dyn_start = 10000;
+    int trip_end = 5000;
     std::string sgs_weights;        /* "SGS weights: <file>" of float32 parameters */
     /* older records spell the LES line "Smagorinski LES: YES/NO"; DynInlet
      * records add "KP" (the inlet P-control gain, MRTtest/DynInlet3.cu:26) */
@@ -203,6 +209,10 @@ int parse_inputs(const char* text, Config& c) {
             c.sgs_mlp = val == "mlp";
         }
         else if (key == "SGS weights") c.sgs_weights = val;
+        else if (key == "DYNY1") I(c.dyny1);
+        else if (key == "DYN every") I(c.dyn_every);
+        else if (key == "DYN start") I(c.dyn_start);
+        else if (key == "TRIP end") I(c.trip_end);
         else if (key == "LID BC") {
             ok = (val == "cpu3d" || val == "regularized");
             c.lid_quirk = val == "cpu3d";
@@ -299,6 +309,10 @@ std::string value_of(const Config& c, const std::string& key, float omega, float
     else if (key == "BOUNCEBACK") o << (c.halfway ? "halfway" : "fullway");
     else if (key == "SGS") o << (c.sgs_mlp ? "mlp" : "smagorinsky");
     else if (key == "SGS weights") o << c.sgs_weights;
+    else if (key == "DYNY1") o << c.dyny1;
+    else if (key == "DYN every") o << c.dyn_every;
+    else if (key == "DYN start") o << c.dyn_start;
+    else if (key == "TRIP end") o << c.trip_end;
     return o.str();
 }
 
@@ -357,6 +371,10 @@ std::string write_inputs(const Config& c, float omega, float omegaLR) {
     if (c.halfway) line("BOUNCEBACK: ", "BOUNCEBACK");
     if (c.sgs_mlp) line("SGS: ", "SGS");
     if (!c.sgs_weights.empty()) line("SGS weights: ", "SGS weights");
+    if (c.dyny1 != d.dyny1) line("DYNY1: ", "DYNY1");
+    if (c.dyn_every != d.dyn_every) line("DYN every: ", "DYN every");
+    if (c.dyn_start != d.dyn_start) line("DYN start: ", "DYN start");
+    if (c.trip_end != d.trip_end) line("TRIP end: ", "TRIP end");
     return o.str();
 }
 
@@ -372,12 +390,13 @@ int body_shape(const std::string& g) {
 
 /* channel programs (LR7:88-127): body, then walls y = 0 / ny-1, inlet x = 0,
  * outlet x = nx-1 (walls override inlet/outlet, both override the body) */
-void mask_base(const Config& c, std::vector<uint8_t>& m) {
+void mask_base(const Config& c, std::vector<uint8_t>& m, int t = 0) {
     const int nx = c.nx, ny = c.ny, nz = c.nz;
     m.assign(size_t(nx) * ny * nz, FLUID);
     const int shape = body_shape(c.geometry);
     const bool channel = c.geometry.rfind("channel", 0) == 0;
     const bool cavity = c.geometry == "cavity";
+    const bool dyn = c.geometry == "dyninlet";
     for (int z = 0; z < nz; ++z)
         for (int y = 0; y < ny; ++y)
             for (int x = 0; x < nx; ++x) {
@@ -392,6 +411,17 @@ void mask_base(const Config& c, std::vector<uint8_t>& m) {
                     if (y == 0 || y == ny - 1) v = WALL;
                     else if (x == 0) v = WEST_INLET;
                     else if (x == nx - 1) v = EAST_OUTLET;
+                } else if (dyn) {
+                    /* DI3's ImageFcn (DI3:72-90): trip blocks around Obst2
+                     * (the second one only in the plane z = 10) until
+                     * TRIP end, walls at x = 0 and nx - 1, periodic in y, z */
+                    const float fx = float(x), fy = float(y);
+                    if (t < c.trip_end) {
+                        if (std::fabs(fx - c.ob2[0]) < c.r2 && std::fabs(fy - c.ob2[1]) < c.r2) v = BODY;
+                        if (std::fabs(fx - c.ob2[0] - 3.f) < c.r2 && std::fabs(fy - c.ob2[1] - 3.f) < c.r2 && z == 10)
+                            v = BODY;
+                    }
+                    if (x == 0 || x == nx - 1) v = WALL;
                 } else if (cavity) {
                     int p[3] = {x, y, z}, n[3] = {nx, ny, nz};
                     int a = c.lid_face / 2;
@@ -476,6 +506,13 @@ struct lbm_handle {
     unsigned char* mlp_blob = nullptr;
     int* mlp_err = nullptr;
     bool mlp_ready = false;
+    std::vector<float> mlp_params; /* host copy, for checkpoints */
+    /* dynamic inlet: the body force on the device, the control history
+     * (t, mean v, dpdy per control step) and whether the trip is in the mask */
+    float* dpdy_dev = nullptr;
+    float* dyn_hist = nullptr;
+    int dyn_cap = 0, dyn_n = 0;
+    bool trip_in_mask = false;
 };
 
 namespace {
@@ -631,6 +668,8 @@ StepParams base_params(const lbm_handle* h, int level) {
     p.stats_weight = level == 0 ? 1.f : c.lrfactor;
     p.noise_amp = level == 0 ? c.noise : 0.f;
     p.noise_seed = c.seed;
+    p.dpdy_dev = h->dpdy_dev;
+    p.dyn_y1 = c.dyny1 >= 0 ? c.dyny1 : (1 << 30);
     return p;
 }
 
@@ -638,9 +677,18 @@ int do_init(lbm_handle* h) {
     const Config& c = h->cfg;
     int kind = c.init >= 0 ? c.init : (h->model == BGK ? 1 : 0);
     float u0 = c.init_u > -1e29f ? c.init_u : (c.geometry == "cavity" || c.geometry == "periodic" ? 0.f : c.umax);
+    /* the dynamic-inlet duct flows along y (DI3:1198-1209) */
+    const int axis = c.geometry == "dyninlet" ? 1 : 0;
+    if (c.geometry == "dyninlet" && !h->trip_in_mask && c.trip_end > 0) {
+        mask_base(c, h->lv[0].hmask, 0);
+        if (int rc = upload_mask(h, 0)) return rc;
+        h->trip_in_mask = true;
+    }
+    if (h->dpdy_dev) CUDA_TRY(cudaMemcpyAsync(h->dpdy_dev, &c.dpdy, sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    h->dyn_n = 0;
     for (int l = 0; l < h->nlevels; ++l) {
         LevelState& s = h->lv[l];
-        for (int i = 0; i < 2; ++i) CUDA_TRY(launch_init(s.L, s.mask, s.f[i], kind, u0, h->stream));
+        for (int i = 0; i < 2; ++i) CUDA_TRY(launch_init(s.L, s.mask, s.f[i], kind, u0, h->stream, axis));
         h->launches += 2;
         s.cur = 0;
         if (s.stats) CUDA_TRY(cudaMemsetAsync(s.stats, 0, size_t(s.L.qstride) * 4 * sizeof(float), h->stream));
@@ -686,6 +734,14 @@ int one_step(lbm_handle* h) {
         int rc = ensure_force_cap(h, fidx + 1);
         if (rc) return rc;
     }
+    if (h->trip_in_mask && t >= c.trip_end) {
+        /* the trip blocks vanish (DI3's ImageFcn is false from TRIP end on) */
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        mask_base(c, C.hmask, t);
+        if (int rc = upload_mask(h, 0)) return rc;
+        h->trip_in_mask = false;
+        p.has_lid = C.has_lid ? 1 : 0;
+    }
     if (c.sgs_mlp && !h->mlp_ready)
         return fail(LBM_ERR_STATE, "SGS mlp: no weights (SGS weights record line or lbm_set_sgs_mlp)");
     if (p.force_on) CUDA_TRY(fork_force(h, C, h->force_hist + 3LL * fidx));
@@ -698,6 +754,14 @@ int one_step(lbm_handle* h) {
     ++h->launches;
     if (p.force_on) CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
     C.cur = 1 - C.cur;
+    if (h->dpdy_dev && c.dyny1 >= 0 && c.dyn_every > 0 && t % c.dyn_every == 0 && t > c.dyn_start &&
+        h->dyn_n < h->dyn_cap) {
+        /* the P-control on the state after step t (DI3:3150-3170) */
+        CUDA_TRY(launch_dyn_control(C.L, C.f[C.cur], c.dyny1, c.umax, c.kp, std::fabs(c.dpdy), h->dpdy_dev,
+                                    h->dyn_hist + 3LL * h->dyn_n, t, h->stream));
+        ++h->launches;
+        ++h->dyn_n;
+    }
     if (c.refinement) {
         LevelState& Fn = h->lv[1];
         const int L = int(std::lround(1.0 / c.lrfactor));
@@ -735,6 +799,14 @@ int check_level(const lbm_handle* h, int level) {
 /* ------------------------------------------------------------------------ */
 /* C ABI                                                                       */
 /* ------------------------------------------------------------------------ */
+
+namespace {
+const char CKPT_MAGIC[12] = {'L', 'B', 'M', 'G', 'B', '3', '0', '0', 'C', 'K', 'P', 'T'};
+constexpr uint32_t CKPT_VERSION = 1;
+
+template <class V> void put(std::ostream& o, const V& v) { o.write(reinterpret_cast<const char*>(&v), sizeof v); }
+template <class V> bool get(std::istream& i, V& v) { return bool(i.read(reinterpret_cast<char*>(&v), sizeof v)); }
+}  // namespace
 
 extern "C" {
 
@@ -825,7 +897,7 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
     if (model < 0) return fail(LBM_ERR_CONFIG, "MODEL '%s' is not one of MRT, MRT_DI3, BGK, MRT_CPU3D", c.model.c_str());
     const int storage = storage_id(c.precision);
     if (storage < 0) return fail(LBM_ERR_CONFIG, "PRECISION '%s' is not one of fp32, fp16, bf16, fp64", c.precision.c_str());
-    static const char* geoms[] = {"channel_square", "channel_circle", "channel", "cavity", "periodic"};
+    static const char* geoms[] = {"channel_square", "channel_circle", "channel", "cavity", "periodic", "dyninlet"};
     if (std::find(std::begin(geoms), std::end(geoms), c.geometry) == std::end(geoms))
         return fail(LBM_ERR_CONFIG, "GEOMETRY '%s' is not supported", c.geometry.c_str());
     if (c.refinement) {
@@ -884,6 +956,16 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
     const float u_ref = c.geometry.rfind("channel", 0) == 0 ? c.umax : 0.f;
     if ((rc = alloc_level(h->lv[0], c.nx, c.ny, c.nz, storage, c.velav != 0, u_ref))) return bail(rc);
     mask_base(c, h->lv[0].hmask);
+    h->trip_in_mask = c.geometry == "dyninlet" && c.trip_end > 0;
+    if (c.dyny1 >= 0) {
+        if (c.dyny1 >= c.ny || c.dyn_every <= 0)
+            return bail(fail(LBM_ERR_CONFIG, "DYNY1 %d must lie in 0..%d and DYN every be positive", c.dyny1, c.ny - 1));
+        h->dyn_cap = std::max(1, c.tmax / c.dyn_every + 2);
+        if (cudaMalloc(&h->dpdy_dev, sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&h->dyn_hist, size_t(h->dyn_cap) * 3 * sizeof(float)) != cudaSuccess)
+            return bail(fail(LBM_ERR_NOMEM, "dynamic inlet buffers"));
+        cudaMemcpy(h->dpdy_dev, &c.dpdy, sizeof(float), cudaMemcpyHostToDevice);
+    }
     if ((rc = upload_mask(h, 0))) return bail(rc);
     if (c.refinement) {
         if ((rc = alloc_level(h->lv[1], c.lrx, c.lry, c.lrz, storage, c.velav != 0, u_ref))) return bail(rc);
@@ -930,6 +1012,8 @@ int lbm_destroy(lbm_handle* h) {
     if (h->ev1) cudaEventDestroy(h->ev1);
     cudaFree(h->mlp_blob);
     cudaFree(h->mlp_err);
+    cudaFree(h->dpdy_dev);
+    cudaFree(h->dyn_hist);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->side) cudaStreamDestroy(h->side);
@@ -1065,7 +1149,167 @@ int lbm_set_sgs_mlp(lbm_handle* h, const float* params, int n) {
     }
     CUDA_TRY(cudaMemcpyAsync(h->mlp_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->mlp_params.assign(params, params + n);
     h->mlp_ready = true;
+    return LBM_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* checkpoint / restart (no counterpart in the reference)                     */
+/* ------------------------------------------------------------------------ */
+
+int lbm_save_state(lbm_handle* h, const char* path) {
+    if (!h || !path) return fail(LBM_ERR_ARG, "null argument");
+    if (int rc = lbm_synchronize(h)) return rc;
+    std::ofstream o(path, std::ios::binary);
+    if (!o) return fail(LBM_ERR_ARG, "checkpoint: cannot write '%s'", path);
+    const std::string rec = write_inputs(h->cfg, h->omega, h->omegaLR);
+    o.write(CKPT_MAGIC, sizeof CKPT_MAGIC);
+    put(o, CKPT_VERSION);
+    put(o, uint64_t(rec.size()));
+    o.write(rec.data(), std::streamsize(rec.size()));
+    put(o, int32_t(h->t));
+    put(o, int32_t(h->nlevels));
+    for (int l = 0; l < h->nlevels; ++l) {
+        const LevelState& s = h->lv[l];
+        const Level& L = s.L;
+        const int32_t hdr[6] = {L.nx, L.ny, L.nz, L.pitch, h->storage, s.stats ? 1 : 0};
+        for (int32_t v : hdr) put(o, v);
+        /* the stored populations as they are (raw FP16 / BF16 / FP32 / FP64) */
+        std::vector<char> raw(size_t(L.qstride) * 19 * storage_bytes(h->storage));
+        CUDA_TRY(cudaMemcpy(raw.data(), s.f[s.cur], raw.size(), cudaMemcpyDeviceToHost));
+        o.write(raw.data(), std::streamsize(raw.size()));
+        if (s.stats) {
+            std::vector<float> st(size_t(L.qstride) * 4);
+            CUDA_TRY(cudaMemcpy(st.data(), s.stats, st.size() * sizeof(float), cudaMemcpyDeviceToHost));
+            o.write(reinterpret_cast<const char*>(st.data()), std::streamsize(st.size() * sizeof(float)));
+        }
+    }
+    const int32_t nf = std::max(0, std::min(h->t - h->cfg.startf, h->force_cap));
+    put(o, nf);
+    if (nf > 0) {
+        std::vector<double> fh(size_t(nf) * 3);
+        CUDA_TRY(cudaMemcpy(fh.data(), h->force_hist, fh.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        o.write(reinterpret_cast<const char*>(fh.data()), std::streamsize(fh.size() * sizeof(double)));
+    }
+    put(o, int32_t(h->mlp_params.size()));
+    if (!h->mlp_params.empty())
+        o.write(reinterpret_cast<const char*>(h->mlp_params.data()), std::streamsize(h->mlp_params.size() * 4));
+    /* dynamic inlet: the controlled body force and the control history */
+    float dp = h->cfg.dpdy;
+    if (h->dpdy_dev) CUDA_TRY(cudaMemcpy(&dp, h->dpdy_dev, sizeof(float), cudaMemcpyDeviceToHost));
+    put(o, dp);
+    put(o, int32_t(h->dyn_n));
+    if (h->dyn_n > 0) {
+        std::vector<float> hh(size_t(h->dyn_n) * 3);
+        CUDA_TRY(cudaMemcpy(hh.data(), h->dyn_hist, hh.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        o.write(reinterpret_cast<const char*>(hh.data()), std::streamsize(hh.size() * sizeof(float)));
+    }
+    if (!o) return fail(LBM_ERR_ARG, "checkpoint: write to '%s' failed", path);
+    return LBM_OK;
+}
+
+static int read_checkpoint_record(std::istream& in, std::string& rec) {
+    char magic[sizeof CKPT_MAGIC];
+    uint32_t ver = 0;
+    uint64_t len = 0;
+    if (!in.read(magic, sizeof magic) || std::memcmp(magic, CKPT_MAGIC, sizeof magic) != 0)
+        return fail(LBM_ERR_PARSE, "checkpoint: not a checkpoint file");
+    if (!get(in, ver) || ver != CKPT_VERSION) return fail(LBM_ERR_PARSE, "checkpoint: version %u not readable", ver);
+    if (!get(in, len) || len > (1u << 24)) return fail(LBM_ERR_PARSE, "checkpoint: bad record length");
+    rec.resize(len);
+    if (!in.read(&rec[0], std::streamsize(len))) return fail(LBM_ERR_PARSE, "checkpoint: truncated record");
+    return LBM_OK;
+}
+
+int lbm_restore_state(lbm_handle* h, const char* path) {
+    if (!h || !path) return fail(LBM_ERR_ARG, "null argument");
+    std::ifstream in(path, std::ios::binary);
+    if (!in) return fail(LBM_ERR_ARG, "checkpoint: cannot read '%s'", path);
+    std::string rec;
+    if (int rc = read_checkpoint_record(in, rec)) return rc;
+    int32_t t = 0, nl = 0;
+    if (!get(in, t) || !get(in, nl) || nl != h->nlevels || t < 0)
+        return fail(LBM_ERR_CONFIG, "checkpoint: %d levels, the handle has %d", nl, h->nlevels);
+    if (int rc = lbm_synchronize(h)) return rc;
+    for (int l = 0; l < nl; ++l) {
+        LevelState& s = h->lv[l];
+        const Level& L = s.L;
+        int32_t hdr[6];
+        for (int32_t& v : hdr)
+            if (!get(in, v)) return fail(LBM_ERR_PARSE, "checkpoint: truncated level header");
+        if (hdr[0] != L.nx || hdr[1] != L.ny || hdr[2] != L.nz || hdr[3] != L.pitch || hdr[4] != h->storage)
+            return fail(LBM_ERR_CONFIG, "checkpoint: level %d is %dx%dx%d (pitch %d, storage %d), the handle's %dx%dx%d",
+                        l, hdr[0], hdr[1], hdr[2], hdr[3], hdr[4], L.nx, L.ny, L.nz);
+        std::vector<char> raw(size_t(L.qstride) * 19 * storage_bytes(h->storage));
+        if (!in.read(raw.data(), std::streamsize(raw.size()))) return fail(LBM_ERR_PARSE, "checkpoint: truncated level");
+        for (int b = 0; b < 2; ++b) CUDA_TRY(cudaMemcpy(s.f[b], raw.data(), raw.size(), cudaMemcpyHostToDevice));
+        s.cur = 0;
+        if (hdr[5]) {
+            std::vector<float> st(size_t(L.qstride) * 4);
+            if (!in.read(reinterpret_cast<char*>(st.data()), std::streamsize(st.size() * 4)))
+                return fail(LBM_ERR_PARSE, "checkpoint: truncated statistics");
+            if (s.stats) CUDA_TRY(cudaMemcpy(s.stats, st.data(), st.size() * 4, cudaMemcpyHostToDevice));
+        }
+    }
+    int32_t nf = 0;
+    if (!get(in, nf) || nf < 0) return fail(LBM_ERR_PARSE, "checkpoint: bad force history");
+    if (nf > 0) {
+        std::vector<double> fh(size_t(nf) * 3);
+        if (!in.read(reinterpret_cast<char*>(fh.data()), std::streamsize(fh.size() * 8)))
+            return fail(LBM_ERR_PARSE, "checkpoint: truncated force history");
+        if (int rc = ensure_force_cap(h, nf)) return rc;
+        CUDA_TRY(cudaMemcpy(h->force_hist, fh.data(), fh.size() * 8, cudaMemcpyHostToDevice));
+    }
+    int32_t np = 0;
+    if (get(in, np) && np > 0) {
+        std::vector<float> prm(np);
+        if (!in.read(reinterpret_cast<char*>(prm.data()), std::streamsize(np) * 4))
+            return fail(LBM_ERR_PARSE, "checkpoint: truncated closure weights");
+        if (h->cfg.sgs_mlp)
+            if (int rc = lbm_set_sgs_mlp(h, prm.data(), np)) return rc;
+    }
+    float dp = 0;
+    int32_t nd = 0;
+    if (get(in, dp) && get(in, nd) && nd >= 0) {
+        std::vector<float> hh(size_t(nd) * 3);
+        if (nd > 0 && !in.read(reinterpret_cast<char*>(hh.data()), std::streamsize(hh.size() * 4)))
+            return fail(LBM_ERR_PARSE, "checkpoint: truncated control history");
+        if (h->dpdy_dev) {
+            CUDA_TRY(cudaMemcpy(h->dpdy_dev, &dp, sizeof(float), cudaMemcpyHostToDevice));
+            const int k = std::min(int(nd), h->dyn_cap);
+            if (k > 0) CUDA_TRY(cudaMemcpy(h->dyn_hist, hh.data(), size_t(k) * 3 * 4, cudaMemcpyHostToDevice));
+            h->dyn_n = k;
+        }
+    }
+    /* the trip blocks are in the mask only before TRIP end */
+    if (h->cfg.geometry == "dyninlet" && h->trip_in_mask != (t < h->cfg.trip_end)) {
+        mask_base(h->cfg, h->lv[0].hmask, t);
+        if (int rc = upload_mask(h, 0)) return rc;
+        h->trip_in_mask = t < h->cfg.trip_end;
+    }
+    h->t = t;
+    return LBM_OK;
+}
+
+int lbm_create_from_state(const char* path, lbm_handle** out) {
+    if (!path || !out) return fail(LBM_ERR_ARG, "null argument");
+    *out = nullptr;
+    std::string rec;
+    {
+        std::ifstream in(path, std::ios::binary);
+        if (!in) return fail(LBM_ERR_ARG, "checkpoint: cannot read '%s'", path);
+        if (int rc = read_checkpoint_record(in, rec)) return rc;
+    }
+    lbm_handle* h = nullptr;
+    if (int rc = lbm_create(rec.c_str(), &h)) return rc;
+    if (int rc = lbm_restore_state(h, path)) {
+        const std::string msg = g_err;
+        lbm_destroy(h);
+        g_err = msg;
+        return rc;
+    }
+    *out = h;
     return LBM_OK;
 }
 
@@ -1112,6 +1356,17 @@ int lbm_get_forces(lbm_handle* h, double* fxyz, int max_steps, int* n) {
         CUDA_TRY(cudaStreamSynchronize(h->stream));
     }
     if (n) *n = k;
+    return LBM_OK;
+}
+
+int lbm_get_dyn_history(lbm_handle* h, float* hist3, int max_entries, int* n) {
+    if (!h || max_entries < 0 || (max_entries > 0 && !hist3)) return fail(LBM_ERR_ARG, "bad argument");
+    const int k = std::min(h->dyn_n, max_entries);
+    if (k > 0) {
+        CUDA_TRY(cudaMemcpyAsync(hist3, h->dyn_hist, size_t(k) * 3 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+    }
+    if (n) *n = h->dyn_n;
     return LBM_OK;
 }
 
@@ -1325,6 +1580,7 @@ int lbm_stream_collide_f32(const float* fA, float* fB, const uint8_t* mask, int 
     p.rho_out = rho_out;
     p.t = t;
     p.stats_weight = 1.f;
+    p.dyn_y1 = 1 << 30;
     p.has_lid = 1; /* the caller's mask may hold any node type */
     CUDA_TRY(launch_stream_collide(L, p, fA, fB, mask, nullptr, nullptr, (cudaStream_t)cuda_stream));
     return LBM_OK;

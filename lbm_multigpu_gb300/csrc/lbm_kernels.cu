@@ -136,7 +136,9 @@ __device__ __forceinline__ void sc_node(const Level& L, const StepParams& p, con
         } else if ((FEAT & FEAT_LID) && type == LID) {
             lid<T>(f, p.lid_face, T(p.lid_u[0]), T(p.lid_u[1]), T(p.lid_u[2]), p.lid_quirk != 0);
         }
-        collide<T>(p.model, f, T(p.omega), p.les != 0, T(p.cs), T(p.dpdy));
+        T dp = T(p.dpdy_dev ? *p.dpdy_dev : p.dpdy);
+        if (y > p.dyn_y1) dp = T(0);
+        collide<T>(p.model, f, T(p.omega), p.les != 0, T(p.cs), dp);
 
         if (p.stats_on && p.t >= p.start_av) {
             /* vel_av / vel_fluc (LR7:1018-1058): running mean, then variance */
@@ -330,6 +332,45 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, 6) k_stream_collide_mlp(const L
 #endif
 }
 
+/* DI3's AverageV (DI3:2561-2598) and the P-control update of the body force
+ * (DI3:3150-3170) in one block on the device, so the loop needs no host
+ * round trip: the y momentum of every node of the plane y1 (all x, all z)
+ * summed in FP64 in a fixed order, divided by (nx - 2) nz as the reference
+ * does, then dpdy += (mean - umax) / umax * kp * |dpdy0| */
+template <class S>
+__global__ void __launch_bounds__(256) k_dyn_control(const Level L, const S* __restrict__ f, int y1, float umax,
+                                                     float kp, float dpdy0_abs, float* __restrict__ dpdy,
+                                                     float* __restrict__ hist3, int t) {
+    using F = Fmt<S>;
+    __shared__ double red[256];
+    double s = 0;
+    const int n = L.nx * L.nz;
+    for (int i = threadIdx.x; i < n; i += 256) {
+        const int x = i % L.nx, z = i / L.nx;
+        const size_t c = size_t(z) * L.plane + size_t(y1) * L.pitch + x;
+        float v = 0;
+#pragma unroll
+        for (int q = 0; q < 19; ++q)
+            if (cy(q)) v += float(cy(q)) * float(F::ld(f + q * L.qstride + c, L.off[q]));
+        s += double(v);
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (int(threadIdx.x) < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const float av = float(red[0]) / float((L.nx - 2) * L.nz);
+        const float diff = (av - umax) / umax;
+        const float d = *dpdy + diff * kp * dpdy0_abs;
+        *dpdy = d;
+        hist3[0] = float(t);
+        hist3[1] = av;
+        hist3[2] = d;
+    }
+}
+
 /* Momentum exchange at BODY nodes (LR7:1494-1502, reduced per block at
  * LR7:1607-1626): F += 2 sum_q c_q f_q over the populations a body node pulls
  * from fA.  Runs over a compact list of body nodes (pitched indices) instead
@@ -444,7 +485,8 @@ __global__ void k_reduce3(const double* __restrict__ part, int n, double* __rest
  * moments (mrt_meq + InvertMoments); kind 1: the BGK equilibrium; kind 2: the
  * BGK equilibrium at u0 on every node, solids included (CPU:1226-1308). */
 template <class S>
-__global__ void k_init(const Level L, const uint8_t* __restrict__ mask, S* __restrict__ f, int kind, float u0) {
+__global__ void k_init(const Level L, const uint8_t* __restrict__ mask, S* __restrict__ f, int kind, float u0,
+                       int axis) {
     using F = Fmt<S>;
     using T = typename F::T;
     const int x = blockIdx.x * SC_BX + threadIdx.x, y = blockIdx.y * SC_BY + threadIdx.y, z = blockIdx.z;
@@ -454,12 +496,13 @@ __global__ void k_init(const Level L, const uint8_t* __restrict__ mask, S* __res
     const T u = (kind != 2 && (type == WALL || type == BODY)) ? T(0) : T(u0);
     T g[19];
     if (kind == 0) {
-        const T mom[9] = {T(1), u, T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+        T mom[9] = {T(1), T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+        mom[1 + axis] = u;
         invert_scaled<T>(mom, T(0), g);
     } else {
 #pragma unroll
         for (int q = 0; q < 19; ++q) {
-            const T cu = T(cx(q)) * u;
+            const T cu = T(axis == 0 ? cx(q) : axis == 1 ? cy(q) : cz(q)) * u;
             g[q] = T(wq(q)) * (T(1) + T(3) * cu + T(4.5) * cu * cu - T(1.5) * u * u);
         }
     }
@@ -841,6 +884,14 @@ cudaError_t launch_stream_collide_mlp(const Level& L, const StepParams& p, const
     }
 }
 
+cudaError_t launch_dyn_control(const Level& L, const void* f, int y1, float umax, float kp, float dpdy0_abs,
+                               float* dpdy_dev, float* hist3, int t, cudaStream_t s) {
+    if (y1 < 0 || y1 >= L.ny) return cudaErrorInvalidValue;
+    LBM_DISPATCH(L.storage, (k_dyn_control<S><<<1, 256, 0, s>>>(L, (const S*)f, y1, umax, kp, dpdy0_abs, dpdy_dev,
+                                                                  hist3, t)));
+    return cudaGetLastError();
+}
+
 int force_partials() { return FORCE_BLOCKS; }
 
 cudaError_t launch_force(const Level& L, const void* fA, const unsigned* body, int nbody, double* partials,
@@ -911,9 +962,9 @@ cudaError_t launch_force_scan(const Level& L, const void* fA, const uint8_t* mas
     return cudaGetLastError();
 }
 
-cudaError_t launch_init(const Level& L, const uint8_t* mask, void* f, int kind, float u0, cudaStream_t s) {
+cudaError_t launch_init(const Level& L, const uint8_t* mask, void* f, int kind, float u0, cudaStream_t s, int axis) {
     const dim3 block(SC_BX, SC_BY), grid = sc_grid(L);
-    LBM_DISPATCH(L.storage, (k_init<S><<<grid, block, 0, s>>>(L, mask, (S*)f, kind, u0)));
+    LBM_DISPATCH(L.storage, (k_init<S><<<grid, block, 0, s>>>(L, mask, (S*)f, kind, u0, axis)));
     return cudaGetLastError();
 }
 

@@ -45,6 +45,11 @@ struct StepParams {
     int model;
     int les;
     float omega, cs, dpdy;
+    /* dynamic inlet (DI3): when dpdy_dev is set the body force is read from
+     * the device (the P-control updates it there); nodes with y > dyn_y1 get
+     * no body force (DI3:1358) */
+    const float* dpdy_dev;
+    int dyn_y1;
     float u_in, rho_out;
     float lid_u[3];
     int lid_face;
@@ -97,7 +102,14 @@ int force_scan_partials();
 
 /* record an error for lbm_last_error(); returns code (lbm_host.cpp) */
 int set_error(int code, const char* what, cudaError_t e);
-cudaError_t launch_init(const Level& L, const uint8_t* mask, void* f, int kind, float u0, cudaStream_t s);
+/* axis: direction of the initial velocity u0 (0 x, 1 y, 2 z) */
+cudaError_t launch_init(const Level& L, const uint8_t* mask, void* f, int kind, float u0, cudaStream_t s,
+                        int axis = 0);
+/* DI3 P-control (DI3:2561-2598, 3150-3170), on the device: the mean y
+ * momentum of the plane y1 over (nx - 2) nz nodes, then
+ * dpdy += (mean - umax) / umax * kp * |dpdy0|; hist3 gets {t, mean, dpdy} */
+cudaError_t launch_dyn_control(const Level& L, const void* f, int y1, float umax, float kp, float dpdy0_abs,
+                               float* dpdy_dev, float* hist3, int t, cudaStream_t s);
 cudaError_t launch_fields(const Level& L, const void* f, float* rho, float* u, float* v, float* w, cudaStream_t s);
 cudaError_t launch_pack(const Level& L, const void* f, float* compact, cudaStream_t s);
 cudaError_t launch_unpack(const Level& L, const float* compact, void* f, cudaStream_t s);

@@ -506,7 +506,9 @@ void step_impl(const orc_params* p, const uint8_t* mask, const T* fA, T* fB, dou
                         orc_collide_mlp(p->mlp, 1.0 / double(p->omega), g, 1, nullptr);
                         for (int q = 0; q < Q; ++q) f[q] = T(g[q]);
                     } else {
-                        collide<T>(p->model, f, T(p->omega), p->les, T(p->cs), T(p->dpdy));
+                        /* DI3:1358: the body force acts only up to DYNY1 */
+                        const T dp = (p->dyn_y1 > 0 && y > p->dyn_y1) ? T(0) : T(p->dpdy);
+                        collide<T>(p->model, f, T(p->omega), p->les, T(p->cs), dp);
                     }
                     if (p->stats_on && av_u) {
                         /* vel_av / vel_fluc (LR7:1018-1058) */
@@ -598,22 +600,28 @@ void orc_lid(float* f, int n, int face, float ux, float uy, float uz, int quirk)
  * (zero at bounce-back nodes).  kind 0: mrt_meq + InvertMoments (LR7);
  * kind 1: BGK equilibrium (DI3); kind 2: BGK equilibrium on every node,
  * solids included (CPU_3D/CPU_3D.cpp:1226-1308). */
-void orc_init(const orc_params* p, const uint8_t* mask, float* f, int kind, float u0) {
+void orc_init_axis(const orc_params* p, const uint8_t* mask, float* f, int kind, float u0, int axis) {
     const long N = long(p->nx) * p->ny * p->nz;
 #pragma omp parallel for schedule(static)
     for (long c = 0; c < N; ++c) {
         /* kind 2: CPU_3D initialises every node, solids included, at u0 */
         float u = (kind != 2 && (mask[c] == ORC_WALL || mask[c] == ORC_BODY)) ? 0.f : u0;
+        float v3[3] = {0.f, 0.f, 0.f};
+        v3[axis] = u;
         float ff[Q];
         if (kind == 0) {
             float meq[Q];
-            meq_lr7<float>(meq, 1.f, u, 0.f, 0.f);
+            meq_lr7<float>(meq, 1.f, v3[0], v3[1], v3[2]);
             invert(meq, ff);
         } else {
-            for (int q = 0; q < Q; ++q) ff[q] = feq_bgk<float>(q, 1.f, u, 0.f, 0.f);
+            for (int q = 0; q < Q; ++q) ff[q] = feq_bgk<float>(q, 1.f, v3[0], v3[1], v3[2]);
         }
         for (int q = 0; q < Q; ++q) f[q * N + c] = ff[q];
     }
+}
+
+void orc_init(const orc_params* p, const uint8_t* mask, float* f, int kind, float u0) {
+    orc_init_axis(p, mask, f, kind, u0, 0);
 }
 
 void orc_step(const orc_params* p, const uint8_t* mask, const float* fA, float* fB, double* force3,
@@ -842,6 +850,21 @@ void orc_mask_cavity(uint8_t* mask, int nx, int ny, int nz, int lid_face) {
                 if (on_lid) v = ORC_LID;
                 else if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || z == 0 || z == nz - 1)
                     v = ORC_WALL;
+                mask[(long(z) * ny + y) * nx + x] = uint8_t(v);
+            }
+}
+
+void orc_mask_dyninlet(uint8_t* mask, int nx, int ny, int nz, float ox, float oy, float r, int trip) {
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                int v = ORC_FLUID;
+                if (trip) {
+                    if (std::fabs(float(x) - ox) < r && std::fabs(float(y) - oy) < r) v = ORC_BODY;
+                    if (std::fabs(float(x) - ox - 3.f) < r && std::fabs(float(y) - oy - 3.f) < r && z == 10)
+                        v = ORC_BODY;
+                }
+                if (x == 0 || x == nx - 1) v = ORC_WALL;
                 mask[(long(z) * ny + y) * nx + x] = uint8_t(v);
             }
 }

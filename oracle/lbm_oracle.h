@@ -79,6 +79,9 @@ typedef struct {
      * of fluid and boundary nodes takes nu_t from this MLP parameter vector
      * (MRT at tau0 + 3 nu_t) instead of the model / LES settings */
     const float* mlp;
+    /* dynamic inlet (DI3:1358): no body force for y > dyn_y1; a large value
+     * switches the cut off */
+    int dyn_y1;
 } orc_params;
 
 typedef struct {
@@ -121,6 +124,12 @@ void orc_mask_channel(uint8_t* mask, int nx, int ny, int nz, int body_shape,
 void orc_mask_fine(uint8_t* mask, int nx, int ny, int nz, float x0, float y0, float z0,
                    float h, int body_shape, float ox, float oy, float r);
 void orc_mask_cavity(uint8_t* mask, int nx, int ny, int nz, int lid_face);
+/* DI3's ImageFcn (DI3:72-90): trip blocks around (ox, oy) of half-width r,
+ * the second shifted by 3 and only in z = 10, while trip != 0; walls at
+ * x = 0 and nx - 1 */
+void orc_mask_dyninlet(uint8_t* mask, int nx, int ny, int nz, float ox, float oy, float r, int trip);
+/* orc_init with the initial velocity along axis (0 x, 1 y, 2 z) */
+void orc_init_axis(const orc_params* p, const uint8_t* mask, float* f, int kind, float u0, int axis);
 
 /* helpers */
 double orc_mass(const float* f, const uint8_t* mask, int ncell);

@@ -37,7 +37,8 @@ class Params(ctypes.Structure):
                 ("start_fluc", ctypes.c_int), ("stats_weight", _F), ("exp_x0", ctypes.c_int),
                 ("exp_y0", ctypes.c_int), ("exp_nx", ctypes.c_int), ("exp_ny", ctypes.c_int),
                 ("noise_amp", _F), ("noise_seed", ctypes.c_uint32), ("pull_clamp", ctypes.c_int),
-                ("lid_quirk", ctypes.c_int), ("halfway", ctypes.c_int), ("mlp", ctypes.c_void_p)]
+                ("lid_quirk", ctypes.c_int), ("halfway", ctypes.c_int), ("mlp", ctypes.c_void_p),
+                ("dyn_y1", ctypes.c_int)]
 
 
 class Refine(ctypes.Structure):

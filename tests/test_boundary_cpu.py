@@ -94,3 +94,16 @@ def test_masks_of_every_geometry(product):
     circle = (x - np.float32(15.5)) ** 2 + (y - np.float32(9.5)) ** 2 < np.float32(16.0)
     inner = (x > 0) & (x < 39) & (y > 0) & (y < 19)
     assert np.array_equal((m[0] == 2) & inner, circle & inner)
+
+
+def test_checkpoint_rejects_other_files(product, tmp_path):
+    """lbm_create_from_state reads the file's header before any device work"""
+    import ctypes
+
+    lib = product.library()
+    bad = tmp_path / "x.ckpt"
+    bad.write_bytes(b"not a checkpoint at all")
+    h = ctypes.c_void_p()
+    assert lib.lbm_create_from_state(str(bad).encode(), ctypes.byref(h)) == 3
+    assert b"not a checkpoint" in lib.lbm_last_error()
+    assert lib.lbm_create_from_state(str(tmp_path / "missing").encode(), ctypes.byref(h)) == 1

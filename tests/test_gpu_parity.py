@@ -391,3 +391,84 @@ def test_errors_are_reported(product):
         lbm.Solver(lbm.make_inputs(64, 24, 4, refinement=1, lr_dims=(32, 32, 6), lr_factor=0.5,
                                    lr_origin=(12.25, 4.25, -0.75)))
     assert e.value.code == 4
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp16"])
+def test_checkpoint_restart_is_bit_exact(product, tmp_path, prec):
+    """stop after 40 steps, restart from the checkpoint, run 40 more: the
+    same populations, force history and statistics as never stopping"""
+    lbm = product
+    text = _chan_inputs(lbm, 100, precision=prec, inlet_noise=0.01, velav=1, start_velav=10, start_velfluc=30,
+                        bounceback="halfway")
+    ck = tmp_path / "run.ckpt"
+    with lbm.Solver(text) as s:
+        s.step(40)
+        s.save_state(ck)
+        s.step(40)
+        f1, F1, st1 = s.populations(), s.forces(), s.stats()
+    with lbm.Solver.from_state(ck) as r:
+        assert r.time == 40
+        r.step(40)
+        np.testing.assert_array_equal(r.populations(), f1)
+        np.testing.assert_array_equal(r.forces(), F1)
+        np.testing.assert_array_equal(r.stats(), st1)
+    with lbm.Solver(text) as r2:
+        r2.step(3)          # any state: the checkpoint replaces it
+        r2.restore_state(ck)
+        r2.step(40)
+        np.testing.assert_array_equal(r2.populations(), f1)
+    with lbm.Solver(_chan_inputs(lbm, 100, precision="fp32")) as other:
+        if prec != "fp32":
+            with pytest.raises(lbm.LbmError):
+                other.restore_state(ck)
+
+
+def test_dynamic_inlet_vs_oracle(product):
+    """DI3's dynamic-inlet duct (64x124x20, walls at x = 0 and 63, periodic
+    in y and z, DI3 MRT with the body force dpdy below DYNY1): trip blocks
+    until t = 50, then the P-control of the plane-mean v every 20 steps after
+    t = 60 updates dpdy on the device.  Against the oracle running the same
+    loop with the control restated on the host"""
+    from oracle_bindings import Params, oracle, ptr
+
+    lbm = product
+    nx, ny, nz, steps = 64, 124, 20, 150
+    y1, every, start, trip_end, kp, dpdy0, umax = 123, 20, 60, 50, 2.0, -5.16e-7, 0.06
+    text = lbm.make_inputs(nx, ny, nz, obst1=(31.5, 92.5, 0.0), r1=31.0, obst2=(25.5, 25.5, 0.0), r2=10.0,
+                           re=5400.0, umax=umax, tmax=steps, les=1, cs=0.02, model="MRT_DI3", dpdy=dpdy0,
+                           geometry="dyninlet", dyny1=y1, dyn_every=every, dyn_start=start, trip_end=trip_end, kp=kp)
+    with lbm.Solver(text) as s:
+        om = s.params()["omega"]
+        s.step(steps)
+        f, mask, hist = s.populations(), s.mask(), s.dyn_history()
+    o = oracle()
+    m = np.zeros((nz, ny, nx), np.uint8)
+    o.orc_mask_dyninlet(ptr(m), nx, ny, nz, ctypes.c_float(25.5), ctypes.c_float(25.5), ctypes.c_float(10.0), 1)
+    p = Params(nx=nx, ny=ny, nz=nz, model=1, les=1, omega=om, cs=0.02, dpdy=dpdy0, u_in=umax, rho_out=1.0,
+               stats_weight=1.0, dyn_y1=y1)
+    fa = np.zeros((19, nz, ny, nx), np.float32)
+    o.orc_init_axis(ctypes.byref(p), ptr(m), ptr(fa), 0, ctypes.c_float(umax), 1)
+    fb = fa.copy()
+    dp = np.float32(dpdy0)
+    want = []
+    from oracle_bindings import CY
+    for t in range(steps):
+        if t == trip_end:
+            o.orc_mask_dyninlet(ptr(m), nx, ny, nz, ctypes.c_float(25.5), ctypes.c_float(25.5), ctypes.c_float(10.0), 0)
+        p.t, p.force_on, p.dpdy = t, 1 if t > 0 else 0, float(dp)
+        f3 = np.zeros(3)
+        o.orc_step(ctypes.byref(p), ptr(m), ptr(fa), ptr(fb), ptr(f3), None, None, None, None, None)
+        fa, fb = fb, fa
+        if t % every == 0 and t > start:
+            v = np.tensordot(CY.astype(np.float64), fa[:, :, y1, :].astype(np.float64), 1)
+            av = np.float32(v.sum() / ((nx - 2) * nz))
+            dp = np.float32(dp + np.float32((av - np.float32(umax)) / np.float32(umax)) * np.float32(kp) *
+                            np.float32(abs(dpdy0)))
+            want.append((t, av, dp))
+    want = np.array(want, np.float64)
+    assert hist.shape == want.shape and np.array_equal(hist[:, 0], want[:, 0])
+    np.testing.assert_allclose(hist[:, 1], want[:, 1], rtol=1e-5)
+    np.testing.assert_allclose(hist[:, 2], want[:, 2], rtol=1e-4)
+    assert abs(hist[-1, 2] - dpdy0) > 1e-3 * abs(dpdy0)            # the control acted
+    err, _ = _compare(f, fa, mask)
+    assert err < RTOL
