@@ -213,7 +213,7 @@ def cpu_baseline(max_samples: int = 1) -> dict:
             secs += sec
         steps = 24 if binary.name.endswith("long") else 8
         return dict(value=statistics.mean(vals), unit="MLUPS", cores=1, kind="reference",
-                    sample=f"CPU_3D/CPU_3D.cpp (staged, g++ -O3 -march=native), 512x128x128, {steps} steps "
+                    sample=f"CPU_3D/CPU_3D.cpp (staged, g++ -O3), 512x128x128, {steps} steps "
                            f"x {len(vals)} run(s), {secs:.1f} s of loop time; its lid-cavity MRT at the same shape")
     sys.path.insert(0, str(ROOT / "tests"))
     import numpy as np
@@ -256,7 +256,7 @@ def reference_arm(args, world, rank):
     steps = 24 if binary.name.endswith("long") else 8
     value = statistics.mean(vals)
     base = dict(value=value, unit="MLUPS", cores=1, kind="reference",
-                sample=f"CPU_3D/CPU_3D.cpp (serial, g++ -O3 -march=native), 512x128x128, {steps} steps x "
+                sample=f"CPU_3D/CPU_3D.cpp (serial, g++ -O3), 512x128x128, {steps} steps x "
                        f"{samples} run(s), {secs:.1f} s of loop time")
     line = dict(metric="MLUPS", value=value, unit="MLUPS", impl="reference", n_gpus=args.gpus, steps=args.steps,
                 warmup=args.warmup, ms_per_step=1e3 * CELLS / (value * 1e6), higher_is_better=True, scaling="weak",

@@ -23,7 +23,9 @@ __all__ = ["Solver", "LbmError", "library", "make_inputs", "normalize_inputs", "
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "_build" / "liblbm_gb300.so"
 
-NODE = dict(FLUID=0, WALL=1, BODY=2, WEST_INLET=3, EAST_OUTLET=4, SOUTH_INLET=5, NORTH_OUTLET=6, LID=7)
+NODE = dict(FLUID=0, WALL=1, BODY=2, WEST_INLET=3, EAST_OUTLET=4, SOUTH_INLET=5, NORTH_OUTLET=6, LID=7,
+            DIR_WEST=8, NEU_EAST=9, NEU_EAST_REG=10, XSYM_TOP=11, XSYM_BOT=12, YSYM_TOP=13, YSYM_BOT=14,
+            ZSYM_TOP=15, ZSYM_BOT=16, WEST_REG=17)
 MODELS = dict(MRT=0, MRT_DI3=1, BGK=2, MRT_CPU3D=3)
 
 _P = ctypes.c_void_p
@@ -162,7 +164,10 @@ def make_inputs(nx: int, ny: int, nz: int, *, obst1=(0.0, 0.0, 0.0), r1=1.0, obs
     keys (geometry, precision, tau, lid, noise, ...) are passed as keyword
     arguments named after the record keys: geometry="cavity", tau=0.6,
     lid_velocity=(0.05, 0, 0), lid_face="+z", precision="fp16",
-    inlet_noise=0.01, seed=12345, velav=1, init=1, init_velocity=0.0.
+    inlet_noise=0.01, seed=12345, velav=1, init=1, init_velocity=0.0,
+    faces=("DIR_WEST", "NEU_EAST", "YSYM_BOT", "YSYM_TOP", "-", "-") (a node
+    type name from NODE per face x = 0, x = nx-1, y = 0, y = ny-1, z = 0,
+    z = nz-1; "-" keeps the geometry's own).
     """
     def tup(t):
         return "(" + ",".join(_fmt(v) for v in t) + ")"
@@ -201,10 +206,12 @@ def make_inputs(nx: int, ny: int, nz: int, *, obst1=(0.0, 0.0, 0.0), r1=1.0, obs
              "init": "Init:", "init_velocity": "Init velocity:", "order": "ORDER:", "fc_top_zflip": "FC top zflip:",
              "edge_pull": "EDGE PULL:", "lid_bc": "LID BC:", "bounceback": "BOUNCEBACK:", "sgs": "SGS:",
              "sgs_weights": "SGS weights:", "dyny1": "DYNY1:", "dyn_every": "DYN every:",
-             "dyn_start": "DYN start:", "trip_end": "TRIP end:", "kp": "KP:"}
+             "dyn_start": "DYN start:", "trip_end": "TRIP end:", "kp": "KP:", "faces": "FACES:"}
     for k, v in ext.items():
         if k not in names:
             raise KeyError(f"unknown .inputs extension key {k!r}")
+        if k == "faces" and isinstance(v, (tuple, list)):
+            v = " ".join(v)
         lines.append((names[k], tup(v) if isinstance(v, (tuple, list)) else (v if isinstance(v, str) else _fmt(v))))
     return "".join(f"{k} \t{v}\n" for k, v in lines)
 

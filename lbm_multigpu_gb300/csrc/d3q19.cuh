@@ -18,6 +18,8 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <cmath>
 #include <stdint.h>
 
 #include "lbm_kernels.cuh"
@@ -343,6 +345,207 @@ template <class T> __host__ __device__ __forceinline__ void extrap(int type, T f
     djz *= T(0.1);
 #pragma unroll
     for (int q = 0; q < 19; ++q) f[q] += r + T(cx(q)) * djx + T(cy(q)) * djy + T(cz(q)) * djz;
+}
+
+/* ---- the alternate boundaries (node types DIR_WEST .. WEST_REG) ----
+ * Per-cell restatements with the reference's own arithmetic and edge cases;
+ * ny, nz are the domain's YDIM, ZDIM. */
+
+/* the y/z edge copies shared by CPU_3D's DirichletWest and LR7's
+ * xsymmetry_bot (CPU:417-470, LR7:901-945) */
+template <class T> __host__ __device__ __forceinline__ void west_edges(T f[19], int y, int z, int ny, int nz) {
+    if (y == 0 && z == 0) {
+        f[2] = f[4], f[13] = f[18], f[11] = f[18], f[16] = f[18], f[6] = f[7], f[9] = f[14], f[12] = f[17];
+    } else if (y == 0 && z == nz - 1) {
+        f[4] = f[2], f[11] = f[13], f[18] = f[13], f[16] = f[13], f[6] = f[7], f[14] = f[9], f[17] = f[12];
+    } else if (y == ny - 1 && z == 0) {
+        f[4] = f[2], f[11] = f[16], f[18] = f[16], f[13] = f[16], f[7] = f[6], f[9] = f[14], f[12] = f[17];
+    } else if (y == ny - 1 && z == nz - 1) {
+        f[4] = f[2], f[16] = f[11], f[18] = f[11], f[13] = f[11], f[7] = f[6], f[14] = f[9], f[17] = f[12];
+    } else {
+        if (y == 0) f[2] = f[4], f[11] = f[13], f[16] = f[18], f[8] = f[5];
+        else if (y == ny - 1) f[4] = f[2], f[13] = f[11], f[18] = f[16], f[5] = f[8];
+    }
+}
+
+/* the corresponding copies at the east face (CPU:658-702, LR7:958-1006) */
+template <class T> __host__ __device__ __forceinline__ void east_edges(T f[19], int y, int z, int ny, int nz) {
+    if (y == 0 && z == 0) {
+        f[2] = f[4], f[13] = f[18], f[11] = f[18], f[16] = f[18], f[5] = f[8], f[9] = f[14], f[10] = f[15];
+    } else if (y == 0 && z == nz - 1) {
+        f[2] = f[4], f[11] = f[13], f[18] = f[13], f[16] = f[13], f[5] = f[8], f[14] = f[9], f[15] = f[10];
+    } else if (y == ny - 1 && z == 0) {
+        f[4] = f[2], f[18] = f[16], f[11] = f[16], f[13] = f[16], f[8] = f[5], f[9] = f[14], f[10] = f[15];
+    } else if (y == ny - 1 && z == nz - 1) {
+        f[4] = f[2], f[13] = f[11], f[16] = f[11], f[18] = f[11], f[8] = f[5], f[14] = f[9], f[15] = f[10];
+    } else {
+        if (y == 0) f[2] = f[4], f[11] = f[13], f[16] = f[18], f[5] = f[8];
+        else if (y == ny - 1) f[4] = f[2], f[13] = f[11], f[18] = f[16], f[8] = f[5];
+    }
+}
+
+/* fused multiply-add as CPU_3D writes it (std::fma) */
+template <class T> __host__ __device__ __forceinline__ T lfma(T a, T b, T c) {
+#ifdef __CUDA_ARCH__
+    return fma(a, b, c);
+#else
+    return std::fma(a, b, c);
+#endif
+}
+
+/* DirichletWest (CPU:411-488): edges, then the unknowns from their
+ * opposites with the inlet velocity u (v = w = 0), incompressible */
+template <class T> __host__ __device__ __forceinline__ void dirichlet_west(T f[19], int y, int z, int ny, int nz, T u) {
+    west_edges(f, y, z, ny, nz);
+    if (!((y == 0 || y == ny - 1) && (z == 0 || z == nz - 1))) {
+        if (z == 0) f[9] = f[14], f[10] = f[15], f[11] = f[16], f[13] = f[18];
+        else if (z == nz - 1) f[14] = f[9], f[15] = f[10], f[16] = f[11], f[18] = f[13];
+    }
+    const T v = T(0), w = T(0);
+    f[1] = lfma(T(0.0555555556), T(6) * u, f[3]);
+    f[5] = lfma(T(0.0277777778), T(6) * (u + v), f[7]);
+    f[8] = lfma(T(0.0277777778), T(6) * (u - v), f[6]);
+    f[10] = lfma(T(0.0277777778), T(6) * (u + w), f[17]);
+    f[15] = lfma(T(0.0277777778), T(6) * (u - w), f[12]);
+}
+
+/* the outlet velocity at rho = 1 from the known populations (CPU:649) */
+template <class T> __host__ __device__ __forceinline__ T east_u(const T f[19]) {
+    return -T(1) + (f[0] + f[2] + f[4] + f[9] + f[11] + f[13] + f[14] + f[16] + f[18] +
+                    T(2) * (f[1] + f[8] + f[5] + f[10] + f[15]));
+}
+
+/* NeumannEast_Reg (CPU:570-650): edges (the corner copies of the east face,
+ * the z-face copies without f12/f17), then the unknowns for rho = 1 */
+template <class T> __host__ __device__ __forceinline__ void neumann_east(T f[19], int y, int z, int ny, int nz) {
+    east_edges(f, y, z, ny, nz);
+    if (!((y == 0 || y == ny - 1) && (z == 0 || z == nz - 1))) {
+        if (z == 0) f[9] = f[14], f[10] = f[15], f[11] = f[16], f[13] = f[18];
+        else if (z == nz - 1) f[14] = f[9], f[15] = f[10], f[16] = f[11], f[18] = f[13];
+    }
+    const T u = east_u(f), v = T(0), w = T(0);
+    f[3] = f[1] - T(0.333333333) * u;
+    f[7] = f[5] - T(0.166666667) * (u + v);
+    f[6] = f[8] - T(0.166666667) * (u - v);
+    f[17] = f[10] - T(0.166666667) * (u + w);
+    f[12] = f[15] - T(0.166666667) * (u - w);
+}
+
+/* NeumannEast_Regularized (CPU:1056-1138) as written: rho = 1, u from the
+ * known populations; the unknowns by non-equilibrium bounce-back where four
+ * of the five read their own equilibrium twice (f3 = f1, f7 = f5,
+ * f17 = f10, f12 = f15), then f = feq + Pi_neq projection */
+template <class T> __host__ __device__ __forceinline__ void neumann_east_regularized(T f[19]) {
+    const T rho = T(1), v = T(0), w = T(0);
+    const T u = east_u(f);
+    const T usq = u * u + v * v + w * w;
+    T fe[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const T cu = T(cx(q)) * u + T(cy(q)) * v + T(cz(q)) * w;
+        const T wgt = q == 0 ? T(0.3333333333) : (q <= 4 || q == 9 || q == 14) ? T(0.0555555556) : T(0.0277777778);
+        fe[q] = q == 0 ? wgt * (rho - T(1.5) * usq) : wgt * (rho + T(3) * cu + T(4.5) * cu * cu - T(1.5) * usq);
+    }
+    f[3] = fe[1] + f[1] - fe[1];
+    f[7] = fe[5] + f[5] - fe[5];
+    f[6] = fe[6] + f[8] - fe[8];
+    f[17] = fe[10] + f[10] - fe[10];
+    f[12] = fe[15] + f[15] - fe[15];
+    T n[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) n[q] = f[q] - fe[q];
+    const T p11 = n[1] + n[3] + n[5] + n[6] + n[7] + n[8] + n[10] + n[12] + n[15] + n[17];
+    const T p22 = n[2] + n[4] + n[5] + n[6] + n[7] + n[8] + n[11] + n[13] + n[16] + n[18];
+    const T p33 = n[9] + n[14] + n[10] + n[12] + n[15] + n[17] + n[11] + n[13] + n[16] + n[18];
+    const T p12 = n[5] + n[7] - n[6] - n[8];
+    const T p13 = n[10] + n[17] - n[12] - n[15];
+    const T p23 = n[11] + n[18] - n[13] - n[16];
+    const T a = T(0.666666667), b = T(-0.333333333);
+    f[0] = fe[0] + T(1.5) * (b * p11 + b * p22 + b * p33);
+    f[1] = fe[1] + T(0.25) * (a * p11 + b * p22 + b * p33);
+    f[2] = fe[2] + T(0.25) * (b * p11 + a * p22 + b * p33);
+    f[3] = fe[3] + T(0.25) * (a * p11 + b * p22 + b * p33);
+    f[4] = fe[4] + T(0.25) * (b * p11 + a * p22 + b * p33);
+    f[5] = fe[5] + T(0.125) * (a * p11 + T(2) * p12 + a * p22 + b * p33);
+    f[6] = fe[6] + T(0.125) * (a * p11 + T(2) * (-p12) + a * p22 + b * p33);
+    f[7] = fe[7] + T(0.125) * (a * p11 + T(2) * p12 + a * p22 + b * p33);
+    f[8] = fe[8] + T(0.125) * (a * p11 + T(2) * (-p12) + a * p22 + b * p33);
+    f[9] = fe[9] + T(0.25) * (b * p11 + b * p22 + a * p33);
+    f[10] = fe[10] + T(0.125) * (a * p11 + T(2) * p13 + b * p22 + a * p33);
+    f[11] = fe[11] + T(0.125) * (b * p11 + T(2) * p23 + a * p22 + a * p33);
+    f[12] = fe[12] + T(0.125) * (a * p11 + T(2) * (-p13) + b * p22 + a * p33);
+    f[13] = fe[13] + T(0.125) * (b * p11 + T(2) * (-p23) + a * p22 + a * p33);
+    f[14] = fe[14] + T(0.25) * (b * p11 + b * p22 + a * p33);
+    f[15] = fe[15] + T(0.125) * (a * p11 + T(2) * (-p13) + b * p22 + a * p33);
+    f[16] = fe[16] + T(0.125) * (b * p11 + T(2) * (-p23) + a * p22 + a * p33);
+    f[17] = fe[17] + T(0.125) * (a * p11 + T(2) * p13 + b * p22 + a * p33);
+    f[18] = fe[18] + T(0.125) * (b * p11 + T(2) * p23 + a * p22 + a * p33);
+}
+
+/* xsymmetry_bot / xsymmetry_top (LR7:899-1016): specular planes at x = 0
+ * and x = nx - 1 with their y/z edge copies */
+template <class T> __host__ __device__ __forceinline__ void xsym_bot(T f[19], int y, int z, int ny, int nz) {
+    west_edges(f, y, z, ny, nz);
+    f[1] = f[3], f[5] = f[6], f[8] = f[7], f[10] = f[12], f[15] = f[17];
+}
+template <class T> __host__ __device__ __forceinline__ void xsym_top(T f[19], int y, int z, int ny, int nz) {
+    east_edges(f, y, z, ny, nz);
+    f[3] = f[1], f[6] = f[5], f[7] = f[8], f[12] = f[10], f[17] = f[15];
+}
+
+/* ysymmetry_top / _bot (CPU:861-916), zsymmetry_top / _bot (CPU:917-972) */
+template <class T> __host__ __device__ __forceinline__ void ysym(T f[19], bool top, int z, int nz) {
+    if (z == 0) f[9] = f[14], f[10] = f[15], f[11] = f[16], f[12] = f[17], f[13] = f[18];
+    if (z == nz - 1) f[14] = f[9], f[15] = f[10], f[16] = f[11], f[17] = f[12], f[18] = f[13];
+    if (top) f[4] = f[2], f[7] = f[6], f[8] = f[5], f[13] = f[11], f[18] = f[16];
+    else f[2] = f[4], f[6] = f[7], f[5] = f[8], f[11] = f[13], f[16] = f[18];
+}
+template <class T> __host__ __device__ __forceinline__ void zsym(T f[19], bool top, int y, int ny) {
+    if (y == 0) f[2] = f[4], f[6] = f[7], f[5] = f[8], f[11] = f[13], f[16] = f[18];
+    if (y == ny - 1) f[4] = f[2], f[7] = f[6], f[8] = f[5], f[13] = f[11], f[18] = f[16];
+    if (top) f[14] = f[9], f[15] = f[10], f[16] = f[11], f[17] = f[12], f[18] = f[13];
+    else f[9] = f[14], f[10] = f[15], f[11] = f[16], f[12] = f[17], f[13] = f[18];
+}
+
+/* West_Reg (BC1/LRMultiGPU7.cu:789-870): the node's own populations keep
+ * rho and every non-momentum moment, the momentum becomes (u, 0, w) with
+ * w = 0.01 at t = 1000, 2000, 3000 (the reference's perturbation).  The
+ * reference rebuilds the node from all 19 MRT moments; with only the
+ * momentum rows changed that is f += c . (j_target - j) / 10 (the momentum
+ * columns of the inverse transform are c / 10), same in real arithmetic,
+ * FP32 results within rounding of the reference's */
+template <class T> __host__ __device__ __forceinline__ void west_reg(T f[19], T u, int t) {
+    const T w = (t == 1000 || t == 2000 || t == 3000) ? T(0.01) : T(0);
+    T jx = 0, jy = 0, jz = 0;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        if (cx(q)) jx += T(cx(q)) * f[q];
+        if (cy(q)) jy += T(cy(q)) * f[q];
+        if (cz(q)) jz += T(cz(q)) * f[q];
+    }
+    const T dx = T(0.1) * (u - jx), dy = T(0.1) * (T(0) - jy), dz = T(0.1) * (w - jz);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) f[q] += T(cx(q)) * dx + T(cy(q)) * dy + T(cz(q)) * dz;
+}
+
+/* the dispatch for a node of an alternate-boundary type */
+template <class T>
+__host__ __device__ __forceinline__ void alt_boundary(int type, T f[19], int x, int y, int z, int nx, int ny, int nz,
+                                                      T u_in, int t) {
+    (void)x, (void)nx;
+    switch (type) {
+        case DIR_WEST: dirichlet_west(f, y, z, ny, nz, u_in); break;
+        case NEU_EAST: neumann_east(f, y, z, ny, nz); break;
+        case NEU_EAST_REG: neumann_east_regularized(f); break;
+        case XSYM_TOP: xsym_top(f, y, z, ny, nz); break;
+        case XSYM_BOT: xsym_bot(f, y, z, ny, nz); break;
+        case YSYM_TOP: ysym(f, true, z, nz); break;
+        case YSYM_BOT: ysym(f, false, z, nz); break;
+        case ZSYM_TOP: zsym(f, true, y, ny); break;
+        case ZSYM_BOT: zsym(f, false, y, ny); break;
+        case WEST_REG: west_reg(f, u_in, t); break;
+        default: break;
+    }
 }
 
 /* Regularised velocity boundary for a moving lid on any face (the reference's

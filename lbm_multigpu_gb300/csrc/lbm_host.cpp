@@ -99,6 +99,11 @@ struct Config {
     int dyn_every = 100, dyn_start = 10000;
     int trip_end = 5000;
     std::string sgs_weights;        /* "SGS weights: <file>" of float32 parameters */
+    /* "FACES: west east south north bottom top": a node type per box face
+     * (x = 0, x = nx-1, y = 0, y = ny-1, z = 0, z = nz-1), "-" keeps the
+     * geometry's own; y faces over z faces over x faces at edges */
+    int faces[6] = {-1, -1, -1, -1, -1, -1};
+    bool faces_set = false;
     /* older records spell the LES line "Smagorinski LES: YES/NO"; DynInlet
      * records add "KP" (the inlet P-control gain, MRTtest/DynInlet3.cu:26) */
     bool les_yesno = false;
@@ -113,6 +118,28 @@ struct Config {
 std::string trim(const std::string& s) {
     size_t a = s.find_first_not_of(" \t\r\n"), b = s.find_last_not_of(" \t\r\n");
     return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+}
+
+/* node type names, by code */
+const char* const NODE_NAMES[NODE_TYPES] = {"FLUID",    "WALL",     "BODY",         "WEST_INLET", "EAST_OUTLET",
+                                            "SOUTH_INLET", "NORTH_OUTLET", "LID",   "DIR_WEST",   "NEU_EAST",
+                                            "NEU_EAST_REG", "XSYM_TOP", "XSYM_BOT", "YSYM_TOP",   "YSYM_BOT",
+                                            "ZSYM_TOP", "ZSYM_BOT", "WEST_REG"};
+
+bool parse_faces(const std::string& v, int out[6]) {
+    std::istringstream in(v);
+    std::string tok;
+    int n = 0;
+    while (in >> tok) {
+        if (n == 6) return false;
+        int code = -2;
+        if (tok == "-") code = -1;
+        for (int i = 0; i < NODE_TYPES; ++i)
+            if (tok == NODE_NAMES[i]) code = i;
+        if (code == -2) return false;
+        out[n++] = code;
+    }
+    return n == 6;
 }
 
 bool parse_xyz_int(const std::string& v, int out[3]) {
@@ -213,6 +240,7 @@ int parse_inputs(const char* text, Config& c) {
         else if (key == "DYN every") I(c.dyn_every);
         else if (key == "DYN start") I(c.dyn_start);
         else if (key == "TRIP end") I(c.trip_end);
+        else if (key == "FACES") { ok = parse_faces(val, c.faces); c.faces_set = true; }
         else if (key == "LID BC") {
             ok = (val == "cpu3d" || val == "regularized");
             c.lid_quirk = val == "cpu3d";
@@ -313,6 +341,8 @@ std::string value_of(const Config& c, const std::string& key, float omega, float
     else if (key == "DYN every") o << c.dyn_every;
     else if (key == "DYN start") o << c.dyn_start;
     else if (key == "TRIP end") o << c.trip_end;
+    else if (key == "FACES")
+        for (int i = 0; i < 6; ++i) o << (i ? " " : "") << (c.faces[i] < 0 ? "-" : NODE_NAMES[c.faces[i]]);
     return o.str();
 }
 
@@ -375,6 +405,7 @@ std::string write_inputs(const Config& c, float omega, float omegaLR) {
     if (c.dyn_every != d.dyn_every) line("DYN every: ", "DYN every");
     if (c.dyn_start != d.dyn_start) line("DYN start: ", "DYN start");
     if (c.trip_end != d.trip_end) line("TRIP end: ", "TRIP end");
+    if (c.faces_set) line("FACES: ", "FACES");
     return o.str();
 }
 
@@ -384,12 +415,19 @@ std::string write_inputs(const Config& c, float omega, float omegaLR) {
 
 int body_shape(const std::string& g) {
     if (g == "channel_square") return 1;
-    if (g == "channel_circle") return 2;
+    if (g == "channel_circle" || g == "duct") return 2;
     return 0;
 }
 
+/* the faces of a "duct" without a FACES line: CPU_3D's cylinder duct
+ * (CPU:39-63, the variant with walls on the y and z faces), its Dirichlet
+ * inlet and its outlet for rho = 1 */
+constexpr int DUCT_FACES[6] = {DIR_WEST, NEU_EAST, WALL, WALL, WALL, WALL};
+
 /* channel programs (LR7:88-127): body, then walls y = 0 / ny-1, inlet x = 0,
- * outlet x = nx-1 (walls override inlet/outlet, both override the body) */
+ * outlet x = nx-1 (walls override inlet/outlet, both override the body).
+ * Then the FACES line, or a duct's default faces: x faces, then z, then y,
+ * so that y faces hold the edges (the precedence of CPU_3D's ImageFcn). */
 void mask_base(const Config& c, std::vector<uint8_t>& m, int t = 0) {
     const int nx = c.nx, ny = c.ny, nz = c.nz;
     m.assign(size_t(nx) * ny * nz, FLUID);
@@ -397,6 +435,7 @@ void mask_base(const Config& c, std::vector<uint8_t>& m, int t = 0) {
     const bool channel = c.geometry.rfind("channel", 0) == 0;
     const bool cavity = c.geometry == "cavity";
     const bool dyn = c.geometry == "dyninlet";
+    const int* faces = c.faces_set ? c.faces : c.geometry == "duct" ? DUCT_FACES : nullptr;
     for (int z = 0; z < nz; ++z)
         for (int y = 0; y < ny; ++y)
             for (int x = 0; x < nx; ++x) {
@@ -428,6 +467,12 @@ void mask_base(const Config& c, std::vector<uint8_t>& m, int t = 0) {
                     bool on_lid = (c.lid_face % 2 == 0) ? p[a] == 0 : p[a] == n[a] - 1;
                     if (on_lid) v = LID;
                     else if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || z == 0 || z == nz - 1) v = WALL;
+                }
+                if (faces) {
+                    const int on[6] = {x == 0, x == nx - 1, z == 0, z == nz - 1, y == 0, y == ny - 1};
+                    const int fi[6] = {0, 1, 4, 5, 2, 3};
+                    for (int k = 0; k < 6; ++k)
+                        if (on[k] && faces[fi[k]] >= 0) v = uint8_t(faces[fi[k]]);
                 }
                 m[(size_t(z) * ny + y) * nx + x] = v;
             }
@@ -469,6 +514,7 @@ struct LevelState {
     double* fpart = nullptr;        /* per-block force partials */
     unsigned* done = nullptr;       /* blocks finished in the force kernel (reset by its last block) */
     bool has_lid = false;           /* the mask has LID nodes */
+    bool has_xbc = false;           /* the mask has alternate-boundary nodes */
     uint32_t* links = nullptr;      /* device, per node: bit q = pull source of q is solid */
 };
 
@@ -587,6 +633,7 @@ int upload_mask(lbm_handle* h, int level) {
     std::vector<unsigned> list;
     std::vector<uint32_t> links(halfway ? size_t(L.qstride) : 0, 0u);
     s.has_lid = std::find(s.hmask.begin(), s.hmask.end(), uint8_t(LID)) != s.hmask.end();
+    s.has_xbc = std::any_of(s.hmask.begin(), s.hmask.end(), [](uint8_t v) { return v >= DIR_WEST; });
     for (int z = 0; z < L.nz; ++z)
         for (int y = 0; y < L.ny; ++y)
             for (int x = 0; x < L.nx; ++x) {
@@ -662,6 +709,7 @@ StepParams base_params(const lbm_handle* h, int level) {
     p.pull_clamp = c.pull_clamp;
     p.halfway = c.halfway;
     p.has_lid = h->lv[level].has_lid ? 1 : 0;
+    p.has_xbc = h->lv[level].has_xbc ? 1 : 0;
     p.stats_on = c.velav;
     p.start_av = c.start_av;
     p.start_fluc = c.start_fluc;
@@ -897,7 +945,7 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
     if (model < 0) return fail(LBM_ERR_CONFIG, "MODEL '%s' is not one of MRT, MRT_DI3, BGK, MRT_CPU3D", c.model.c_str());
     const int storage = storage_id(c.precision);
     if (storage < 0) return fail(LBM_ERR_CONFIG, "PRECISION '%s' is not one of fp32, fp16, bf16, fp64", c.precision.c_str());
-    static const char* geoms[] = {"channel_square", "channel_circle", "channel", "cavity", "periodic", "dyninlet"};
+    static const char* geoms[] = {"channel_square", "channel_circle", "channel", "cavity", "periodic", "dyninlet", "duct"};
     if (std::find(std::begin(geoms), std::end(geoms), c.geometry) == std::end(geoms))
         return fail(LBM_ERR_CONFIG, "GEOMETRY '%s' is not supported", c.geometry.c_str());
     if (c.refinement) {
@@ -918,8 +966,10 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
             return fail(LBM_ERR_CONFIG, "refinement patch does not fit in the base grid");
         if (c.lrx < 2 * lev + 2 || c.lry < 2 * lev + 2) return fail(LBM_ERR_CONFIG, "refinement patch too small");
     }
-    if (c.sgs_mlp && (c.refinement || c.geometry == "cavity" || c.pull_clamp || storage == STORE_F64))
-        return fail(LBM_ERR_CONFIG, "SGS mlp runs on channel and periodic levels without refinement, FP32/FP16/BF16");
+    if (c.sgs_mlp && (c.refinement || c.geometry == "cavity" || c.geometry == "duct" || c.faces_set || c.pull_clamp ||
+                      storage == STORE_F64))
+        return fail(LBM_ERR_CONFIG, "SGS mlp runs on channel, dyninlet and periodic levels without refinement or "
+                                    "FACES, FP32/FP16/BF16");
     std::vector<float> sgs_params;
     if (!c.sgs_weights.empty()) {
         std::ifstream in(c.sgs_weights, std::ios::binary);
@@ -953,7 +1003,7 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
             return bail(fail(LBM_ERR_CUDA, "cannot create the force stream"));
     }
     /* reference velocity of the FP16/BF16 offsets: the inlet velocity of a channel */
-    const float u_ref = c.geometry.rfind("channel", 0) == 0 ? c.umax : 0.f;
+    const float u_ref = c.geometry.rfind("channel", 0) == 0 || c.geometry == "duct" ? c.umax : 0.f;
     if ((rc = alloc_level(h->lv[0], c.nx, c.ny, c.nz, storage, c.velav != 0, u_ref))) return bail(rc);
     mask_base(c, h->lv[0].hmask);
     h->trip_in_mask = c.geometry == "dyninlet" && c.trip_end > 0;
@@ -1063,7 +1113,7 @@ int lbm_set_mask(lbm_handle* h, int level, const uint8_t* mask) {
     if (int rc = check_level(h, level)) return rc;
     if (!mask) return fail(LBM_ERR_ARG, "mask is null");
     for (size_t i = 0; i < h->lv[level].hmask.size(); ++i)
-        if (mask[i] > LID) return fail(LBM_ERR_ARG, "mask value %d at %zu is not a node type", int(mask[i]), i);
+        if (mask[i] >= NODE_TYPES) return fail(LBM_ERR_ARG, "mask value %d at %zu is not a node type", int(mask[i]), i);
     memcpy(h->lv[level].hmask.data(), mask, h->lv[level].hmask.size());
     return upload_mask(h, level);
 }
@@ -1582,6 +1632,7 @@ int lbm_stream_collide_f32(const float* fA, float* fB, const uint8_t* mask, int 
     p.stats_weight = 1.f;
     p.dyn_y1 = 1 << 30;
     p.has_lid = 1; /* the caller's mask may hold any node type */
+    p.has_xbc = 1;
     CUDA_TRY(launch_stream_collide(L, p, fA, fB, mask, nullptr, nullptr, (cudaStream_t)cuda_stream));
     return LBM_OK;
 }

@@ -60,7 +60,7 @@ template <> struct Fmt<__nv_bfloat16> {
 /* FEAT: compile-time features, chosen at launch from the configuration and
  * the node types present, so a channel kernel carries no lid code (whose
  * 19-entry temporaries would otherwise set every variant's register count) */
-constexpr int FEAT_HALFWAY = 1, FEAT_LID = 2, FEAT_CLAMP = 4;
+constexpr int FEAT_HALFWAY = 1, FEAT_LID = 2, FEAT_CLAMP = 4, FEAT_XBC = 8;
 /* the node update of one node (x, y, z) inside the level; shared by the
  * one-node-per-thread kernel and the slow path of the paired kernel */
 template <class S, int FEAT>
@@ -135,6 +135,8 @@ __device__ __forceinline__ void sc_node(const Level& L, const StepParams& p, con
             extrap<T>(type, f, T(p.rho_out), uin);
         } else if ((FEAT & FEAT_LID) && type == LID) {
             lid<T>(f, p.lid_face, T(p.lid_u[0]), T(p.lid_u[1]), T(p.lid_u[2]), p.lid_quirk != 0);
+        } else if ((FEAT & FEAT_XBC) && type >= DIR_WEST) {
+            alt_boundary<T>(type, f, x, y, z, L.nx, L.ny, L.nz, T(p.u_in), p.t);
         }
         T dp = T(p.dpdy_dev ? *p.dpdy_dev : p.dpdy);
         if (y > p.dyn_y1) dp = T(0);
@@ -808,7 +810,8 @@ cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const voi
     if (p.halfway && !links) return cudaErrorInvalidValue;
 
     const dim3 block(SC_BX, SC_BY), grid = sc_grid(L);
-    const int feat = (p.halfway ? FEAT_HALFWAY : 0) | (p.has_lid ? FEAT_LID : 0) | (p.pull_clamp ? FEAT_CLAMP : 0);
+    const int feat = (p.halfway ? FEAT_HALFWAY : 0) | (p.has_lid ? FEAT_LID : 0) | (p.pull_clamp ? FEAT_CLAMP : 0) |
+                     (p.has_xbc ? FEAT_XBC : 0);
 #define LBM_SC(FT) \
     LBM_DISPATCH(L.storage, (k_stream_collide<S, FT><<<grid, block, 0, s>>>(L, p, (const S*)fA, (S*)fB, mask, stats, \
                                                                              mom_export, links)))
@@ -820,7 +823,17 @@ cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const voi
         case 4: LBM_SC(4); break;
         case 5: LBM_SC(5); break;
         case 6: LBM_SC(6); break;
-        default: LBM_SC(7); break;
+        case 7: LBM_SC(7); break;
+        /* alternate boundaries, with every combination of the others */
+        case 8: LBM_SC(8); break;
+        case 9: LBM_SC(9); break;
+        case 10: LBM_SC(10); break;
+        case 11: LBM_SC(11); break;
+        case 12: LBM_SC(12); break;
+        case 13: LBM_SC(13); break;
+        case 14: LBM_SC(14); break;
+        case 15: LBM_SC(15); break;
+        default: return cudaErrorInvalidValue;
     }
 #undef LBM_SC
     return cudaGetLastError();
@@ -868,7 +881,7 @@ template <class S, bool HW> static cudaError_t sc_mlp_t(const Level& L, const St
 cudaError_t launch_stream_collide_mlp(const Level& L, const StepParams& p, const void* fA, void* fB,
                                       const uint8_t* mask, float* stats, const uint32_t* links, const void* blob,
                                       int* err, cudaStream_t s) {
-    if ((p.halfway && !links) || !blob || !err || p.has_lid || p.pull_clamp || p.exp_nx > 0)
+    if ((p.halfway && !links) || !blob || !err || p.has_lid || p.has_xbc || p.pull_clamp || p.exp_nx > 0)
         return cudaErrorInvalidValue;
     switch (L.storage) {
         case STORE_F32:

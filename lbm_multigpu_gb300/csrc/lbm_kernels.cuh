@@ -21,7 +21,21 @@ enum NodeType : uint8_t {
     EAST_OUTLET = 4,
     SOUTH_INLET = 5,
     NORTH_OUTLET = 6,
-    LID = 7
+    LID = 7,
+    /* the alternate boundaries of CPU_3D (CPU:411-1140), LR7's x symmetry
+     * planes (LR7:899-1016) and BC1's West_Reg (BC1/LRMultiGPU7.cu:789):
+     * applied to the pulled populations before the collision */
+    DIR_WEST = 8,       /* DirichletWest, CPU_3D im 3 */
+    NEU_EAST = 9,       /* NeumannEast_Reg, im 14 */
+    NEU_EAST_REG = 10,  /* NeumannEast_Regularized, im 54 */
+    XSYM_TOP = 11,      /* xsymmetry_top, x = nx - 1 */
+    XSYM_BOT = 12,      /* xsymmetry_bot, x = 0 */
+    YSYM_TOP = 13,      /* ysymmetry_top, im 21 */
+    YSYM_BOT = 14,      /* ysymmetry_bot, im 22 */
+    ZSYM_TOP = 15,      /* zsymmetry_top, im 23 */
+    ZSYM_BOT = 16,      /* zsymmetry_bot, im 24 */
+    WEST_REG = 17,      /* BC1 West_Reg */
+    NODE_TYPES = 18
 };
 
 /* collision models: LR7 mrt_collide, DynInlet3's MRT (bgk_meq + AddForce),
@@ -50,6 +64,7 @@ struct StepParams {
      * no body force (DI3:1358) */
     const float* dpdy_dev;
     int dyn_y1;
+    int has_xbc; /* the level holds alternate-boundary nodes (DIR_WEST ..) */
     float u_in, rho_out;
     float lid_u[3];
     int lid_face;

@@ -21,6 +21,8 @@
 
 namespace {
 
+
+
 constexpr int Q = 19;
 constexpr int CX[Q] = {0, 1, 0, -1, 0, 1, -1, -1, 1, 0, 1, 0, -1, 0, 0, 1, 0, -1, 0};
 constexpr int CY[Q] = {0, 0, 1, 0, -1, 1, 1, -1, -1, 0, 0, 1, 0, -1, 0, 0, 1, 0, -1};
@@ -274,6 +276,125 @@ template <class T> inline void extrap(int kind, T* f, T rho_bc, T u_in) {
  * DirichletWest_Regularized (CPU:974-1054) written for any face: density from
  * the known populations, unknown populations by non-equilibrium bounce-back,
  * then f = feq + w_q 4.5 (c_q c_q - I/3) : Pi_neq. */
+/* ---- alternate boundaries, restated from CPU_3D/CPU_3D.cpp:411-1140,
+ * LRTurbTest/LRMultiGPU7.cu:899-1016 and BC1/LRMultiGPU7.cu:789-870 ---- */
+
+/* the y/z edge assignments at a west face (CPU:417-470; LR7:901-945):
+ * each entry {dst, src}; corners first, else the y edges */
+template <class T> void alt_west_edges(T* f, int y, int z, int ny, int nz) {
+    const bool y0 = y == 0, y1 = y == ny - 1, z0 = z == 0, z1 = z == nz - 1;
+    if (y0 && z0) { f[2] = f[4]; f[13] = f[18]; f[11] = f[18]; f[16] = f[18]; f[6] = f[7]; f[9] = f[14]; f[12] = f[17]; }
+    else if (y0 && z1) { f[4] = f[2]; f[11] = f[13]; f[18] = f[13]; f[16] = f[13]; f[6] = f[7]; f[14] = f[9]; f[17] = f[12]; }
+    else if (y1 && z0) { f[4] = f[2]; f[11] = f[16]; f[18] = f[16]; f[13] = f[16]; f[7] = f[6]; f[9] = f[14]; f[12] = f[17]; }
+    else if (y1 && z1) { f[4] = f[2]; f[16] = f[11]; f[18] = f[11]; f[13] = f[11]; f[7] = f[6]; f[14] = f[9]; f[17] = f[12]; }
+    else if (y0) { f[2] = f[4]; f[11] = f[13]; f[16] = f[18]; f[8] = f[5]; }
+    else if (y1) { f[4] = f[2]; f[13] = f[11]; f[18] = f[16]; f[5] = f[8]; }
+}
+/* at an east face (CPU:590-644; LR7:958-1006) */
+template <class T> void alt_east_edges(T* f, int y, int z, int ny, int nz) {
+    const bool y0 = y == 0, y1 = y == ny - 1, z0 = z == 0, z1 = z == nz - 1;
+    if (y0 && z0) { f[2] = f[4]; f[13] = f[18]; f[11] = f[18]; f[16] = f[18]; f[5] = f[8]; f[9] = f[14]; f[10] = f[15]; }
+    else if (y0 && z1) { f[2] = f[4]; f[11] = f[13]; f[18] = f[13]; f[16] = f[13]; f[5] = f[8]; f[14] = f[9]; f[15] = f[10]; }
+    else if (y1 && z0) { f[4] = f[2]; f[18] = f[16]; f[11] = f[16]; f[13] = f[16]; f[8] = f[5]; f[9] = f[14]; f[10] = f[15]; }
+    else if (y1 && z1) { f[4] = f[2]; f[13] = f[11]; f[16] = f[11]; f[18] = f[11]; f[8] = f[5]; f[14] = f[9]; f[15] = f[10]; }
+    else if (y0) { f[2] = f[4]; f[11] = f[13]; f[16] = f[18]; f[5] = f[8]; }
+    else if (y1) { f[4] = f[2]; f[13] = f[11]; f[18] = f[16]; f[8] = f[5]; }
+}
+/* the z edge copies of a non-corner west / east node (CPU:471-482, 633-644) */
+template <class T> void alt_z_edges(T* f, int y, int z, int ny, int nz) {
+    if ((y == 0 || y == ny - 1) && (z == 0 || z == nz - 1)) return;
+    if (z == 0) { f[9] = f[14]; f[10] = f[15]; f[11] = f[16]; f[13] = f[18]; }
+    else if (z == nz - 1) { f[14] = f[9]; f[15] = f[10]; f[16] = f[11]; f[18] = f[13]; }
+}
+
+template <class T> void alt_boundary(int type, T* f, int y, int z, int ny, int nz, T u, int t) {
+    if (type == ORC_DIR_WEST) {
+        alt_west_edges(f, y, z, ny, nz);
+        alt_z_edges(f, y, z, ny, nz);
+        /* CPU:484-488 with v = w = 0 */
+        f[1] = std::fma(T(0.0555555556), T(6) * u, f[3]);
+        f[5] = std::fma(T(0.0277777778), T(6) * u, f[7]);
+        f[8] = std::fma(T(0.0277777778), T(6) * u, f[6]);
+        f[10] = std::fma(T(0.0277777778), T(6) * u, f[17]);
+        f[15] = std::fma(T(0.0277777778), T(6) * u, f[12]);
+    } else if (type == ORC_NEU_EAST || type == ORC_NEU_EAST_REG) {
+        if (type == ORC_NEU_EAST) {
+            alt_east_edges(f, y, z, ny, nz);
+            alt_z_edges(f, y, z, ny, nz);
+        }
+        const T rho = 1;
+        const T ux = -rho + (f[0] + f[2] + f[4] + f[9] + f[11] + f[13] + f[14] + f[16] + f[18] +
+                             T(2) * (f[1] + f[8] + f[5] + f[10] + f[15]));
+        if (type == ORC_NEU_EAST) {
+            /* CPU:651-655 with v = w = 0 */
+            f[3] = f[1] - T(0.333333333) * ux;
+            f[7] = f[5] - T(0.166666667) * ux;
+            f[6] = f[8] - T(0.166666667) * ux;
+            f[17] = f[10] - T(0.166666667) * ux;
+            f[12] = f[15] - T(0.166666667) * ux;
+        } else {
+            /* CPU:1080-1137 as written */
+            T fe[19];
+            const T usq = ux * ux;
+            for (int q = 0; q < 19; ++q) {
+                const T cu = T(CX[q]) * ux;
+                const T w = q == 0 ? T(0.3333333333) : (q <= 4 || q == 9 || q == 14) ? T(0.0555555556) : T(0.0277777778);
+                fe[q] = q == 0 ? w * (rho - T(1.5) * usq) : w * (rho + T(3) * cu + T(4.5) * cu * cu - T(1.5) * usq);
+            }
+            f[3] = fe[1] + f[1] - fe[1];
+            f[7] = fe[5] + f[5] - fe[5];
+            f[6] = fe[6] + f[8] - fe[8];
+            f[17] = fe[10] + f[10] - fe[10];
+            f[12] = fe[15] + f[15] - fe[15];
+            T d[19];
+            for (int q = 0; q < 19; ++q) d[q] = f[q] - fe[q];
+            const T P11 = d[1] + d[3] + d[5] + d[6] + d[7] + d[8] + d[10] + d[12] + d[15] + d[17];
+            const T P22 = d[2] + d[4] + d[5] + d[6] + d[7] + d[8] + d[11] + d[13] + d[16] + d[18];
+            const T P33 = d[9] + d[14] + d[10] + d[12] + d[15] + d[17] + d[11] + d[13] + d[16] + d[18];
+            const T P12 = d[5] + d[7] - d[6] - d[8];
+            const T P13 = d[10] + d[17] - d[12] - d[15];
+            const T P23 = d[11] + d[18] - d[13] - d[16];
+            const T A = T(0.666666667), B = T(-0.333333333);
+            /* f_q = feq_q + w'_q (Q_q : Pi), Q_q = c c - I/3 scaled as CPU:1119-1137 */
+            for (int q = 0; q < 19; ++q) {
+                const int ax = CX[q] * CX[q], ay = CY[q] * CY[q], az = CZ[q] * CZ[q];
+                const T pre = q == 0 ? T(1.5) : (q <= 4 || q == 9 || q == 14) ? T(0.25) : T(0.125);
+                T s = (ax ? A : B) * P11;
+                if (CX[q] * CY[q]) s = s + T(2) * (T(CX[q] * CY[q]) * P12);
+                if (CX[q] * CZ[q]) s = s + T(2) * (T(CX[q] * CZ[q]) * P13);
+                if (CY[q] * CZ[q]) s = s + T(2) * (T(CY[q] * CZ[q]) * P23);
+                s = s + (ay ? A : B) * P22;
+                s = s + (az ? A : B) * P33;
+                f[q] = fe[q] + pre * s;
+            }
+        }
+    } else if (type == ORC_XSYM_BOT) {
+        alt_west_edges(f, y, z, ny, nz);
+        f[1] = f[3]; f[5] = f[6]; f[8] = f[7]; f[10] = f[12]; f[15] = f[17];
+    } else if (type == ORC_XSYM_TOP) {
+        alt_east_edges(f, y, z, ny, nz);
+        f[3] = f[1]; f[6] = f[5]; f[7] = f[8]; f[12] = f[10]; f[17] = f[15];
+    } else if (type == ORC_YSYM_TOP || type == ORC_YSYM_BOT) {
+        if (z == 0) { f[9] = f[14]; f[10] = f[15]; f[11] = f[16]; f[12] = f[17]; f[13] = f[18]; }
+        if (z == nz - 1) { f[14] = f[9]; f[15] = f[10]; f[16] = f[11]; f[17] = f[12]; f[18] = f[13]; }
+        if (type == ORC_YSYM_TOP) { f[4] = f[2]; f[7] = f[6]; f[8] = f[5]; f[13] = f[11]; f[18] = f[16]; }
+        else { f[2] = f[4]; f[6] = f[7]; f[5] = f[8]; f[11] = f[13]; f[16] = f[18]; }
+    } else if (type == ORC_ZSYM_TOP || type == ORC_ZSYM_BOT) {
+        if (y == 0) { f[2] = f[4]; f[6] = f[7]; f[5] = f[8]; f[11] = f[13]; f[16] = f[18]; }
+        if (y == ny - 1) { f[4] = f[2]; f[7] = f[6]; f[8] = f[5]; f[13] = f[11]; f[18] = f[16]; }
+        if (type == ORC_ZSYM_TOP) { f[14] = f[9]; f[15] = f[10]; f[16] = f[11]; f[17] = f[12]; f[18] = f[13]; }
+        else { f[9] = f[14]; f[10] = f[15]; f[11] = f[16]; f[12] = f[17]; f[13] = f[18]; }
+    } else if (type == ORC_WEST_REG) {
+        /* BC1:789-870: momentum replaced by (u, 0, w), everything else kept;
+         * w = 0.01 at t = 1000, 2000, 3000 */
+        const T w = (t == 1000 || t == 2000 || t == 3000) ? T(0.01) : T(0);
+        T j[3] = {0, 0, 0};
+        for (int q = 0; q < 19; ++q) j[0] += CX[q] * f[q], j[1] += CY[q] * f[q], j[2] += CZ[q] * f[q];
+        const T d[3] = {(u - j[0]) / T(10), (T(0) - j[1]) / T(10), (w - j[2]) / T(10)};
+        for (int q = 0; q < 19; ++q) f[q] += CX[q] * d[0] + CY[q] * d[1] + CZ[q] * d[2];
+    }
+}
+
 template <class T> inline void lid(T* f, int face, T ux, T uy, T uz, int quirk) {
     int axis = face / 2;
     int sgn = (face % 2 == 0) ? 1 : -1; /* inward normal component */
@@ -499,6 +620,8 @@ void step_impl(const orc_params* p, const uint8_t* mask, const T* fA, T* fB, dou
                         extrap<T>(im, f, T(p->rho_out), uin);
                     } else if (im == ORC_LID) {
                         lid<T>(f, p->lid_face, T(p->lid_u[0]), T(p->lid_u[1]), T(p->lid_u[2]), p->lid_quirk);
+                    } else if (im >= ORC_DIR_WEST) {
+                        alt_boundary<T>(im, f, y, z, ny, nz, T(p->u_in), p->t);
                     }
                     if (p->mlp) {
                         double g[Q];
@@ -590,6 +713,10 @@ void orc_invert_les_cf(const float* mom, float* f, int n, float omega_c, float c
 
 void orc_invert_les_fc(const float* mom, float* f, int n, float omega_f, float cs, float lrf) {
     for (int i = 0; i < n; ++i) invert_les_fc(mom + 9L * i, omega_f, cs, lrf, f + 19L * i);
+}
+
+void orc_alt_boundary(int type, float* f, int n, const int* yz, int ny, int nz, float u, int t) {
+    for (int i = 0; i < n; ++i) alt_boundary<float>(type, f + 19L * i, yz[2 * i], yz[2 * i + 1], ny, nz, u, t);
 }
 
 void orc_lid(float* f, int n, int face, float ux, float uy, float uz, int quirk) {

@@ -36,7 +36,19 @@ enum {
     ORC_EAST_OUTLET = 4,  /* ImageFcn 300: East_Extrap, LR7:805-850 */
     ORC_SOUTH_INLET = 5,  /* ImageFcn 200: South_Extrap, LR7:760-803 */
     ORC_NORTH_OUTLET = 6, /* ImageFcn 100: North_Extrap, LR7:713-758 */
-    ORC_LID = 7           /* moving lid, regularised Dirichlet (CPU_3D/CPU_3D.cpp:974-1054) */
+    ORC_LID = 7,          /* moving lid, regularised Dirichlet (CPU_3D/CPU_3D.cpp:974-1054) */
+    /* alternate boundaries (CPU_3D/CPU_3D.cpp:411-1140, LRTurbTest/LRMultiGPU7.cu:899-1016,
+     * BC1/LRMultiGPU7.cu:789), applied to the pulled populations before the collision */
+    ORC_DIR_WEST = 8,     /* DirichletWest, CPU_3D im 3 */
+    ORC_NEU_EAST = 9,     /* NeumannEast_Reg, im 14 */
+    ORC_NEU_EAST_REG = 10,/* NeumannEast_Regularized, im 54 */
+    ORC_XSYM_TOP = 11,    /* xsymmetry_top (LR7) */
+    ORC_XSYM_BOT = 12,    /* xsymmetry_bot (LR7) */
+    ORC_YSYM_TOP = 13,    /* ysymmetry_top, im 21 */
+    ORC_YSYM_BOT = 14,    /* ysymmetry_bot, im 22 */
+    ORC_ZSYM_TOP = 15,    /* zsymmetry_top, im 23 */
+    ORC_ZSYM_BOT = 16,    /* zsymmetry_bot, im 24 */
+    ORC_WEST_REG = 17     /* BC1 West_Reg */
 };
 
 /* collision models */
@@ -107,6 +119,9 @@ void orc_strain_rate(const float* mom, float* s, int n);
 void orc_invert_les_cf(const float* mom, float* f, int n, float omega_c, float cs, float lrfactor);
 void orc_invert_les_fc(const float* mom, float* f, int n, float omega_f, float cs, float lrfactor);
 void orc_lid(float* f, int n, int face, float ux, float uy, float uz, int quirk);
+/* an alternate boundary of node type on n cells at (y, z) = yz[2i], yz[2i+1]
+ * of an ny x nz domain; u the inlet velocity, t the step */
+void orc_alt_boundary(int type, float* f, int n, const int* yz, int ny, int nz, float u, int t);
 
 /* whole-level operations on compact SoA arrays */
 void orc_init(const orc_params* p, const uint8_t* mask, float* f, int kind, float u0);

@@ -139,6 +139,11 @@ def stage(ref_root: Path = REF_ROOT) -> bool:
             # timing harness: the final tecplot dump of every node is not part of the loop
             s = s.replace('output.open ("output.dat");', "/* output.dat dump disabled for timing */")
         (REF_DIR / f"cpu3d_{name}.cpp").write_text(s)
+    bc1 = ref_root / "BC1" / "LRMultiGPU7.cu"
+    if bc1.exists():
+        t = bc1.read_text(errors="replace")
+        (REF_DIR / "bc1_westreg.inc").write_text(
+            _cut(t, r"inline __device__ void West_Reg", r"(inline |__global__|__device__ |int main)"))
     for name, (rel, subs) in POST_PROGRAMS.items():
         src = ref_root / rel
         if not src.exists():
@@ -213,24 +218,18 @@ def build_ref(force: bool = False, jobs: int = 8) -> list[Path]:
     for name in CPU3D_PROGRAMS:
         out = REF_DIR / f"cpu3d_{name}"
         if force or not out.exists():
-            jobs_list.append([CXX, "-O3", "-march=native", "-w", "-o", str(out), str(REF_DIR / f"cpu3d_{name}.cpp")])
+            # portable flags: the same build on the x86 and the Arm host
+            jobs_list.append([CXX, "-O3", "-w", "-o", str(out), str(REF_DIR / f"cpu3d_{name}.cpp")])
+    out = REF_DIR / "bc1.so"
+    if (REF_DIR / "bc1_westreg.inc").exists() and (force or not out.exists()):
+        jobs_list.append([CXX, *SHIM_FLAGS, f"-I{REF_DIR}", "-o", str(out), str(HERE / "ref_shim_bc1.cpp")])
     for name in POST_PROGRAMS:
         src, out = REF_DIR / f"{name}.cpp", REF_DIR / name
         if src.exists() and (force or not out.exists()):
             jobs_list.append([CXX, "-O2", "-ffp-contract=off", "-w", "-o", str(out), str(src)])
     with ThreadPoolExecutor(jobs) as ex:
-        list(ex.map(_run_cpu3d_fallback, jobs_list))
+        list(ex.map(_run, jobs_list))
     return sorted(REF_DIR.glob("*.so"))
-
-
-def _run_cpu3d_fallback(cmd: list[str]) -> None:
-    try:
-        _run(cmd)
-    except RuntimeError:
-        if "-march=native" in cmd:
-            _run([c for c in cmd if c != "-march=native"])
-        else:
-            raise
 
 
 if __name__ == "__main__":

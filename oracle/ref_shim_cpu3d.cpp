@@ -3,8 +3,9 @@
  * functions (CPU_3D/CPU_3D.cpp from bgk_collide up to main(), CPU:116-1209),
  * staged by oracle/ref_recipe.py into oracle/_ref/cpu3d_body.inc.
  *
- * TEST INFRASTRUCTURE ONLY.  Exposes bgk_collide, mrt_collide and the
- * regularised lid boundary DirichletWest_Regularized on n cells (cell-major).
+ * TEST INFRASTRUCTURE ONLY.  Exposes bgk_collide, mrt_collide, the
+ * regularised lid boundary DirichletWest_Regularized and the boundaries()
+ * dispatch on n cells (cell-major).
  */
 #include <sys/time.h>
 
@@ -40,5 +41,19 @@ void ref_cpu3d_lid_west(float* f, int n) {
         DirichletWest_Regularized(F19(g), 1, 1);
     }
 }
+
+/* CPU_3D's boundaries() dispatch (CPU:1142-1196) for node code im on n
+ * cells at (y, z) = yz[2 i], yz[2 i + 1] of its YDIM x ZDIM domain */
+void ref_cpu3d_boundary(float* f, int n, const int* yz, int im) {
+    for (int i = 0; i < n; ++i) {
+        float* g = f + 19L * i;
+        boundaries(F19(g), yz[2 * i], yz[2 * i + 1], im);
+    }
+}
+
+/* the domain the staged functions were compiled for */
+int ref_cpu3d_ydim(void) { return YDIM; }
+int ref_cpu3d_zdim(void) { return ZDIM; }
+float ref_cpu3d_umax(void) { return UMAX; }
 
 }  // extern "C"

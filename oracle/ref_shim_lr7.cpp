@@ -469,4 +469,14 @@ int ref_write_forces(char* buf, int len, int level) {
     return int(s.size());
 }
 
+/* xsymmetry_top / xsymmetry_bot (LR7:899-1016) on n cells at (y, z) */
+void ref_xsymmetry(float* f, int n, const int* yz, int top) {
+    for (int i = 0; i < n; ++i) {
+        if (top) xsymmetry_top(f + 19L * i, yz[2 * i], yz[2 * i + 1]);
+        else xsymmetry_bot(f + 19L * i, yz[2 * i], yz[2 * i + 1]);
+    }
+}
+int ref_ydim(void) { return YDIM; }
+int ref_zdim(void) { return ZDIM; }
+
 }  // extern "C"

@@ -6,7 +6,7 @@ harness that oracle/ref_recipe.py stages and builds in oracle/_ref/ (needs the
 reference sources, i.e. the development container).  Seeded inputs; rerunning
 reproduces the files.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [part ...]   (all parts by default)
 """
 from __future__ import annotations
 
@@ -197,14 +197,57 @@ def cpu3d_cavity():
     np.savez_compressed(HERE / "cpu3d_cavity24.npz", uvrho=out, steps=100)
 
 
+def alt_bc():
+    """the reference's alternate boundaries on seeded cells at every edge and
+    corner class of their domains: CPU_3D's boundaries() dispatch (CPU:1027-
+    1078) for the codes it routes (3 DirichletWest, 14 NeumannEast_Reg, 54
+    NeumannEast_Regularized, 21/22 y symmetry, 23/24 z symmetry) on its
+    YDIM x ZDIM face, LR7's xsymmetry_top / _bot on its own, and BC1's
+    West_Reg at perturbed and plain time steps"""
+    c3, lr7, bc1 = lib("cpu3d.so"), lib("lr7_tiny.so"), lib("bc1.so")
+    out = {}
+
+    def positions(ny, nz):
+        ys = sorted({0, 1, ny // 2, ny - 2, ny - 1})
+        zs = sorted({0, 1, nz // 2, nz - 2, nz - 1})
+        return np.array([(y, z) for y in ys for z in zs], np.int32)
+
+    ny, nz = c3.ref_cpu3d_ydim(), c3.ref_cpu3d_zdim()
+    c3.ref_cpu3d_umax.restype = F
+    yz = positions(ny, nz)
+    f0 = random_cells(len(yz), 20251204)
+    out.update(cpu3d_f0=f0, cpu3d_yz=yz, cpu3d_dims=np.array([ny, nz], np.int32),
+               cpu3d_umax=np.float32(c3.ref_cpu3d_umax()))
+    for im in (3, 14, 54, 21, 22, 23, 24):
+        g = f0.copy()
+        c3.ref_cpu3d_boundary(ptr(g), len(yz), ptr(yz), im)
+        out[f"cpu3d_im{im}"] = g
+    ny, nz = lr7.ref_ydim(), lr7.ref_zdim()
+    yz = positions(ny, nz)
+    f0 = random_cells(len(yz), 20251205)
+    out.update(lr7_f0=f0, lr7_yz=yz, lr7_dims=np.array([ny, nz], np.int32))
+    for top in (1, 0):
+        g = f0.copy()
+        lr7.ref_xsymmetry(ptr(g), len(yz), ptr(yz), top)
+        out[f"lr7_xsym_top{top}"] = g
+    f0 = random_cells(32, 20251206)
+    out["bc1_f0"] = f0
+    for t in (1, 1000, 2000, 3000, 4000):
+        g = f0.copy()
+        bc1.ref_west_reg(ptr(g), len(g), F(0.05), t)
+        out[f"bc1_west_reg_u0.05_t{t}"] = g
+    np.savez_compressed(HERE / "alt_bc.npz", **out)
+
+
+PARTS = dict(cells=lambda: cells(), runs=lambda: runs(), writer=lambda: writer(),
+             cpu3d_cavity=lambda: cpu3d_cavity(), alt_bc=lambda: alt_bc())
+
 if __name__ == "__main__":
     if not ref_recipe.staged():
         if not ref_recipe.stage():
             sys.exit("reference sources not found; set LBM_REFERENCE")
     ref_recipe.build_ref()
-    cells()
-    runs()
-    writer()
-    cpu3d_cavity()
+    for name in sys.argv[1:] or PARTS:
+        PARTS[name]()
     for p in sorted(HERE.iterdir()):
         print(f"{p.stat().st_size:>9} {p.name}")

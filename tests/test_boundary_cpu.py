@@ -96,6 +96,36 @@ def test_masks_of_every_geometry(product):
     assert np.array_equal((m[0] == 2) & inner, circle & inner)
 
 
+def test_duct_and_faces_masks(product):
+    """"duct" is CPU_3D's cylinder duct (CPU:39-63 with walls on the y and z
+    faces, 3 = DirichletWest at x = 0, 14 = NeumannEast_Reg at x = nx-1);
+    FACES puts a node type on each face with y faces over z over x"""
+    N = product.NODE
+    nx, ny, nz = 40, 20, 8
+    t = product.make_inputs(nx, ny, nz, obst1=(15.5, 9.5, 0.0), r1=4.0, geometry="duct")
+    m = product.inputs_mask(t).reshape(nz, ny, nx)
+    z, y, x = np.mgrid[0:nz, 0:ny, 0:nx]
+    want = np.zeros((nz, ny, nx), np.uint8)
+    xf, yf = x.astype(np.float32), y.astype(np.float32)
+    want[(xf - np.float32(15.5)) ** 2 + (yf - np.float32(9.5)) ** 2 < np.float32(16.0)] = N["BODY"]
+    want[x == 0], want[x == nx - 1] = N["DIR_WEST"], N["NEU_EAST"]
+    want[(z == 0) | (z == nz - 1)] = N["WALL"]
+    want[(y == 0) | (y == ny - 1)] = N["WALL"]
+    assert np.array_equal(m, want)
+    faces = ("XSYM_BOT", "WEST_REG", "YSYM_BOT", "YSYM_TOP", "-", "ZSYM_TOP")
+    t = product.make_inputs(nx, ny, nz, geometry="periodic", faces=faces)
+    assert "FACES: \tXSYM_BOT WEST_REG YSYM_BOT YSYM_TOP - ZSYM_TOP" in product.normalize_inputs(t)
+    m = product.inputs_mask(t).reshape(nz, ny, nx)
+    want = np.zeros((nz, ny, nx), np.uint8)
+    want[x == 0], want[x == nx - 1] = N["XSYM_BOT"], N["WEST_REG"]
+    want[z == nz - 1] = N["ZSYM_TOP"]
+    want[y == 0], want[y == ny - 1] = N["YSYM_BOT"], N["YSYM_TOP"]
+    assert np.array_equal(m, want)
+    for bad in ("DIR_WEST NEU_EAST", "DIR_WEST NEU_EAST - - - - -", "DIR_WEST X - - - -"):
+        with pytest.raises(product.LbmError):
+            product.inputs_mask(product.make_inputs(nx, ny, nz, faces=bad))
+
+
 def test_checkpoint_rejects_other_files(product, tmp_path):
     """lbm_create_from_state reads the file's header before any device work"""
     import ctypes

@@ -472,3 +472,97 @@ def test_dynamic_inlet_vs_oracle(product):
     assert abs(hist[-1, 2] - dpdy0) > 1e-3 * abs(dpdy0)            # the control acted
     err, _ = _compare(f, fa, mask)
     assert err < RTOL
+
+
+def _alt_bc_mask(case, nx, ny, nz):
+    N = lambda k: product_node(k)  # noqa: E731
+    m = np.zeros((nz, ny, nx), np.uint8)
+    if case == "dirichlet_neumann_ysym":
+        m[:, 0, :], m[:, -1, :] = N("YSYM_BOT"), N("YSYM_TOP")
+        m[:, :, 0], m[:, :, -1] = N("DIR_WEST"), N("NEU_EAST")
+    elif case == "xsym_regularised_zsym":
+        m[:, 0, :] = m[:, -1, :] = N("WALL")
+        m[0], m[-1] = N("ZSYM_BOT"), N("ZSYM_TOP")
+        m[:, 1:-1, 0], m[:, 1:-1, -1] = N("XSYM_BOT"), N("NEU_EAST_REG")
+    else:  # "west_reg_xsym_body"
+        m[:, 0, :] = m[:, -1, :] = N("WALL")
+        m[:, 1:-1, 0], m[:, 1:-1, -1] = N("WEST_REG"), N("XSYM_TOP")
+        m[:, 6:10, 12:16] = N("BODY")
+    return m
+
+
+def product_node(k):
+    import lbm_multigpu_gb300 as lbm
+
+    return lbm.NODE[k]
+
+
+@pytest.mark.parametrize("case,model,les", [("dirichlet_neumann_ysym", "MRT_CPU3D", 0),
+                                            ("xsym_regularised_zsym", "MRT", 1),
+                                            ("west_reg_xsym_body", "BGK", 0)])
+def test_alternate_boundaries_vs_oracle(product, case, model, les):
+    """the alternate boundary node types (CPU_3D's Dirichlet west, Neumann and
+    regularised east, y/z symmetry planes; LR7's x symmetry planes; BC1's
+    West_Reg through its t = 1000 perturbation) in a 30x16x12 box stepped
+    through lbm_stream_collide_f32, against the oracle's step on the same mask"""
+    torch = pytest.importorskip("torch")
+    lbm = product
+    lib = lbm.library()
+    nx, ny, nz, pitch, steps, t0, om, u = 30, 16, 12, 32, 80, 960, 1.7, 0.04
+    mask = _alt_bc_mask(case, nx, ny, nz)
+    # the box starts at half the inlet speed so that the inlet drives the flow
+    o = OracleRun(nx, ny, nz, mask, om, model=lbm.MODELS[model], les=les, cs=0.02, u_in=u, init_kind=0,
+                  init_u=u / 2)
+    o.t = t0
+    dev = torch.device("cuda", torch.cuda.current_device())
+    fa = torch.zeros((19, nz, ny, pitch), dtype=torch.float32, device=dev)
+    fa[..., :nx] = torch.from_numpy(o.fa.copy()).to(dev)
+    fb = torch.zeros_like(fa)
+    m = torch.full((nz, ny, pitch), 1, dtype=torch.uint8, device=dev)
+    m[..., :nx] = torch.from_numpy(mask).to(dev)
+    P = ctypes.c_void_p
+    stream = P(torch.cuda.current_stream().cuda_stream)
+    for t in range(t0, t0 + steps):
+        assert lib.lbm_stream_collide_f32(P(fa.data_ptr()), P(fb.data_ptr()), P(m.data_ptr()), nx, ny, nz, pitch,
+                                          lbm.MODELS[model], les, ctypes.c_float(om), ctypes.c_float(0.02),
+                                          ctypes.c_float(u), ctypes.c_float(1.0), t, stream) == 0
+        fa, fb = fb, fa
+    torch.cuda.synchronize()
+    o.step(steps)
+    f = fa[..., :nx].cpu().numpy()
+    assert np.isfinite(f).all()
+    err, drho = _compare(f, o.fa, mask)
+    assert err < RTOL and drho < 1e-5, (err, drho)
+    # the boundaries acted: the flow differs from the same box without them
+    plain = OracleRun(nx, ny, nz, np.where(mask >= product_node("DIR_WEST"), 0, mask).astype(np.uint8), om,
+                      model=lbm.MODELS[model], les=les, cs=0.02, u_in=u, init_kind=0, init_u=u / 2)
+    plain.t = t0
+    plain.step(steps)
+    assert _compare(plain.fa, o.fa, mask)[0] > 100 * RTOL
+
+
+@pytest.mark.parametrize("faces,model,les", [(None, "MRT_CPU3D", 0),
+                                             (("DIR_WEST", "NEU_EAST", "YSYM_BOT", "YSYM_TOP", "ZSYM_BOT",
+                                               "ZSYM_TOP"), "MRT", 1)])
+def test_duct_solver_vs_oracle(product, faces, model, les):
+    """the "duct" geometry through the handle: CPU_3D's cylinder duct with
+    its Dirichlet inlet and rho = 1 outlet (walls on y and z), and the same
+    duct with symmetry planes from a FACES line; flow and drag/lift against
+    the oracle.  (NEU_EAST_REG, NeumannEast_Regularized as the reference
+    wrote it, diverges within ~100 steps in such a duct; it is checked per
+    cell and in the short box runs only.)"""
+    lbm = product
+    nx, ny, nz, steps = 48, 24, 12, 150
+    ext = dict(geometry="duct") if faces is None else dict(geometry="duct", faces=faces)
+    text = lbm.make_inputs(nx, ny, nz, obst1=(12.5, 11.5, 0.0), r1=4.0, re=40.0, umax=0.04, tmax=steps, les=les,
+                           cs=0.02, model=model, **ext)
+    with lbm.Solver(text) as s:
+        s.step(steps)
+        f, mask, om, F = s.populations(), s.mask(), s.params()["omega"], s.forces()
+    assert (mask >= lbm.NODE["DIR_WEST"]).any()
+    o = OracleRun(nx, ny, nz, mask, om, model=lbm.MODELS[model], les=les, cs=0.02, u_in=0.04, init_kind=0,
+                  init_u=0.04)
+    o.step(steps)
+    err, drho = _compare(f, o.fa, mask)
+    assert err < RTOL and drho < 1e-5, (err, drho)
+    assert rel_l2(F[:, 0], np.array(o.forces)[: len(F), 0]) < FTOL
