@@ -25,7 +25,7 @@ LIB_PATH = _PKG / "_build" / "liblbm_gb300.so"
 
 NODE = dict(FLUID=0, WALL=1, BODY=2, WEST_INLET=3, EAST_OUTLET=4, SOUTH_INLET=5, NORTH_OUTLET=6, LID=7,
             DIR_WEST=8, NEU_EAST=9, NEU_EAST_REG=10, XSYM_TOP=11, XSYM_BOT=12, YSYM_TOP=13, YSYM_BOT=14,
-            ZSYM_TOP=15, ZSYM_BOT=16, WEST_REG=17)
+            ZSYM_TOP=15, ZSYM_BOT=16, WEST_REG=17, DIR_WEST_V=18, DIR_NORTH=19, DIR_SOUTH=20)
 MODELS = dict(MRT=0, MRT_DI3=1, BGK=2, MRT_CPU3D=3)
 
 _P = ctypes.c_void_p

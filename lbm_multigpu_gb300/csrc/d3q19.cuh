@@ -528,6 +528,44 @@ template <class T> __host__ __device__ __forceinline__ void west_reg(T f[19], T 
     for (int q = 0; q < 19; ++q) f[q] += T(cx(q)) * dx + T(cy(q)) * dy + T(cz(q)) * dz;
 }
 
+/* DirichletWest_Reg (CPU:379-453): x = 0 with velocity (0, v, 0), its y
+ * edge copies, then the z face copies; DirichletNorth_Reg / _South_Reg
+ * (CPU:578-745): y = ny - 1 / y = 0 walls moving with (u, 0, 0) after the
+ * z face copies.  Unknowns from their opposites plus 6 w_q c_q . u (rho = 1) */
+template <class T> __host__ __device__ __forceinline__ void z_face_copies(T f[19], int z, int nz) {
+    if (z == 0) f[9] = f[14], f[10] = f[15], f[11] = f[16], f[12] = f[17], f[13] = f[18];
+    else if (z == nz - 1) f[14] = f[9], f[15] = f[10], f[16] = f[11], f[17] = f[12], f[18] = f[13];
+}
+template <class T> __host__ __device__ __forceinline__ void dirichlet_west_v(T f[19], int y, int z, int ny, int nz, T v) {
+    if (y == 0) f[2] = f[4], f[6] = f[7], f[11] = f[13], f[16] = f[18];
+    else if (y == ny - 1) f[4] = f[2], f[7] = f[6], f[13] = f[11], f[18] = f[16];
+    z_face_copies(f, z, nz);
+    const T u = T(0), w = T(0);
+    f[1] = f[3] + T(0.33333333) * u;
+    f[5] = f[7] + T(0.166666667) * (u + v);
+    f[8] = f[6] + T(0.166666667) * (u - v);
+    f[10] = f[17] + T(0.166666667) * (u + w);
+    f[15] = f[12] + T(0.166666667) * (u - w);
+}
+template <class T> __host__ __device__ __forceinline__ void dirichlet_north(T f[19], int z, int nz, T u) {
+    z_face_copies(f, z, nz);
+    const T v = T(0), w = T(0);
+    f[4] = f[2] - T(0.33333333) * v;
+    f[7] = f[5] - T(0.166666667) * (u + v);
+    f[8] = f[6] + T(0.166666667) * (u - v);
+    f[13] = f[16] - T(0.166666667) * (v - w);
+    f[18] = f[11] - T(0.166666667) * (v + w);
+}
+template <class T> __host__ __device__ __forceinline__ void dirichlet_south(T f[19], int z, int nz, T u) {
+    z_face_copies(f, z, nz);
+    const T v = T(0), w = T(0);
+    f[2] = f[4] + T(0.33333333) * v;
+    f[5] = f[7] + T(0.166666667) * (u + v);
+    f[6] = f[8] - T(0.166666667) * (u - v);
+    f[16] = f[13] + T(0.166666667) * (v - w);
+    f[11] = f[18] + T(0.166666667) * (v + w);
+}
+
 /* the dispatch for a node of an alternate-boundary type */
 template <class T>
 __host__ __device__ __forceinline__ void alt_boundary(int type, T f[19], int x, int y, int z, int nx, int ny, int nz,
@@ -544,6 +582,9 @@ __host__ __device__ __forceinline__ void alt_boundary(int type, T f[19], int x, 
         case ZSYM_TOP: zsym(f, true, y, ny); break;
         case ZSYM_BOT: zsym(f, false, y, ny); break;
         case WEST_REG: west_reg(f, u_in, t); break;
+        case DIR_WEST_V: dirichlet_west_v(f, y, z, ny, nz, u_in); break;
+        case DIR_NORTH: dirichlet_north(f, z, nz, u_in); break;
+        case DIR_SOUTH: dirichlet_south(f, z, nz, u_in); break;
         default: break;
     }
 }

@@ -124,7 +124,8 @@ std::string trim(const std::string& s) {
 const char* const NODE_NAMES[NODE_TYPES] = {"FLUID",    "WALL",     "BODY",         "WEST_INLET", "EAST_OUTLET",
                                             "SOUTH_INLET", "NORTH_OUTLET", "LID",   "DIR_WEST",   "NEU_EAST",
                                             "NEU_EAST_REG", "XSYM_TOP", "XSYM_BOT", "YSYM_TOP",   "YSYM_BOT",
-                                            "ZSYM_TOP", "ZSYM_BOT", "WEST_REG"};
+                                            "ZSYM_TOP", "ZSYM_BOT", "WEST_REG", "DIR_WEST_V", "DIR_NORTH",
+                                            "DIR_SOUTH"};
 
 bool parse_faces(const std::string& v, int out[6]) {
     std::istringstream in(v);

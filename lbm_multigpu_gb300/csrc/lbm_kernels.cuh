@@ -35,7 +35,10 @@ enum NodeType : uint8_t {
     ZSYM_TOP = 15,      /* zsymmetry_top, im 23 */
     ZSYM_BOT = 16,      /* zsymmetry_bot, im 24 */
     WEST_REG = 17,      /* BC1 West_Reg */
-    NODE_TYPES = 18
+    DIR_WEST_V = 18,    /* DirichletWest_Reg, im 13: tangential v on x = 0 */
+    DIR_NORTH = 19,     /* DirichletNorth_Reg: y = ny - 1 moving in x */
+    DIR_SOUTH = 20,     /* DirichletSouth_Reg: y = 0 moving in x */
+    NODE_TYPES = 21
 };
 
 /* collision models: LR7 mrt_collide, DynInlet3's MRT (bgk_meq + AddForce),

@@ -392,6 +392,38 @@ template <class T> void alt_boundary(int type, T* f, int y, int z, int ny, int n
         for (int q = 0; q < 19; ++q) j[0] += CX[q] * f[q], j[1] += CY[q] * f[q], j[2] += CZ[q] * f[q];
         const T d[3] = {(u - j[0]) / T(10), (T(0) - j[1]) / T(10), (w - j[2]) / T(10)};
         for (int q = 0; q < 19; ++q) f[q] += CX[q] * d[0] + CY[q] * d[1] + CZ[q] * d[2];
+    } else if (type == ORC_DIR_WEST_V || type == ORC_DIR_NORTH || type == ORC_DIR_SOUTH) {
+        /* CPU:379-453 (west, velocity (0, u, 0), its y edges first) and
+         * CPU:578-745 (north / south walls moving with (u, 0, 0)): the z
+         * face copies, then each unknown from its opposite plus
+         * 6 w_q rho c_q . u at rho = 1 */
+        if (type == ORC_DIR_WEST_V) {
+            if (y == 0) { f[2] = f[4]; f[6] = f[7]; f[11] = f[13]; f[16] = f[18]; }
+            else if (y == ny - 1) { f[4] = f[2]; f[7] = f[6]; f[13] = f[11]; f[18] = f[16]; }
+        }
+        if (z == 0) { f[9] = f[14]; f[10] = f[15]; f[11] = f[16]; f[12] = f[17]; f[13] = f[18]; }
+        else if (z == nz - 1) { f[14] = f[9]; f[15] = f[10]; f[16] = f[11]; f[17] = f[12]; f[18] = f[13]; }
+        const T ux = type == ORC_DIR_WEST_V ? T(0) : u, uy = type == ORC_DIR_WEST_V ? u : T(0), uz = 0;
+        const T a = T(0.33333333), b = T(0.166666667);
+        if (type == ORC_DIR_WEST_V) {
+            f[1] = f[3] + a * ux;
+            f[5] = f[7] + b * (ux + uy);
+            f[8] = f[6] + b * (ux - uy);
+            f[10] = f[17] + b * (ux + uz);
+            f[15] = f[12] + b * (ux - uz);
+        } else if (type == ORC_DIR_NORTH) {
+            f[4] = f[2] - a * uy;
+            f[7] = f[5] - b * (ux + uy);
+            f[8] = f[6] + b * (ux - uy);
+            f[13] = f[16] - b * (uy - uz);
+            f[18] = f[11] - b * (uy + uz);
+        } else {
+            f[2] = f[4] + a * uy;
+            f[5] = f[7] + b * (ux + uy);
+            f[6] = f[8] - b * (ux - uy);
+            f[16] = f[13] + b * (uy - uz);
+            f[11] = f[18] + b * (uy + uz);
+        }
     }
 }
 

@@ -48,7 +48,10 @@ enum {
     ORC_YSYM_BOT = 14,    /* ysymmetry_bot, im 22 */
     ORC_ZSYM_TOP = 15,    /* zsymmetry_top, im 23 */
     ORC_ZSYM_BOT = 16,    /* zsymmetry_bot, im 24 */
-    ORC_WEST_REG = 17     /* BC1 West_Reg */
+    ORC_WEST_REG = 17,    /* BC1 West_Reg */
+    ORC_DIR_WEST_V = 18,  /* DirichletWest_Reg, im 13 (x = 0, velocity (0, u, 0)) */
+    ORC_DIR_NORTH = 19,   /* DirichletNorth_Reg (y = ny - 1, velocity (u, 0, 0)) */
+    ORC_DIR_SOUTH = 20    /* DirichletSouth_Reg (y = 0, velocity (u, 0, 0)) */
 };
 
 /* collision models */

@@ -51,6 +51,16 @@ void ref_cpu3d_boundary(float* f, int n, const int* yz, int im) {
     }
 }
 
+/* DirichletNorth_Reg / DirichletSouth_Reg (CPU:578-745; written, but the
+ * dispatch's lines for them are commented out) on n cells at (y, z) */
+void ref_cpu3d_dirichlet_ns(float* f, int n, const int* yz, int north) {
+    for (int i = 0; i < n; ++i) {
+        float* g = f + 19L * i;
+        if (north) DirichletNorth_Reg(F19(g), yz[2 * i], yz[2 * i + 1]);
+        else DirichletSouth_Reg(F19(g), yz[2 * i], yz[2 * i + 1]);
+    }
+}
+
 /* the domain the staged functions were compiled for */
 int ref_cpu3d_ydim(void) { return YDIM; }
 int ref_cpu3d_zdim(void) { return ZDIM; }

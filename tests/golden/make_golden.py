@@ -200,9 +200,9 @@ def cpu3d_cavity():
 def alt_bc():
     """the reference's alternate boundaries on seeded cells at every edge and
     corner class of their domains: CPU_3D's boundaries() dispatch (CPU:1027-
-    1078) for the codes it routes (3 DirichletWest, 14 NeumannEast_Reg, 54
-    NeumannEast_Regularized, 21/22 y symmetry, 23/24 z symmetry) on its
-    YDIM x ZDIM face, LR7's xsymmetry_top / _bot on its own, and BC1's
+    1078) for the codes it routes (3 DirichletWest, 13 DirichletWest_Reg,
+    14 NeumannEast_Reg, 54 NeumannEast_Regularized, 21/22 y symmetry, 23/24 z
+    symmetry) on its YDIM x ZDIM face, its DirichletNorth_Reg / _South_Reg, LR7's xsymmetry_top / _bot on its own, and BC1's
     West_Reg at perturbed and plain time steps"""
     c3, lr7, bc1 = lib("cpu3d.so"), lib("lr7_tiny.so"), lib("bc1.so")
     out = {}
@@ -218,10 +218,14 @@ def alt_bc():
     f0 = random_cells(len(yz), 20251204)
     out.update(cpu3d_f0=f0, cpu3d_yz=yz, cpu3d_dims=np.array([ny, nz], np.int32),
                cpu3d_umax=np.float32(c3.ref_cpu3d_umax()))
-    for im in (3, 14, 54, 21, 22, 23, 24):
+    for im in (3, 13, 14, 54, 21, 22, 23, 24):
         g = f0.copy()
         c3.ref_cpu3d_boundary(ptr(g), len(yz), ptr(yz), im)
         out[f"cpu3d_im{im}"] = g
+    for north in (1, 0):
+        g = f0.copy()
+        c3.ref_cpu3d_dirichlet_ns(ptr(g), len(yz), ptr(yz), north)
+        out[f"cpu3d_dirichlet_north{north}"] = g
     ny, nz = lr7.ref_ydim(), lr7.ref_zdim()
     yz = positions(ny, nz)
     f0 = random_cells(len(yz), 20251205)

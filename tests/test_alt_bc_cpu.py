@@ -4,8 +4,9 @@ Fixtures (tests/golden/alt_bc.npz, made by tests/golden/make_golden.py) hold
 the reference's outputs on seeded near-equilibrium cells at every edge and
 corner class of its domain:
   CPU_3D/CPU_3D.cpp boundaries() (CPU:1027-1078): 3 DirichletWest,
-    14 NeumannEast_Reg, 54 NeumannEast_Regularized, 21/22 ysymmetry_top/_bot,
-    23/24 zsymmetry_top/_bot, on its 43 x 43 face with UMAX = 0.04;
+    13 DirichletWest_Reg, 14 NeumannEast_Reg, 54 NeumannEast_Regularized, 21/22 ysymmetry_top/_bot,
+    23/24 zsymmetry_top/_bot, on its 43 x 43 face with UMAX = 0.04, and
+    its DirichletNorth_Reg / DirichletSouth_Reg (CPU:578-745);
   LRTurbTest/LRMultiGPU7.cu xsymmetry_top / _bot (LR7:899-1016);
   BC1/LRMultiGPU7.cu West_Reg (:789-870) at perturbed and plain steps.
 The product's cell functions (host build of d3q19.cuh) and the oracle's
@@ -29,11 +30,11 @@ P = ctypes.c_void_p
 F = ctypes.c_float
 
 NODE = dict(DIR_WEST=8, NEU_EAST=9, NEU_EAST_REG=10, XSYM_TOP=11, XSYM_BOT=12, YSYM_TOP=13, YSYM_BOT=14,
-            ZSYM_TOP=15, ZSYM_BOT=16, WEST_REG=17)
+            ZSYM_TOP=15, ZSYM_BOT=16, WEST_REG=17, DIR_WEST_V=18, DIR_NORTH=19, DIR_SOUTH=20)
 # FP32 per-cell tolerance (populations O(0.03..0.33)); the same bound as the
 # collide tests, for a map the reference evaluates in another order
 ATOL_CELL = 5e-7
-CPU3D_CODE = {3: "DIR_WEST", 14: "NEU_EAST", 54: "NEU_EAST_REG", 21: "YSYM_TOP", 22: "YSYM_BOT",
+CPU3D_CODE = {3: "DIR_WEST", 13: "DIR_WEST_V", 14: "NEU_EAST", 54: "NEU_EAST_REG", 21: "YSYM_TOP", 22: "YSYM_BOT",
               23: "ZSYM_TOP", 24: "ZSYM_BOT"}
 
 
@@ -74,6 +75,15 @@ def test_cpu3d_boundaries_vs_reference(alt, cellops, orc, im):
     for fn in (cellops.cell_alt_boundary, orc.orc_alt_boundary):
         got = run(fn, kind, f0, yz, dims, u, 0)
         np.testing.assert_array_equal(got, want, err_msg=f"{kind} (CPU_3D im {im})")
+
+
+@pytest.mark.parametrize("north", [1, 0])
+def test_cpu3d_moving_walls_vs_reference(alt, cellops, orc, north):
+    f0, yz, dims, u = alt["cpu3d_f0"], alt["cpu3d_yz"], alt["cpu3d_dims"], float(alt["cpu3d_umax"])
+    want = alt[f"cpu3d_dirichlet_north{north}"]
+    for fn in (cellops.cell_alt_boundary, orc.orc_alt_boundary):
+        got = run(fn, "DIR_NORTH" if north else "DIR_SOUTH", f0, yz, dims, u, 0)
+        np.testing.assert_array_equal(got, want)
 
 
 @pytest.mark.parametrize("top", [1, 0])

@@ -484,6 +484,9 @@ def _alt_bc_mask(case, nx, ny, nz):
         m[:, 0, :] = m[:, -1, :] = N("WALL")
         m[0], m[-1] = N("ZSYM_BOT"), N("ZSYM_TOP")
         m[:, 1:-1, 0], m[:, 1:-1, -1] = N("XSYM_BOT"), N("NEU_EAST_REG")
+    elif case == "moving_walls_west_v":
+        m[:, 0, :], m[:, -1, :] = N("DIR_SOUTH"), N("DIR_NORTH")
+        m[:, 1:-1, 0], m[:, 1:-1, -1] = N("DIR_WEST_V"), N("NEU_EAST")
     else:  # "west_reg_xsym_body"
         m[:, 0, :] = m[:, -1, :] = N("WALL")
         m[:, 1:-1, 0], m[:, 1:-1, -1] = N("WEST_REG"), N("XSYM_TOP")
@@ -499,11 +502,13 @@ def product_node(k):
 
 @pytest.mark.parametrize("case,model,les", [("dirichlet_neumann_ysym", "MRT_CPU3D", 0),
                                             ("xsym_regularised_zsym", "MRT", 1),
-                                            ("west_reg_xsym_body", "BGK", 0)])
+                                            ("west_reg_xsym_body", "BGK", 0),
+                                            ("moving_walls_west_v", "MRT", 0)])
 def test_alternate_boundaries_vs_oracle(product, case, model, les):
     """the alternate boundary node types (CPU_3D's Dirichlet west, Neumann and
-    regularised east, y/z symmetry planes; LR7's x symmetry planes; BC1's
-    West_Reg through its t = 1000 perturbation) in a 30x16x12 box stepped
+    regularised east, y/z symmetry planes, the tangential west inlet and the
+    moving north/south walls; LR7's x symmetry planes; BC1's West_Reg through
+    its t = 1000 perturbation) in a 30x16x12 box stepped
     through lbm_stream_collide_f32, against the oracle's step on the same mask"""
     torch = pytest.importorskip("torch")
     lbm = product
