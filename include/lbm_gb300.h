@@ -305,6 +305,12 @@ int lbm_force_coefficients(const double* fxyz, int n, int t_start, double u, dou
  * sqrt(fluctuation) / u_tau; any output may be NULL */
 int lbm_wall_profile(const float* v_mean, const float* u_fluc, const float* v_fluc, const float* w_fluc, int n,
                      float u_tau, float nu, float* yplus, float* vplus, float* urms, float* vrms, float* wrms);
+/* velplus (TurbChannel3/Re500/velplus.cpp:60-112): on the plane z = nz / 2
+ * of a level's statistics (lbm_get_stats layout), uave[y] = velAv_u / umax
+ * and urms[y] = sqrt(velFluc_u) / umax on x = nx / 2, vave[x], vrms[x] the
+ * same of v on y = ny / 2; any output may be NULL */
+int lbm_centerline_profiles(const float* stats4, int nx, int ny, int nz, double umax, float* uave, float* urms,
+                            float* vave, float* vrms);
 /* profiles along y at x of a level's statistics (lbm_get_stats layout
  * float[4][nz][ny][nx]: velAv u, v, velFluc u, v), averaged over z:
  * prof4[4][ny] */

@@ -78,6 +78,7 @@ SIGNATURES = [
                                     _P, _P, _P]),
     ("lbm_wall_profile", _I, [_P, _P, _P, _P, _I, _F, _F, _P, _P, _P, _P, _P]),
     ("lbm_stats_profiles", _I, [_P, _I, _I, _I, _I, _P]),
+    ("lbm_centerline_profiles", _I, [_P, _I, _I, _I, ctypes.c_double, _P, _P, _P, _P]),
     ("lbm_ensemble_create", _I, [_I, _P, _P, _I, _F, _P]),
     ("lbm_ensemble_destroy", _I, [_P]),
     ("lbm_ensemble_init_turbulence", _I, [_P, ctypes.c_uint32, _F, _I, _I]),
@@ -562,6 +563,18 @@ def wall_profile(v_mean, u_fluc, v_fluc, w_fluc, u_tau: float, nu: float) -> np.
     out = np.zeros((5, n), np.float32)
     _check(library().lbm_wall_profile(*[_ptr(a) for a in arrs], n, _F(u_tau), _F(nu),
                                       *[_ptr(out[k]) for k in range(5)]))
+    return out
+
+
+def centerline_profiles(stats4: np.ndarray, umax: float) -> dict:
+    """velplus: centre-line mean / RMS profiles of the plane z = nz / 2 of
+    statistics float[4][nz][ny][nx], in units of umax"""
+    s = np.ascontiguousarray(stats4, np.float32)
+    _, nz, ny, nx = s.shape
+    out = dict(uave=np.zeros(ny, np.float32), urms=np.zeros(ny, np.float32), vave=np.zeros(nx, np.float32),
+               vrms=np.zeros(nx, np.float32))
+    _check(library().lbm_centerline_profiles(_ptr(s), nx, ny, nz, umax, _ptr(out["uave"]),
+                                             _ptr(out["urms"]), _ptr(out["vave"]), _ptr(out["vrms"])))
     return out
 
 

@@ -9,6 +9,8 @@
  *   VelProf (bgk_channel1/Re3000/VelProf.cpp, MRTtest/bgk/VelProf.cpp,
  *   TurbChannel4/VelProf.cpp): a wall-normal line of mean and fluctuation
  *   statistics in wall units (VelProf.cpp:94-100);
+ *   velplus (TurbChannel3/Re500/velplus.cpp): centre-line mean and RMS
+ *   profiles of the middle z plane, in units of uMax;
  *   mean/fluctuation profiles along y from a level's statistics arrays,
  *   averaged over z (the `_slice.dat` columns velAv / velFluc, LR7:2350-2420).
  */
@@ -128,6 +130,31 @@ int lbm_wall_profile(const float* v_mean, const float* u_fluc, const float* v_fl
         if (urms) urms[i] = std::sqrt(u_fluc[i]) / u_tau;
         if (vrms) vrms[i] = std::sqrt(v_fluc[i]) / u_tau;
         if (wrms) wrms[i] = std::sqrt(w_fluc[i]) / u_tau;
+    }
+    return LBM_OK;
+}
+
+int lbm_centerline_profiles(const float* stats4, int nx, int ny, int nz, double umax, float* uave, float* urms,
+                            float* vave, float* vrms) {
+    if (!stats4 || nx <= 0 || ny <= 0 || nz <= 0 || !(umax > 0))
+        return set_error(LBM_ERR_ARG, "centerline profiles: bad arguments", cudaSuccess);
+    const size_t n = size_t(nx) * ny * nz;
+    const size_t plane = size_t(nz / 2) * ny * nx;
+    const float* au = stats4;
+    const float* av = stats4 + n;
+    const float* fu = stats4 + 2 * n;
+    const float* fv = stats4 + 3 * n;
+    /* u along y on x = nx / 2, v along x on y = ny / 2 (velplus.cpp:94-101);
+     * the division by uMax in double, stored as float as that program does */
+    for (int y = 0; y < ny; ++y) {
+        const size_t c = plane + size_t(y) * nx + nx / 2;
+        if (uave) uave[y] = float(au[c] / umax);
+        if (urms) urms[y] = float(std::sqrt(fu[c]) / umax);
+    }
+    for (int x = 0; x < nx; ++x) {
+        const size_t c = plane + size_t(ny / 2) * nx + x;
+        if (vave) vave[x] = float(av[c] / umax);
+        if (vrms) vrms[x] = float(std::sqrt(fv[c]) / umax);
     }
     return LBM_OK;
 }

@@ -91,6 +91,9 @@ POST_PROGRAMS = {
     "velprof": ("bgk_channel1/Re3000/VelProf.cpp",
                 [(r'string casename = "[^"]*";', 'string casename = "post";'),
                  (r"for\(i = 0; i<xDim; i\+\+\)\{\n\toutput", "for(i = 0; i<xDim/2; i++){\n\toutput")]),
+    "velplus": ("TurbChannel3/Re500/velplus.cpp",
+                [(r"xDim = 128;", "xDim = 24;"), (r"yDim = 128;", "yDim = 24;"), (r"zDim = 16;", "zDim = 6;"),
+                 (r'string casename = "[^"]*";', 'string casename = "post";')]),
 }
 
 

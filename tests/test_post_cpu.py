@@ -96,3 +96,29 @@ def test_stats_profiles_average_over_z(product):
     s = rng.random((4, 6, 10, 12)).astype(np.float32)
     got = lbm.stats_profiles(s, 7)
     np.testing.assert_allclose(got, s[:, :, :, 7].mean(axis=1), rtol=1e-6)
+
+
+def test_centerline_profiles_match_velplus(product, tmp_path):
+    """velplus on a zone file of the reference's WriteResults layout (the
+    writer here produces it), against lbm_centerline_profiles on the
+    statistics as that file prints them"""
+    lbm = product
+    exe = _ref_program("velplus")
+    nx, ny, nz, umax = 24, 24, 6, 0.06  # the staged program's xDim, yDim, zDim and uMax
+    text = lbm.make_inputs(nx, ny, nz, geometry="periodic", umax=umax)
+    rng = np.random.default_rng(11)
+    f = (np.full((19, nz, ny, nx), 1 / 19) + 1e-3 * rng.standard_normal((19, nz, ny, nx))).astype(np.float32)
+    st = np.stack([0.05 + 0.01 * rng.standard_normal((nz, ny, nx)), 0.01 * rng.standard_normal((nz, ny, nx)),
+                   1e-5 * rng.random((nz, ny, nx)), 1e-5 * rng.random((nz, ny, nx))]).astype(np.float32)
+    zone, _ = lbm.format_tecplot(text, f, 0, st)
+    (tmp_path / "post.dat").write_text(zone)
+    subprocess.run([str(exe)], cwd=tmp_path, capture_output=True, text=True, timeout=60, check=True)
+    out = (tmp_path / "post.vel").read_text().splitlines()
+    assert out[0] == "x,u,v,urms,vrms" and len(out) == 1 + nx
+    # the statistics as the zone file holds them
+    rows = np.array([[float(t) for t in line.split(",")] for line in zone.splitlines()[2:]])
+    printed = rows[:, 7:11].T.reshape(4, nz, ny, nx).astype(np.float32)
+    got = lbm.centerline_profiles(printed, umax)
+    for i in range(nx):
+        mine = ",".join([_g(np.float32(i) / nx)] + [_g(got[k][i]) for k in ("uave", "vave", "urms", "vrms")])
+        assert mine == out[1 + i], (i, mine, out[1 + i])
