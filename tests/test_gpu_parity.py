@@ -571,3 +571,41 @@ def test_duct_solver_vs_oracle(product, faces, model, les):
     err, drho = _compare(f, o.fa, mask)
     assert err < RTOL and drho < 1e-5, (err, drho)
     assert rel_l2(F[:, 0], np.array(o.forces)[: len(F), 0]) < FTOL
+
+
+@pytest.mark.parametrize("prec,rel", [("fp16", 2.0 ** -11), ("bf16", 2.0 ** -8)])
+@pytest.mark.parametrize("halfway", [0, 1])
+def test_fp16_bf16_one_step_vs_oracle(product, prec, rel, halfway):
+    """One FP16 / BF16 step from the stored populations of a developed
+    channel flow matches the oracle's FP32 step from the same values to the
+    storage rounding of the stored deviation f - feq(1, (UMAX, 0, 0)): half
+    an ulp of the format, doubled for margin.  A per-value check of the
+    reduced-precision pull, offsets and conversions, sharper than the
+    trajectory comparison against the FP64 twin"""
+    from oracle_bindings import CX
+
+    lbm = product
+    kw = dict(bounceback="halfway") if halfway else {}
+    with lbm.Solver(_chan_inputs(lbm, 60, **kw)) as s:
+        s.step(60)
+        f_dev = s.populations()
+    with lbm.Solver(_chan_inputs(lbm, 60, precision=prec, **kw)) as s:
+        s.set_populations(f_dev)
+        g0 = s.populations()
+        s.step(1)
+        g1, mask, om = s.populations(), s.mask(), s.params()["omega"]
+    o = OracleRun(NX, NY, NZ, mask, om, model=0, les=1, cs=0.01, u_in=0.05, f0=g0, halfway=halfway)
+    o.step(1)
+    w = np.array([1 / 3] + [1 / 18] * 4 + [1 / 36] * 4 + [1 / 18] + [1 / 36] * 4 + [1 / 18] + [1 / 36] * 4)
+    cu = 0.05 * CX.astype(np.float64)
+    off = (w * (1 + 3 * cu + 4.5 * cu ** 2 - 1.5 * 0.05 ** 2))[:, None, None, None]
+    bound = 2 * rel * np.abs(o.fa - off) + 2e-7
+    fl = np.broadcast_to(_fluid(mask), g1.shape)
+    bad = (np.abs(g1 - o.fa) > bound) & fl
+    assert not bad.any(), (int(bad.sum()), float(np.abs(g1 - o.fa)[fl].max()))
+    # the bound resolves the step: without the update, or with the result one
+    # node off in x, many values would fall outside it (oracle on the CPU:
+    # 74 % / 85 % for FP16, 10 % / 40 % for BF16)
+    n = fl.sum()
+    assert ((np.abs(g0 - o.fa) > bound) & fl).sum() > 0.05 * n
+    assert ((np.abs(np.roll(o.fa, 1, axis=-1) - o.fa) > bound) & fl).sum() > 0.3 * n
