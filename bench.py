@@ -174,7 +174,8 @@ def time_e2e(steps: int, world: int, dist) -> dict:
     for i in range(steps):
         s.step(1)
         s.last_force_async(force[i])
-    host_out[...] = s.populations()
+    s.populations(out=host_out)
+    s.synchronize()  # the queued force reads have landed
     t1 = time.perf_counter()
     if dist:
         dist.barrier()

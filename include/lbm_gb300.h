@@ -122,7 +122,8 @@ int lbm_get_forces(lbm_handle* h, double* fxyz, int max_steps, int* n);
 /* the force of the last step (3 doubles; zeros before STARTF) */
 int lbm_get_last_force(lbm_handle* h, double* f3);
 
-/* the same copy queued on the handle's stream without waiting: f3 (pinned
+/* the same copy queued without waiting, behind the force reduction on the
+ * handle's force stream (the step stream does not wait for it): f3 (pinned
  * host memory for a truly asynchronous copy) holds the force once
  * lbm_synchronize returns; lets a monitor read every step's drag without
  * stalling the step loop.  No reference counterpart (the reference copies its

@@ -325,9 +325,17 @@ class Solver:
     def init_equilibrium(self) -> None:
         _check(self._lib.lbm_init_equilibrium(self._h))
 
-    def populations(self, level: int = 0) -> np.ndarray:
+    def populations(self, level: int = 0, out: np.ndarray | None = None) -> np.ndarray:
+        """populations float32[19][nz][ny][nx]; with out (C-contiguous
+        float32 of that shape, e.g. pinned host memory) the copy lands there
+        directly"""
         nx, ny, nz = self.dims(level)
-        f = np.zeros((19, nz, ny, nx), np.float32)
+        if out is None:
+            f = np.empty((19, nz, ny, nx), np.float32)
+        else:
+            f = out
+            if f.dtype != np.float32 or f.shape != (19, nz, ny, nx) or not f.flags["C_CONTIGUOUS"]:
+                raise ValueError(f"out must be C-contiguous float32 of shape {(19, nz, ny, nx)}")
         _check(self._lib.lbm_get_populations(self._h, level, _ptr(f)))
         return f
 

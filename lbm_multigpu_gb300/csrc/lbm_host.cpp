@@ -1129,6 +1129,13 @@ int lbm_get_populations(lbm_handle* h, int level, float* f) {
     if (!f) return fail(LBM_ERR_ARG, "f is null");
     LevelState& s = h->lv[level];
     const size_t n = size_t(s.L.nx) * s.L.ny * s.L.nz * 19;
+    if (s.L.storage == STORE_F32 && s.L.pitch == s.L.nx) {
+        /* FP32 without row padding: the stored layout is the caller's */
+        cudaError_t e = cudaMemcpyAsync(f, s.f[s.cur], n * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "get_populations: %s", cudaGetErrorString(e));
+        return LBM_OK;
+    }
     float* d = nullptr;
     CUDA_TRY(cudaMallocAsync((void**)&d, n * sizeof(float), h->stream));
     cudaError_t e = launch_pack(s.L, s.f[s.cur], d, h->stream);
@@ -1145,6 +1152,15 @@ int lbm_set_populations(lbm_handle* h, int level, const float* f) {
     if (!f) return fail(LBM_ERR_ARG, "f is null");
     LevelState& s = h->lv[level];
     const size_t n = size_t(s.L.nx) * s.L.ny * s.L.nz * 19;
+    if (s.L.storage == STORE_F32 && s.L.pitch == s.L.nx) {
+        /* FP32 without row padding: straight into both buffers */
+        cudaError_t e = cudaMemcpyAsync(s.f[0], f, n * sizeof(float), cudaMemcpyHostToDevice, h->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s.f[1], s.f[0], n * sizeof(float), cudaMemcpyDeviceToDevice, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "set_populations: %s", cudaGetErrorString(e));
+        return LBM_OK;
+    }
     float* d = nullptr;
     CUDA_TRY(cudaMallocAsync((void**)&d, n * sizeof(float), h->stream));
     cudaError_t e = cudaMemcpyAsync(d, f, n * sizeof(float), cudaMemcpyHostToDevice, h->stream);
@@ -1176,6 +1192,7 @@ int lbm_step_timed(lbm_handle* h, int nsteps, float* ms) {
 int lbm_synchronize(lbm_handle* h) {
     if (!h) return fail(LBM_ERR_ARG, "null handle");
     CUDA_TRY(cudaStreamSynchronize(h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->side));
     if (h->mlp_err) {
         int e = 0;
         CUDA_TRY(cudaMemcpy(&e, h->mlp_err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1446,7 +1463,9 @@ int lbm_get_last_force_async(lbm_handle* h, double* f3) {
         f3[0] = f3[1] = f3[2] = 0.0;
         return LBM_OK;
     }
-    CUDA_TRY(cudaMemcpyAsync(f3, h->force_hist + 3LL * i, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    /* on the force stream, behind the kernel that wrote the entry: the step
+     * stream does not wait for the copy */
+    CUDA_TRY(cudaMemcpyAsync(f3, h->force_hist + 3LL * i, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->side));
     return LBM_OK;
 }
 
