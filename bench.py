@@ -216,6 +216,11 @@ def cpu_baseline(max_samples: int = 1) -> dict:
         return dict(value=statistics.mean(vals), unit="MLUPS", cores=1, kind="reference",
                     sample=f"CPU_3D/CPU_3D.cpp (staged, g++ -O3), 512x128x128, {steps} steps "
                            f"x {len(vals)} run(s), {secs:.1f} s of loop time; its lid-cavity MRT at the same shape")
+    return oracle_baseline()
+
+
+def oracle_baseline() -> dict:
+    """the oracle's OpenMP restatement of the same step on all host cores"""
     sys.path.insert(0, str(ROOT / "tests"))
     import numpy as np
 
@@ -514,6 +519,8 @@ def main():
                                    kernel="k_stream_collide_mlp<fp32>", weights=str(SGS_WEIGHTS.relative_to(ROOT)))
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
+        if line["cpu_baseline"]["kind"] == "reference":
+            line["cpu_port"] = oracle_baseline()
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
