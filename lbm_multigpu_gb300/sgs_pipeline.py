@@ -18,7 +18,12 @@ Acoustic scaling between the grids: same lattice velocity, dt_c = 2 dt_f,
 nu_f (lattice) = 2 nu_c (lattice), so tau_f - 1/2 = 2 (tau_c - 1/2) and one
 coarse step is two fine steps.
 
+4. The same three closures in the square-cylinder channel against its 2x
+   run (channel_profiles): mean-velocity and fluctuation profiles behind
+   the cylinder.
+
 Run:  python -m lbm_multigpu_gb300.sgs_pipeline --out weights.bin
+      python -m lbm_multigpu_gb300.sgs_pipeline channel --weights weights.bin
 """
 from __future__ import annotations
 
@@ -145,6 +150,92 @@ def evaluate(params: np.ndarray, sizes: list[int], seed: int, coarse_steps: int 
     return out
 
 
+def _channel_run(nx: int, ny: int, nz: int, centre: tuple[float, float], half: float, tau: float, sgs: str,
+                 params, spinup: int, mean_steps: int, fluc_steps: int, seed: int, chunk: int = 2000):
+    """one square-cylinder channel run (MRT, half-way walls, inlet 0.05 with
+    1 % seeded noise) with running statistics: the mean over
+    [spinup, spinup + mean_steps), the variance about it over the next
+    fluc_steps.  Returns the statistics, or None if the run blew up."""
+    from . import Solver, make_inputs
+
+    t_end = spinup + mean_steps + fluc_steps
+    kw = dict(sgs="mlp") if sgs == "mlp" else {}
+    text = make_inputs(nx, ny, nz, obst1=(centre[0], centre[1], 0.0), r1=half, umax=0.05, tmax=t_end,
+                       les=0 if sgs == "none" else 1, cs=CS, model="MRT", geometry="channel_square", tau=tau,
+                       velav=1, start_velav=spinup, start_velfluc=spinup + mean_steps, inlet_noise=0.01, seed=seed,
+                       bounceback="halfway", **kw)
+    with Solver(text) as s:
+        if sgs == "mlp":
+            s.set_sgs_mlp(params)
+        t = 0
+        while t < t_end:
+            k = min(chunk, t_end - t)
+            s.step(k)
+            t += k
+        st = s.stats()
+    return st if np.isfinite(st).all() else None
+
+
+def channel_profiles(params: np.ndarray, coarse=(192, 64, 32), side: int = 8, spinup: int = 4000,
+                     mean_steps: int = 4000, fluc_steps: int = 4000, stations=(1, 2, 4, 8), seed: int = 12345,
+                     models=("none", "smagorinsky", "mlp")):
+    """a-posteriori comparison in the C2 geometry family: a square cylinder
+    of side `side` in a channel (coarse grid `coarse`, tau0 = TAU_C, i.e.
+    Re = 3 * 0.05 * side / (TAU_C - 1/2)) run with no model, Smagorinsky and
+    the learned closure, against the same channel at 2x resolution
+    (tau_f = TAU_F, molecular viscosity only, twice the steps), whose
+    statistics are box-filtered 2 x 2 in x and y (z is averaged) onto the
+    coarse stations.  Profiles along y, z-averaged, at `stations` cylinder
+    sides behind the rear face: mean u, and the rms of u and v.  Returns the
+    relative L2 error of each against the filtered fine profiles (walls
+    excluded), and the profiles themselves.
+
+    The fine walls sit half a coarse cell outside the coarse ones (both
+    grids put the half-way wall half a spacing off their first node); the
+    fine variances include the fluctuations below the coarse filter width."""
+    from . import stats_profiles
+
+    nx, ny, nz = coarse
+    half = side / 2
+    cx, cy = nx // 6 + 0.5, ny // 2 - 0.5               # coarse centre (a node boundary on both axes)
+    fine = _channel_run(2 * nx, 2 * ny, 2 * nz, (2 * cx + 0.5, 2 * cy + 0.5), 2 * half, TAU_F, "none", None,
+                        2 * spinup, 2 * mean_steps, 2 * fluc_steps, seed)
+    if fine is None:
+        raise FloatingPointError("the 2x reference channel run went unstable")
+    rear = int(np.floor(cx + half))                     # last coarse node inside the cylinder
+    xs = [rear + k * side for k in stations if rear + k * side < nx - 1]
+
+    def fine_profile(x: int) -> np.ndarray:
+        p = 0.5 * (stats_profiles(fine, 2 * x) + stats_profiles(fine, 2 * x + 1))   # (4, 2 ny)
+        return p.reshape(4, ny, 2).mean(axis=2)
+
+    truth = np.stack([fine_profile(x) for x in xs])      # (stations, 4, ny)
+    out = dict(stations=xs, coarse=list(coarse), side=side, tau_c=TAU_C, tau_f=TAU_F,
+               re=3 * 0.05 * side / (TAU_C - 0.5), steps=[spinup, mean_steps, fluc_steps])
+    inner = slice(1, ny - 1)
+
+    def rel(a: np.ndarray, b: np.ndarray) -> float:
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    def measures(prof: np.ndarray) -> dict:
+        rms = np.sqrt(np.maximum(prof[:, 2:4], 0.0))
+        rms_t = np.sqrt(np.maximum(truth[:, 2:4], 0.0))
+        return dict(u_mean_rel_l2=rel(prof[:, 0, inner], truth[:, 0, inner]),
+                    u_rms_rel_l2=rel(rms[:, 0, inner], rms_t[:, 0, inner]),
+                    v_rms_rel_l2=rel(rms[:, 1, inner], rms_t[:, 1, inner]))
+
+    profiles = dict(truth=truth)
+    for name in models:
+        st = _channel_run(nx, ny, nz, (cx, cy), half, TAU_C, name, params, spinup, mean_steps, fluc_steps, seed)
+        if st is None:
+            out[name] = "unstable"
+            continue
+        prof = np.stack([stats_profiles(st, x) for x in xs])
+        profiles[name] = prof
+        out[name] = measures(prof)
+    return out, profiles
+
+
 def calibrate(X, T, sizes: list[int], seed: int, alphas, steps: int, batch: int, lr: float, train_seed: int):
     """scale of the training targets chosen a posteriori on boxes of the
     training distribution (the least-squares eddy viscosity of the filtered
@@ -160,7 +251,39 @@ def calibrate(X, T, sizes: list[int], seed: int, alphas, steps: int, batch: int,
     return res[0][1], res[0][2], res[0][3], [(float(a), float(e)) for e, a, _, _ in res]
 
 
+def channel_main(argv) -> int:
+    """python -m lbm_multigpu_gb300.sgs_pipeline channel --weights W [--report R]"""
+    ap = argparse.ArgumentParser(description="learned closure vs Smagorinsky in the square-cylinder channel")
+    ap.add_argument("--weights", required=True, help="float32 parameter file")
+    ap.add_argument("--coarse", default="192x64x32")
+    ap.add_argument("--side", type=int, default=8)
+    ap.add_argument("--steps", default="4000,4000,4000", help="spin-up, mean, fluctuation coarse steps")
+    ap.add_argument("--seed", type=int, default=12345)
+    ap.add_argument("--report", default=None, help="JSON report path")
+    ap.add_argument("--profiles", default=None, help=".npz of the profiles")
+    a = ap.parse_args(argv)
+    P = np.fromfile(a.weights, dtype="<f4")
+    coarse = tuple(int(v) for v in a.coarse.split("x"))
+    sp, ms, fs = (int(v) for v in a.steps.split(","))
+    t0 = time.perf_counter()
+    out, prof = channel_profiles(P, coarse, a.side, sp, ms, fs, seed=a.seed)
+    out["seconds"] = time.perf_counter() - t0
+    out["weights"] = a.weights
+    print(json.dumps(out))
+    if a.report:
+        with open(a.report, "w") as f:
+            json.dump(out, f, indent=1)
+    if a.profiles:
+        np.savez_compressed(a.profiles, **prof)
+    return 0
+
+
 def main(argv=None) -> int:
+    import sys
+
+    argv = sys.argv[1:] if argv is None else argv
+    if argv and argv[0] == "channel":
+        return channel_main(argv[1:])
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--out", required=True, help="float32 parameter file (lbm_mlp_param_count values)")
     ap.add_argument("--seed", type=int, default=2024)

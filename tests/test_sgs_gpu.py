@@ -199,3 +199,26 @@ def test_trained_closure_beats_smagorinsky_on_held_out_boxes(product):
     mlp, smag, none = ev["mlp"], ev["smagorinsky"], ev["none"]
     assert mlp["energy_rel_l2"] < smag["energy_rel_l2"] < none["energy_rel_l2"], ev
     assert mlp["spectrum_log_rms"] < smag["spectrum_log_rms"], ev
+
+
+def test_channel_comparison_runs(product):
+    """channel_profiles on a small case: every model's statistics exist,
+    the filtered 2x profiles are finite with a wake (reversed or slowed
+    mean flow and fluctuations behind the cylinder), and each model's
+    errors are finite numbers.  Which closure wins is reported, not asserted
+    (the committed weights lose to Smagorinsky in the wake)."""
+    import numpy as np
+
+    from lbm_multigpu_gb300 import sgs_pipeline
+
+    P = np.fromfile(product.__path__[0] + "/data/sgs_mlp.bin", dtype="<f4")
+    out, prof = sgs_pipeline.channel_profiles(P, coarse=(96, 32, 8), side=4, spinup=600, mean_steps=400,
+                                              fluc_steps=400, stations=(1, 2, 4))
+    assert out["stations"] == [22, 26, 34]  # rear face at x = 18, side 4
+    truth = prof["truth"]
+    assert truth.shape == (3, 4, 32) and np.isfinite(truth).all()
+    assert truth[0, 0, 14:18].mean() < 0.7 * truth[0, 0, 3:7].mean()  # slowed behind the cylinder
+    assert (truth[:, 2, 1:-1] >= 0).all() and truth[:, 2].max() > 0
+    for name in ("smagorinsky", "mlp"):
+        assert isinstance(out[name], dict), name
+        assert all(np.isfinite(v) and v > 0 for v in out[name].values()), out[name]
