@@ -150,20 +150,107 @@ def evaluate(params: np.ndarray, sizes: list[int], seed: int, coarse_steps: int 
     return out
 
 
+def features_np(p: np.ndarray, tau0: float) -> np.ndarray:
+    """the closure's 16 inputs (as the collide kernel forms them, sgs_mlp.cuh)
+    of p_ij = [xx, yy, zz, xy, xz, yz] (shape (6, n)), in float64"""
+    P_REF = S_REF = 0.01
+    xx, yy, zz, xy, xz, yz = p
+    pp = xx * xx + yy * yy + zz * zz + 2 * (xy * xy + xz * xz + yz * yz)
+    tr3 = (xx ** 3 + yy ** 3 + zz ** 3 + 3 * xx * (xy * xy + xz * xz) + 3 * yy * (xy * xy + yz * yz) +
+           3 * zz * (xz * xz + yz * yz) + 6 * xy * xz * yz)
+    x = np.empty((16, p.shape[1]))
+    x[0:6] = p / P_REF
+    x[6:12] = p / tau0 / S_REF
+    x[12] = np.sqrt(2 * pp) / P_REF
+    with np.errstate(divide="ignore", invalid="ignore"):
+        x[13] = np.where(pp > 1e-30, tr3 / (pp * np.sqrt(np.maximum(pp, 1e-300))), 0.0)
+    x[14] = (tau0 - 0.5) * 100
+    x[15] = 1.0
+    return x.T
+
+
+def samples_from_velocity(u: np.ndarray, fluid: np.ndarray, tau0: float, margin: int = 2):
+    """training samples of a 2x-resolution field that is periodic in z only:
+    u float[3][fz][fy][fx] and fluid bool[fz][fy][fx] (nodes that are plain
+    fluid).  As the ensemble's samples (2x2x2 box filter, central-difference
+    strain of the filtered velocity, the deviatoric subgrid stress, 3x3x3
+    averages of tau^d:S and S:S, nu = max(0, -<tau^d:S> / (2 <S:S>)),
+    features of p = (tau0 + 3 nu) S), on the coarse cells whose filter
+    boxes, and those of their neighbours up to `margin` cells in x and y, hold
+    fluid only.  Returns X float32[n][16], T float32[n]."""
+    _, fz, fy, fx = u.shape
+    cz, cy, cx = fz // 2, fy // 2, fx // 2
+
+    def box(a):
+        return a.reshape(a.shape[:-3] + (cz, 2, cy, 2, cx, 2)).mean(axis=(-5, -3, -1))
+
+    ub = box(u.astype(np.float64))
+    uu = box(np.stack([u[0] * u[0], u[1] * u[1], u[2] * u[2], u[0] * u[1], u[0] * u[2], u[1] * u[2]]).astype(np.float64))
+    ok = box(fluid.astype(np.float64)) == 1.0
+
+    def d(a, axis):
+        return 0.5 * (np.roll(a, -1, axis) - np.roll(a, 1, axis))
+
+    g = np.stack([np.stack([d(ub[k], 2), d(ub[k], 1), d(ub[k], 0)]) for k in range(3)])  # g[k][axis x,y,z]
+    S = np.stack([g[0, 0], g[1, 1], g[2, 2], 0.5 * (g[0, 1] + g[1, 0]), 0.5 * (g[0, 2] + g[2, 0]),
+                  0.5 * (g[1, 2] + g[2, 1])])
+    tau = uu - np.stack([ub[0] * ub[0], ub[1] * ub[1], ub[2] * ub[2], ub[0] * ub[1], ub[0] * ub[2], ub[1] * ub[2]])
+    tau[:3] -= tau[:3].sum(0) / 3
+    w = np.array([1, 1, 1, 2, 2, 2], np.float64)[:, None, None, None]
+    ts, ss = (w * tau * S).sum(0), (w * S * S).sum(0)
+
+    def avg3(a):
+        out = np.zeros_like(a)
+        for dz in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dx in (-1, 0, 1):
+                    out += np.roll(a, (dz, dy, dx), axis=(0, 1, 2))
+        return out
+
+    ts, ss = avg3(ts), avg3(ss)
+    valid = ok.copy()
+    for dy in range(-margin, margin + 1):
+        for dx in range(-margin, margin + 1):
+            valid &= np.roll(ok, (dy, dx), axis=(1, 2))
+    if margin > 0:
+        valid[:, :margin, :] = valid[:, -margin:, :] = False
+        valid[:, :, :margin] = valid[:, :, -margin:] = False
+    with np.errstate(divide="ignore", invalid="ignore"):
+        nu = np.where(ss > 1e-30, np.maximum(-ts / (2 * ss), 0.0), 0.0)
+    nu = nu[valid]
+    p = (tau0 + 3 * nu) * S[:, valid]
+    return features_np(p, tau0).astype(np.float32), nu.astype(np.float32)
+
+
+def _channel_record(nx: int, ny: int, nz: int, centre: tuple[float, float], half: float, tau: float, sgs: str,
+                    tmax: int, seed: int, stats: tuple[int, int] | None = None) -> str:
+    """the square-cylinder channel (MRT, half-way walls, inlet 0.05 with 1 %
+    seeded noise); stats = (start of the mean, start of the variance)"""
+    from . import make_inputs
+
+    kw = dict(sgs="mlp") if sgs == "mlp" else {}
+    if stats:
+        kw.update(velav=1, start_velav=stats[0], start_velfluc=stats[1])
+    return make_inputs(nx, ny, nz, obst1=(centre[0], centre[1], 0.0), r1=half, umax=0.05, tmax=tmax,
+                       les=0 if sgs == "none" else 1, cs=CS, model="MRT", geometry="channel_square", tau=tau,
+                       inlet_noise=0.01, seed=seed, bounceback="halfway", **kw)
+
+
+def _channel_geometry(coarse, side: int):
+    """coarse centre (a node boundary on both axes) and half side"""
+    nx, ny, _ = coarse
+    return (nx // 6 + 0.5, ny // 2 - 0.5), side / 2
+
+
 def _channel_run(nx: int, ny: int, nz: int, centre: tuple[float, float], half: float, tau: float, sgs: str,
                  params, spinup: int, mean_steps: int, fluc_steps: int, seed: int, chunk: int = 2000):
-    """one square-cylinder channel run (MRT, half-way walls, inlet 0.05 with
-    1 % seeded noise) with running statistics: the mean over
+    """one channel run with running statistics: the mean over
     [spinup, spinup + mean_steps), the variance about it over the next
     fluc_steps.  Returns the statistics, or None if the run blew up."""
-    from . import Solver, make_inputs
+    from . import Solver
 
     t_end = spinup + mean_steps + fluc_steps
-    kw = dict(sgs="mlp") if sgs == "mlp" else {}
-    text = make_inputs(nx, ny, nz, obst1=(centre[0], centre[1], 0.0), r1=half, umax=0.05, tmax=t_end,
-                       les=0 if sgs == "none" else 1, cs=CS, model="MRT", geometry="channel_square", tau=tau,
-                       velav=1, start_velav=spinup, start_velfluc=spinup + mean_steps, inlet_noise=0.01, seed=seed,
-                       bounceback="halfway", **kw)
+    text = _channel_record(nx, ny, nz, centre, half, tau, sgs, t_end, seed, (spinup, spinup + mean_steps))
     with Solver(text) as s:
         if sgs == "mlp":
             s.set_sgs_mlp(params)
@@ -176,28 +263,49 @@ def _channel_run(nx: int, ny: int, nz: int, centre: tuple[float, float], half: f
     return st if np.isfinite(st).all() else None
 
 
-def channel_profiles(params: np.ndarray, coarse=(192, 64, 32), side: int = 8, spinup: int = 4000,
-                     mean_steps: int = 4000, fluc_steps: int = 4000, stations=(1, 2, 4, 8), seed: int = 12345,
-                     models=("none", "smagorinsky", "mlp")):
-    """a-posteriori comparison in the C2 geometry family: a square cylinder
-    of side `side` in a channel (coarse grid `coarse`, tau0 = TAU_C, i.e.
-    Re = 3 * 0.05 * side / (TAU_C - 1/2)) run with no model, Smagorinsky and
-    the learned closure, against the same channel at 2x resolution
-    (tau_f = TAU_F, molecular viscosity only, twice the steps), whose
-    statistics are box-filtered 2 x 2 in x and y (z is averaged) onto the
-    coarse stations.  Profiles along y, z-averaged, at `stations` cylinder
-    sides behind the rear face: mean u, and the rms of u and v.  Returns the
-    relative L2 error of each against the filtered fine profiles (walls
-    excluded), and the profiles themselves.
+def generate_channel(coarse=(160, 64, 32), side: int = 8, seed: int = 777, spinup: int = 6000, snapshots: int = 12,
+                     every: int = 500):
+    """training samples from the square-cylinder channel at 2x resolution
+    (tau_f, no model), taken every `every` coarse steps after `spinup`"""
+    import torch
 
-    The fine walls sit half a coarse cell outside the coarse ones (both
-    grids put the half-way wall half a spacing off their first node); the
-    fine variances include the fluctuations below the coarse filter width."""
+    from . import Solver
+
+    nx, ny, nz = coarse
+    (cx, cy), half = _channel_geometry(coarse, side)
+    t_end = 2 * (spinup + snapshots * every)
+    text = _channel_record(2 * nx, 2 * ny, 2 * nz, (2 * cx + 0.5, 2 * cy + 0.5), 2 * half, TAU_F, "none", t_end, seed)
+    Xs, Ts = [], []
+    t0 = time.perf_counter()
+    with Solver(text) as s:
+        fluid = s.mask() == 0
+        s.step(2 * spinup)
+        for _ in range(snapshots):
+            s.step(2 * every)
+            rho, jx, jy, jz = s.fields()
+            if not np.isfinite(rho).all():
+                raise FloatingPointError("the 2x channel run for training went unstable")
+            X, T = samples_from_velocity(np.stack([jx, jy, jz]) / rho, fluid, TAU_C)
+            Xs.append(X)
+            Ts.append(T)
+    X, T = np.concatenate(Xs), np.concatenate(Ts)
+    info = dict(coarse=list(coarse), side=side, seed=seed, spinup=spinup, snapshots=snapshots, every=every,
+                samples=int(len(T)), seconds=time.perf_counter() - t0)
+    return torch.from_numpy(X).cuda(), torch.from_numpy(T).cuda(), info
+
+
+def channel_truth(coarse=(192, 64, 32), side: int = 8, spinup: int = 4000, mean_steps: int = 4000,
+                  fluc_steps: int = 4000, stations=(1, 2, 4, 8), seed: int = 12345) -> dict:
+    """the reference of the channel comparison: the square cylinder of side
+    `side` in a channel on the 2x grid (tau_f = TAU_F, molecular viscosity
+    only, twice the steps), its statistics box-filtered 2 x 2 in x and y
+    (z is averaged) onto the coarse stations `stations` cylinder sides
+    behind the rear face.  Profiles along y: mean u, mean v, variance of u,
+    variance of v (truth: float[stations][4][ny])."""
     from . import stats_profiles
 
     nx, ny, nz = coarse
-    half = side / 2
-    cx, cy = nx // 6 + 0.5, ny // 2 - 0.5               # coarse centre (a node boundary on both axes)
+    (cx, cy), half = _channel_geometry(coarse, side)
     fine = _channel_run(2 * nx, 2 * ny, 2 * nz, (2 * cx + 0.5, 2 * cy + 0.5), 2 * half, TAU_F, "none", None,
                         2 * spinup, 2 * mean_steps, 2 * fluc_steps, seed)
     if fine is None:
@@ -209,46 +317,90 @@ def channel_profiles(params: np.ndarray, coarse=(192, 64, 32), side: int = 8, sp
         p = 0.5 * (stats_profiles(fine, 2 * x) + stats_profiles(fine, 2 * x + 1))   # (4, 2 ny)
         return p.reshape(4, ny, 2).mean(axis=2)
 
-    truth = np.stack([fine_profile(x) for x in xs])      # (stations, 4, ny)
-    out = dict(stations=xs, coarse=list(coarse), side=side, tau_c=TAU_C, tau_f=TAU_F,
-               re=3 * 0.05 * side / (TAU_C - 0.5), steps=[spinup, mean_steps, fluc_steps])
-    inner = slice(1, ny - 1)
+    return dict(truth=np.stack([fine_profile(x) for x in xs]), stations=xs, coarse=tuple(coarse), side=side,
+                steps=(spinup, mean_steps, fluc_steps), seed=seed)
+
+
+def channel_errors(params, ref: dict, models=("none", "smagorinsky", "mlp")):
+    """the coarse runs of `models` (tau0 = TAU_C) against `ref`
+    (channel_truth): relative L2 of the mean-u, u-rms and v-rms profiles
+    (walls excluded), "unstable" for a run that blew up; and the profiles"""
+    from . import stats_profiles
+
+    nx, ny, nz = ref["coarse"]
+    (cx, cy), half = _channel_geometry(ref["coarse"], ref["side"])
+    truth, inner = ref["truth"], slice(1, ny - 1)
 
     def rel(a: np.ndarray, b: np.ndarray) -> float:
         return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
-    def measures(prof: np.ndarray) -> dict:
-        rms = np.sqrt(np.maximum(prof[:, 2:4], 0.0))
-        rms_t = np.sqrt(np.maximum(truth[:, 2:4], 0.0))
-        return dict(u_mean_rel_l2=rel(prof[:, 0, inner], truth[:, 0, inner]),
-                    u_rms_rel_l2=rel(rms[:, 0, inner], rms_t[:, 0, inner]),
-                    v_rms_rel_l2=rel(rms[:, 1, inner], rms_t[:, 1, inner]))
-
-    profiles = dict(truth=truth)
+    rms_t = np.sqrt(np.maximum(truth[:, 2:4], 0.0))
+    out, profiles = {}, {}
     for name in models:
-        st = _channel_run(nx, ny, nz, (cx, cy), half, TAU_C, name, params, spinup, mean_steps, fluc_steps, seed)
+        st = _channel_run(nx, ny, nz, (cx, cy), half, TAU_C, name, params, *ref["steps"], ref["seed"])
         if st is None:
             out[name] = "unstable"
             continue
-        prof = np.stack([stats_profiles(st, x) for x in xs])
+        prof = np.stack([stats_profiles(st, x) for x in ref["stations"]])
+        rms = np.sqrt(np.maximum(prof[:, 2:4], 0.0))
         profiles[name] = prof
-        out[name] = measures(prof)
+        out[name] = dict(u_mean_rel_l2=rel(prof[:, 0, inner], truth[:, 0, inner]),
+                         u_rms_rel_l2=rel(rms[:, 0, inner], rms_t[:, 0, inner]),
+                         v_rms_rel_l2=rel(rms[:, 1, inner], rms_t[:, 1, inner]))
     return out, profiles
 
 
-def calibrate(X, T, sizes: list[int], seed: int, alphas, steps: int, batch: int, lr: float, train_seed: int):
-    """scale of the training targets chosen a posteriori on boxes of the
-    training distribution (the least-squares eddy viscosity of the filtered
+def channel_profiles(params: np.ndarray, coarse=(192, 64, 32), side: int = 8, spinup: int = 4000,
+                     mean_steps: int = 4000, fluc_steps: int = 4000, stations=(1, 2, 4, 8), seed: int = 12345,
+                     models=("none", "smagorinsky", "mlp")):
+    """a-posteriori comparison in the C2 geometry family: a square cylinder
+    in a channel (coarse grid `coarse`, tau0 = TAU_C, i.e.
+    Re = 3 * 0.05 * side / (TAU_C - 1/2)) run with no model, Smagorinsky and
+    the learned closure, against the same channel at 2x resolution
+    (channel_truth).  Returns the errors (channel_errors) with the setup, and
+    the profiles (the reference as "truth").
+
+    The fine walls sit half a coarse cell outside the coarse ones (both
+    grids put the half-way wall half a spacing off their first node); the
+    fine variances include the fluctuations below the coarse filter width."""
+    ref = channel_truth(coarse, side, spinup, mean_steps, fluc_steps, stations, seed)
+    out = dict(stations=ref["stations"], coarse=list(coarse), side=side, tau_c=TAU_C, tau_f=TAU_F,
+               re=3 * 0.05 * side / (TAU_C - 0.5), steps=[spinup, mean_steps, fluc_steps])
+    errs, profiles = channel_errors(params, ref, models)
+    out.update(errs)
+    profiles["truth"] = ref["truth"]
+    return out, profiles
+
+
+def calibrate(X, T, sizes: list[int], seed: int, alphas, steps: int, batch: int, lr: float, train_seed: int,
+              channel_ref: dict | None = None):
+    """scale of the training targets chosen a posteriori on configurations
+    of the training data (the least-squares eddy viscosity of the filtered
     stress is an a-priori estimate; the coarse solver has numerical
-    dissipation of its own): the scale whose closure best reproduces the
-    filtered 2x energy history"""
+    dissipation of its own).  Score of a scale: the filtered-2x energy-history
+    error on the training-seed boxes relative to Smagorinsky's, plus, with
+    `channel_ref` (channel_truth of the training channel), the mean-u and
+    u-rms profile errors relative to Smagorinsky's there.  Lowest score wins."""
+    base = evaluate(np.zeros(0, np.float32), sizes, seed, coarse_steps=600, models=("smagorinsky",))
+    iso_smag = base["smagorinsky"]["energy_rel_l2"]
+    if channel_ref is not None:
+        cs_err, _ = channel_errors(None, channel_ref, ("smagorinsky",))
+        chan_smag = cs_err["smagorinsky"]["u_mean_rel_l2"] + cs_err["smagorinsky"]["u_rms_rel_l2"]
     res = []
     for a in alphas:
         P, hist, _ = train(X, T, steps, batch, lr, train_seed, scale=a)
         ev = evaluate(P, sizes, seed, coarse_steps=600, models=("mlp",))
-        res.append((ev["mlp"]["energy_rel_l2"], a, P, hist))
-    res.sort(key=lambda r: r[0] if np.isfinite(r[0]) else np.inf)
-    return res[0][1], res[0][2], res[0][3], [(float(a), float(e)) for e, a, _, _ in res]
+        parts = dict(iso=ev["mlp"]["energy_rel_l2"] / iso_smag)
+        if channel_ref is not None:
+            ce, _ = channel_errors(P, channel_ref, ("mlp",))
+            m = ce["mlp"]
+            parts["channel"] = (m["u_mean_rel_l2"] + m["u_rms_rel_l2"]) / chan_smag if isinstance(m, dict) else np.inf
+        score = float(sum(parts.values()))
+        res.append((score if np.isfinite(score) else np.inf, a, P, hist, parts))
+    res.sort(key=lambda r: r[0])
+    table = [dict(alpha=float(a), score=float(sc), **{k: float(v) for k, v in pt.items()})
+             for sc, a, _, _, pt in res]
+    return res[0][1], res[0][2], res[0][3], table
 
 
 def channel_main(argv) -> int:
@@ -295,23 +447,42 @@ def main(argv=None) -> int:
     ap.add_argument("--report", default=None, help="JSON report path")
     ap.add_argument("--alphas", default="0.3,0.4,0.5,0.6,0.7,0.85",
                     help="candidate target scales for the a-posteriori calibration")
+    ap.add_argument("--channel-train", default="160x64x32",
+                    help="coarse size of the training channel ('' for isotropic boxes only)")
+    ap.add_argument("--channel-seed", type=int, default=777)
+    ap.add_argument("--channel-eval", default="192x64x32", help="coarse size of the held-out channel")
+    ap.add_argument("--channel-eval-seed", type=int, default=12345)
+    ap.add_argument("--channel-steps", default="6000,6000,6000", help="spin-up, mean, fluctuation coarse steps")
     a = ap.parse_args(argv)
+    import torch
+
     sizes = ensemble_sizes(a.seed, a.members)
     X, T, gen = generate(sizes, a.seed)
+    ch_steps = tuple(int(v) for v in a.channel_steps.split(","))
+    chan_gen, chan_ref = None, None
+    if a.channel_train:
+        coarse = tuple(int(v) for v in a.channel_train.split("x"))
+        Xc, Tc, chan_gen = generate_channel(coarse, seed=a.channel_seed)
+        X, T = torch.cat([X, Xc]), torch.cat([T, Tc])
+        chan_ref = channel_truth(coarse, 8, *ch_steps, seed=a.channel_seed)
     t0 = time.perf_counter()
     eval_sizes = [int(v) for v in a.eval_sizes.split(",")]
-    # calibration boxes: the evaluation sizes with the training seed's fields
+    # calibration: the evaluation sizes with the training seed's fields, and
+    # the training channel
     alpha, P, hist, table = calibrate(X, T, eval_sizes, a.seed, [float(v) for v in a.alphas.split(",")],
-                                      a.train_steps, a.batch, a.lr, a.seed)
+                                      a.train_steps, a.batch, a.lr, a.seed, chan_ref)
     secs = time.perf_counter() - t0
     P.astype("<f4").tofile(a.out)
-    # held out: a different seed for the initial fields
+    # held out: a different seed for the initial fields, another channel
     ev = evaluate(P, eval_sizes, a.seed + 1)
-    rep = dict(generate=gen, train=dict(steps=a.train_steps, batch=a.batch, lr=a.lr, seconds_with_calibration=secs,
-                                        alpha=alpha, calibration=table, loss_first=float(hist[:10].mean()),
-                                        loss_last=float(hist[-50:].mean()), target_mean=float(T.mean().item()),
-                                        target_std=float(T.std().item())),
-               evaluate=ev, weights=a.out)
+    ch_eval, _ = channel_profiles(P, tuple(int(v) for v in a.channel_eval.split("x")), 8, *ch_steps,
+                                  seed=a.channel_eval_seed)
+    rep = dict(generate=gen, generate_channel=chan_gen,
+               train=dict(steps=a.train_steps, batch=a.batch, lr=a.lr, seconds_with_calibration=secs,
+                          alpha=alpha, calibration=table, loss_first=float(hist[:10].mean()),
+                          loss_last=float(hist[-50:].mean()), target_mean=float(T.mean().item()),
+                          target_std=float(T.std().item()), samples=int(T.shape[0])),
+               evaluate=ev, evaluate_channel=ch_eval, weights=a.out)
     print(json.dumps(rep))
     if a.report:
         with open(a.report, "w") as f:

@@ -105,3 +105,39 @@ def test_oracle_box_filter_and_target():
     o.orc_box_filter(ptr(u2), fx, fy, fz, ptr(ub), ptr(uu))
     o.orc_sgs_targets(ptr(ub), ptr(uu), 8, 8, 8, ctypes.c_double(0.52), ptr(X), ptr(T))
     assert T.min() >= 0 and T.max() > 0
+
+
+def test_host_samples_match_the_oracle_on_a_periodic_field(orc):
+    """the host sample extraction used for channel runs (samples_from_velocity,
+    features_np) reproduces the oracle's box filter, least-squares targets
+    and features on a periodic field (all fluid, no margin)"""
+    from lbm_multigpu_gb300.sgs_pipeline import samples_from_velocity
+
+    rng = np.random.default_rng(5)
+    fz, fy, fx = 12, 16, 20
+    u = (0.03 * rng.standard_normal((3, fz, fy, fx))).astype(np.float32)
+    ub = np.zeros(3 * (fx // 2) * (fy // 2) * (fz // 2))
+    uu = np.zeros(6 * (fx // 2) * (fy // 2) * (fz // 2))
+    n = (fx // 2) * (fy // 2) * (fz // 2)
+    Xo, To = np.zeros((n, 16), np.float32), np.zeros(n, np.float32)
+    orc.orc_box_filter(ptr(u), fx, fy, fz, ptr(ub), ptr(uu))
+    orc.orc_sgs_targets(ptr(ub), ptr(uu), fx // 2, fy // 2, fz // 2, ctypes.c_double(0.505), ptr(Xo), ptr(To))
+    X, T = samples_from_velocity(u, np.ones((fz, fy, fx), bool), 0.505, margin=0)
+    assert X.shape == (n, 16) and (To > 0).mean() > 0.2
+    np.testing.assert_allclose(T, To, rtol=1e-5, atol=1e-9)
+    np.testing.assert_allclose(X, Xo, rtol=1e-4, atol=1e-5)
+
+
+def test_host_samples_stay_clear_of_solids():
+    """cells within the margin of a non-fluid node or a non-periodic edge
+    give no sample"""
+    from lbm_multigpu_gb300.sgs_pipeline import samples_from_velocity
+
+    rng = np.random.default_rng(6)
+    u = (0.02 * rng.standard_normal((3, 8, 24, 24))).astype(np.float32)
+    fluid = np.ones((8, 24, 24), bool)
+    X, _ = samples_from_velocity(u, fluid, 0.505, margin=2)
+    assert len(X) == 4 * 8 * 8           # 12 x 12 coarse cells less 2 on each side in x and y
+    fluid[:, 10:12, 10:12] = False       # one coarse column solid
+    X2, _ = samples_from_velocity(u, fluid, 0.505, margin=2)
+    assert len(X2) == 4 * (64 - 25)      # the 5 x 5 cells around it drop out (all inside the interior)
