@@ -294,13 +294,20 @@ def workload_c3(steps: int, warmup: int) -> dict:
         kf = s.time_stream_collide(20, 1)
         audit = s.audit(0)
     nodes = 256 * 128 * 64 + 96 * 64 * 128 * 2
+    # the same with linear temporal interpolation of the fine band (an extension)
+    with lbm.Solver(text.replace("GPUs per node \t: 1\n", "GPUs per node \t: 1\nCF TIME: \tlinear\n")) as s:
+        s.step(warmup)
+        s.synchronize()
+        ms_t = s.step_timed(steps)
+    cf_time = dict(value=nodes * steps / (ms_t * 1e3), ms_per_coarse_step=ms_t / steps,
+                   note="CF TIME: linear, one more coarse-to-fine interpolation per coarse step")
     return dict(workload="C3 two-level refinement: coarse 256x128x64 + fine 96x64x128 (ratio 2, full z), "
                          "MRT-LES, circular cylinder D=12, tau0=0.52 (RE=90), CS=0.01, 1% inlet noise",
                 metric="MLUPS (coarse + 2 x fine nodes per coarse step)", value=nodes * steps / (ms * 1e3),
                 unit="MLUPS", steps=steps, warmup=warmup, ms_per_coarse_step=ms / steps,
                 kernel_ms=dict(coarse_stream_collide=kc, fine_stream_collide=kf,
                                interface_and_force=ms / steps - kc - 2 * kf),
-                gpu_launches=launches, audit_mass=float(audit[0]))
+                gpu_launches=launches, audit_mass=float(audit[0]), cf_time_linear=cf_time)
 
 
 def workload_c4(steps: int) -> dict:

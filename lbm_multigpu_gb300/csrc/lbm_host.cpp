@@ -104,6 +104,10 @@ struct Config {
      * geometry's own; y faces over z faces over x faces at edges */
     int faces[6] = {-1, -1, -1, -1, -1, -1};
     bool faces_set = false;
+    /* "CF TIME: linear": the fine band gets coarse moments interpolated in
+     * time before every fine sub-step after the first (the reference, "none",
+     * fills it once per coarse step, LR7:2926) */
+    int cf_time = 0;
     /* older records spell the LES line "Smagorinski LES: YES/NO"; DynInlet
      * records add "KP" (the inlet P-control gain, MRTtest/DynInlet3.cu:26) */
     bool les_yesno = false;
@@ -242,6 +246,10 @@ int parse_inputs(const char* text, Config& c) {
         else if (key == "DYN start") I(c.dyn_start);
         else if (key == "TRIP end") I(c.trip_end);
         else if (key == "FACES") { ok = parse_faces(val, c.faces); c.faces_set = true; }
+        else if (key == "CF TIME") {
+            ok = (val == "linear" || val == "none");
+            c.cf_time = val == "linear";
+        }
         else if (key == "LID BC") {
             ok = (val == "cpu3d" || val == "regularized");
             c.lid_quirk = val == "cpu3d";
@@ -342,6 +350,7 @@ std::string value_of(const Config& c, const std::string& key, float omega, float
     else if (key == "DYN every") o << c.dyn_every;
     else if (key == "DYN start") o << c.dyn_start;
     else if (key == "TRIP end") o << c.trip_end;
+    else if (key == "CF TIME") o << (c.cf_time ? "linear" : "none");
     else if (key == "FACES")
         for (int i = 0; i < 6; ++i) o << (i ? " " : "") << (c.faces[i] < 0 ? "-" : NODE_NAMES[c.faces[i]]);
     return o.str();
@@ -407,6 +416,7 @@ std::string write_inputs(const Config& c, float omega, float omegaLR) {
     if (c.dyn_start != d.dyn_start) line("DYN start: ", "DYN start");
     if (c.trip_end != d.trip_end) line("TRIP end: ", "TRIP end");
     if (c.faces_set) line("FACES: ", "FACES");
+    if (c.cf_time) line("CF TIME: ", "CF TIME");
     return o.str();
 }
 
@@ -538,6 +548,8 @@ struct lbm_handle {
     double* force_hist = nullptr;   /* device, 3 doubles per recorded step */
     int force_cap = 0;
     float* mom = nullptr;           /* coarse moment export, [9][nz][eny][enx] */
+    float* mom_prev = nullptr;      /* CF TIME linear: the previous coarse step's export */
+    bool have_mom = false;          /* mom holds an export (CF TIME linear) */
     int enx = 0, eny = 0;
     double* audit_part = nullptr;
     double* audit_out = nullptr;
@@ -735,6 +747,7 @@ int do_init(lbm_handle* h) {
     }
     if (h->dpdy_dev) CUDA_TRY(cudaMemcpyAsync(h->dpdy_dev, &c.dpdy, sizeof(float), cudaMemcpyHostToDevice, h->stream));
     h->dyn_n = 0;
+    h->have_mom = false;
     for (int l = 0; l < h->nlevels; ++l) {
         LevelState& s = h->lv[l];
         for (int i = 0; i < 2; ++i) CUDA_TRY(launch_init(s.L, s.mask, s.f[i], kind, u0, h->stream, axis));
@@ -794,6 +807,14 @@ int one_step(lbm_handle* h) {
     if (c.sgs_mlp && !h->mlp_ready)
         return fail(LBM_ERR_STATE, "SGS mlp: no weights (SGS weights record line or lbm_set_sgs_mlp)");
     if (p.force_on) CUDA_TRY(fork_force(h, C, h->force_hist + 3LL * fidx));
+    /* CF TIME linear: this step's export goes to the other buffer, the last
+     * one is kept for the interpolation in time */
+    bool blend = false;
+    if (c.refinement && c.cf_time) {
+        std::swap(h->mom, h->mom_prev);
+        blend = h->have_mom;
+        h->have_mom = true;
+    }
     if (c.sgs_mlp)
         CUDA_TRY(launch_stream_collide_mlp(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, C.links, h->mlp_blob,
                                            h->mlp_err, h->stream));
@@ -815,6 +836,12 @@ int one_step(lbm_handle* h) {
         LevelState& Fn = h->lv[1];
         const int L = int(std::lround(1.0 / c.lrfactor));
         for (int i = 0; i < L; ++i) {
+            if (blend && i > 0) {
+                /* the band at fine time i / L of the coarse step */
+                CUDA_TRY(launch_interp_cf(h->rp, Fn.L, h->mom, Fn.f[Fn.cur], Fn.mask, h->stream, h->mom_prev,
+                                          float(i) / float(L)));
+                ++h->launches;
+            }
             StepParams pf = base_params(h, 1);
             pf.t = t;
             pf.force_on = (t > c.startf && i == 0) ? 1 : 0;
@@ -1024,6 +1051,11 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
         if ((rc = upload_mask(h, 1))) return bail(rc);
         h->enx = int(c.lrx * c.lrfactor) + 1;
         h->eny = int(c.lry * c.lrfactor) + 1;
+        if (c.cf_time) {
+            if (cudaMalloc(&h->mom_prev, size_t(9) * h->enx * h->eny * c.nz * sizeof(float)) != cudaSuccess)
+                return bail(fail(LBM_ERR_NOMEM, "cannot allocate the second moment export"));
+            cudaMemset(h->mom_prev, 0, size_t(9) * h->enx * h->eny * c.nz * sizeof(float));
+        }
         if (cudaMalloc(&h->mom, size_t(9) * h->enx * h->eny * c.nz * sizeof(float)) != cudaSuccess)
             return bail(fail(LBM_ERR_NOMEM, "cannot allocate the moment export"));
         cudaMemset(h->mom, 0, size_t(9) * h->enx * h->eny * c.nz * sizeof(float));
@@ -1057,6 +1089,7 @@ int lbm_destroy(lbm_handle* h) {
     for (auto& s : h->lv) free_level(s);
     cudaFree(h->force_hist);
     cudaFree(h->mom);
+    cudaFree(h->mom_prev);
     cudaFree(h->audit_part);
     cudaFree(h->audit_out);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -1273,6 +1306,15 @@ int lbm_save_state(lbm_handle* h, const char* path) {
         CUDA_TRY(cudaMemcpy(hh.data(), h->dyn_hist, hh.size() * sizeof(float), cudaMemcpyDeviceToHost));
         o.write(reinterpret_cast<const char*>(hh.data()), std::streamsize(hh.size() * sizeof(float)));
     }
+    /* CF TIME linear: the last coarse export, which the next step blends */
+    if (h->cfg.refinement && h->cfg.cf_time) {
+        put(o, int32_t(h->have_mom ? 1 : 0));
+        if (h->have_mom) {
+            std::vector<float> m(size_t(9) * h->enx * h->eny * h->cfg.nz);
+            CUDA_TRY(cudaMemcpy(m.data(), h->mom, m.size() * sizeof(float), cudaMemcpyDeviceToHost));
+            o.write(reinterpret_cast<const char*>(m.data()), std::streamsize(m.size() * sizeof(float)));
+        }
+    }
     if (!o) return fail(LBM_ERR_ARG, "checkpoint: write to '%s' failed", path);
     return LBM_OK;
 }
@@ -1348,6 +1390,17 @@ int lbm_restore_state(lbm_handle* h, const char* path) {
             const int k = std::min(int(nd), h->dyn_cap);
             if (k > 0) CUDA_TRY(cudaMemcpy(h->dyn_hist, hh.data(), size_t(k) * 3 * 4, cudaMemcpyHostToDevice));
             h->dyn_n = k;
+        }
+    }
+    h->have_mom = false;
+    if (h->cfg.refinement && h->cfg.cf_time) {
+        int32_t hm = 0;
+        if (get(in, hm) && hm) {
+            std::vector<float> m(size_t(9) * h->enx * h->eny * h->cfg.nz);
+            if (!in.read(reinterpret_cast<char*>(m.data()), std::streamsize(m.size() * sizeof(float))))
+                return fail(LBM_ERR_PARSE, "checkpoint: truncated moment export");
+            CUDA_TRY(cudaMemcpy(h->mom, m.data(), m.size() * sizeof(float), cudaMemcpyHostToDevice));
+            h->have_mom = true;
         }
     }
     /* the trip blocks are in the mask only before TRIP end */

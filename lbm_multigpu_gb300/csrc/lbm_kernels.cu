@@ -655,9 +655,12 @@ __device__ __forceinline__ void second_order(const float mc[8][9], const float S
 /* InterpCF (LR7:1991-2170): fine nodes of the LRLEVEL-wide x/y band get the
  * coarse moments interpolated (trilinear + second-order velocity correction)
  * and rebuilt with the LES-aware non-equilibrium rescale (LR7:524-579).  One
- * thread per band node; mom_c is [9][cnz][eny][enx] (coarse footprint). */
+ * thread per band node; mom_c is [9][cnz][eny][enx] (coarse footprint).
+ * With mom_prev (the previous coarse step's export) the corner moments are
+ * first interpolated in time, (1 - theta) prev + theta cur. */
 template <class S>
-__global__ void k_interp_cf(const RefineParams r, const Level F, const float* __restrict__ mom_c, S* __restrict__ f_f,
+__global__ void k_interp_cf(const RefineParams r, const Level F, const float* __restrict__ mom_c,
+                            const float* __restrict__ mom_prev, float theta, S* __restrict__ f_f,
                             const uint8_t* __restrict__ mask_f) {
     const int L = r.lrlevel;
     const int nb_x = r.fny * 2 * L;                /* x-band nodes per plane */
@@ -694,6 +697,10 @@ __global__ void k_interp_cf(const RefineParams r, const Level F, const float* __
         const long long ce = ((long long)zc * r.eny + (ym + ((c >> 1) & 1))) * r.enx + (xm + (c & 1));
 #pragma unroll
         for (int m = 0; m < 9; ++m) mc[c][m] = __ldg(mom_c + m * ne + ce);
+        if (mom_prev) {
+#pragma unroll
+            for (int m = 0; m < 9; ++m) mc[c][m] = (1.f - theta) * __ldg(mom_prev + m * ne + ce) + theta * mc[c][m];
+        }
         strain_rate<float>(mc[c], Sc[c]);
     }
     float mom[9];
@@ -1010,12 +1017,13 @@ cudaError_t launch_audit(const Level& L, const void* f, const uint8_t* mask, dou
 }
 
 cudaError_t launch_interp_cf(const RefineParams& r, const Level& F, const float* mom_c, void* f_f,
-                             const uint8_t* mask_f, cudaStream_t s) {
+                             const uint8_t* mask_f, cudaStream_t s, const float* mom_prev, float theta) {
     const int L = r.lrlevel;
     const long long n = (long long)(r.fny * 2 * L + (r.fnx - 2 * L) * 2 * L) * r.fnz;
     const int threads = 128;
     const unsigned blocks = unsigned((n + threads - 1) / threads);
-    LBM_DISPATCH(F.storage, (k_interp_cf<S><<<blocks, threads, 0, s>>>(r, F, mom_c, (S*)f_f, mask_f)));
+    LBM_DISPATCH(F.storage,
+                 (k_interp_cf<S><<<blocks, threads, 0, s>>>(r, F, mom_c, mom_prev, theta, (S*)f_f, mask_f)));
     return cudaGetLastError();
 }
 

@@ -148,8 +148,11 @@ struct RefineParams {
     int enx, eny;          /* exported coarse-moment footprint */
 };
 
+/* mom_prev: the previous coarse export, blended in time with weight theta
+ * on mom_c (linear temporal interpolation); null: mom_c alone */
 cudaError_t launch_interp_cf(const RefineParams& r, const Level& F, const float* mom_c, void* f_f,
-                             const uint8_t* mask_f, cudaStream_t s);
+                             const uint8_t* mask_f, cudaStream_t s, const float* mom_prev = nullptr,
+                             float theta = 1.f);
 cudaError_t launch_interp_fc(const RefineParams& r, const Level& C, const Level& F, const void* f_f, void* f_c,
                              const uint8_t* mask_c, cudaStream_t s);
 

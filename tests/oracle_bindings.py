@@ -88,7 +88,7 @@ class OracleRun:
 
     def __init__(self, nx, ny, nz, mask, omega, *, model=0, les=0, cs=0.02, dpdy=0.0, u_in=0.05, init_kind=0,
                  init_u=0.05, lid_u=(0, 0, 0), lid_face=5, startf=0, refine=None, noise_amp=0.0, seed=12345,
-                 stats=None, f0=None, pull_clamp=0, lid_quirk=0, halfway=0, mlp=None):
+                 stats=None, f0=None, pull_clamp=0, lid_quirk=0, halfway=0, mlp=None, cf_time=False):
         o = oracle()
         self.p = Params(nx=nx, ny=ny, nz=nz, model=model, les=les, omega=omega, cs=cs, dpdy=dpdy, u_in=u_in,
                         rho_out=1.0, lid_face=lid_face, stats_weight=1.0, noise_amp=noise_amp, noise_seed=seed,
@@ -126,6 +126,9 @@ class OracleRun:
             enx, eny = int(r.fnx * r.lrfactor) + 1, int(r.fny * r.lrfactor) + 1
             self.p.exp_x0, self.p.exp_y0, self.p.exp_nx, self.p.exp_ny = int(r.lrx0), int(r.lry0), enx, eny
             self.mom = np.zeros((9, nz, eny, enx), np.float32)
+            # linear temporal interpolation of the band (CF TIME: linear)
+            self.cf_time, self.have_mom = cf_time, False
+            self.mom_prev = np.zeros_like(self.mom)
 
     def step(self, n=1):
         o = oracle()
@@ -135,12 +138,20 @@ class OracleRun:
             self.p.force_on = 1 if (self.refine is None and t > self.startf) else 0
             f3 = np.zeros(3)
             st = [ptr(self.st[i]) for i in range(4)] if self.st is not None else [None] * 4
+            blend = False
+            if self.refine is not None and self.cf_time:
+                self.mom, self.mom_prev = self.mom_prev, self.mom
+                blend, self.have_mom = self.have_mom, True
             o.orc_step(ctypes.byref(self.p), ptr(self.mask), ptr(self.fa), ptr(self.fb), ptr(f3), *st,
                        ptr(self.mom) if self.refine is not None else None)
             self.fa, self.fb = self.fb, self.fa
             if self.refine is not None:
                 L = self.r.lrlevel
                 for i in range(L):
+                    if blend and i > 0:
+                        th = np.float32(i / L)
+                        mb = np.ascontiguousarray((np.float32(1) - th) * self.mom_prev + th * self.mom, np.float32)
+                        o.orc_interp_cf(ctypes.byref(self.r), ptr(mb), ptr(self.ffa), ptr(self.fmask))
                     self.pf.t = t
                     self.pf.force_on = 1 if (t > self.startf and i == 0) else 0
                     o.orc_step(ctypes.byref(self.pf), ptr(self.fmask), ptr(self.ffa), ptr(self.ffb), ptr(f3),

@@ -114,6 +114,55 @@ def test_refinement_vs_oracle(product, les, re):
     assert rel_l2(jf[:, mf != 2], jo[:, mf != 2]) < RTOL
 
 
+def _lr_time_setup(lbm, steps):
+    return _lr_setup(lbm, 1, 60.0, steps).replace("GPUs per node \t: 1\n", "GPUs per node \t: 1\nCF TIME: \tlinear\n")
+
+
+def test_refinement_temporal_interpolation_vs_oracle(product):
+    """CF TIME: linear (an extension; the reference fills the fine band once
+    per coarse step): before the second fine sub-step the band gets the
+    coarse moments halfway between the previous and the current coarse
+    export.  Against the oracle's loop doing the same; and not the
+    reference schedule's result"""
+    lbm = product
+    steps = 60
+    text = _lr_time_setup(lbm, steps)
+    assert "CF TIME: \tlinear" in lbm.normalize_inputs(text)
+    with lbm.Solver(text) as s:
+        s.step(steps)
+        fc, ff, mc, mf, pr = s.populations(0), s.populations(1), s.mask(0), s.mask(1), s.params()
+    with lbm.Solver(_lr_setup(lbm, 1, 60.0, steps)) as s0:
+        s0.step(steps)
+        ff0 = s0.populations(1)
+    r = Refine(cnx=64, cny=24, cnz=4, fnx=32, fny=32, fnz=8, lrx0=12.25, lry0=4.25, lrz0=-0.75, lrfactor=0.5,
+               lrlevel=2, order=2, cs=0.01, omega_c=pr["omega"], omega_f=pr["omega_lr"], quirk_fc_top_zflip=1)
+    o = OracleRun(64, 24, 4, mc, pr["omega"], les=1, cs=0.01, refine=dict(r=r, mask=mf, omega_f=pr["omega_lr"]),
+                  cf_time=True)
+    o.step(steps)
+    assert _compare(fc, o.fa, mc)[0] < RTOL
+    _, jf = moments(ff)
+    _, jo = moments(o.ffa)
+    assert rel_l2(jf[:, mf != 2], jo[:, mf != 2]) < RTOL
+    _, j0 = moments(ff0)
+    assert rel_l2(jf[:, mf != 2], j0[:, mf != 2]) > 100 * RTOL
+
+
+def test_checkpoint_with_temporal_interpolation_is_bit_exact(product, tmp_path):
+    """the kept coarse export travels in the checkpoint: a restart continues
+    bit for bit"""
+    lbm = product
+    ck = tmp_path / "lr.ckpt"
+    with lbm.Solver(_lr_time_setup(lbm, 60)) as s:
+        s.step(20)
+        s.save_state(ck)
+        s.step(20)
+        f0, f1 = s.populations(0), s.populations(1)
+    with lbm.Solver.from_state(ck) as r:
+        r.step(20)
+        np.testing.assert_array_equal(r.populations(0), f0)
+        np.testing.assert_array_equal(r.populations(1), f1)
+
+
 def test_statistics_vs_oracle(product):
     lbm = product
     steps = 200
