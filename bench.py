@@ -274,40 +274,45 @@ def reference_arm(args, world, rank):
 
 
 def workload_c3(steps: int, warmup: int) -> dict:
-    """two-level refinement: coarse 256x128x64 MRT-LES channel, circular
-    cylinder of diameter 12 coarse cells, ratio-2 patch spanning the periodic
-    z extent (96x64x128 fine, the reference's full-z layout), 2 fine steps per
-    coarse step; MLUPS by the reference's count (LR7:2956-2961): coarse nodes
-    + fine nodes x LRLEVEL per coarse step"""
+    """two-level refinement as the configuration names it: coarse 256x128x64
+    MRT-LES channel, circular cylinder of diameter 12 coarse cells, a ratio-2
+    fine patch of 96x64x64 fine cells (bounded in z: coarse planes 16-48),
+    second-order spatial and linear temporal coarse-to-fine interpolation,
+    2 fine steps per coarse step; MLUPS by the reference's count
+    (LR7:2956-2961): coarse nodes + fine nodes x LRLEVEL per coarse step.
+    Beside it the reference's own layout (patch spanning the periodic z
+    extent, 96x64x128, no time interpolation)."""
     import lbm_multigpu_gb300 as lbm
 
-    text = lbm.make_inputs(256, 128, 64, obst1=(64.5, 63.5, 0.0), r1=6.0, re=90.0, umax=0.05,
-                           tmax=steps + warmup + 10, les=1, cs=0.01, geometry="channel_circle", refinement=1,
-                           lr_dims=(96, 64, 128), lr_factor=0.5, lr_origin=(48.25, 47.25, -0.75), inlet_noise=0.01)
-    with lbm.Solver(text) as s:
-        s.step(warmup)
-        s.synchronize()
-        n0 = s.launch_count()
-        ms = s.step_timed(steps)
-        launches = s.launch_count() - n0
-        kc = s.time_stream_collide(20, 0)
-        kf = s.time_stream_collide(20, 1)
-        audit = s.audit(0)
-    nodes = 256 * 128 * 64 + 96 * 64 * 128 * 2
-    # the same with linear temporal interpolation of the fine band (an extension)
-    with lbm.Solver(text.replace("GPUs per node \t: 1\n", "GPUs per node \t: 1\nCF TIME: \tlinear\n")) as s:
-        s.step(warmup)
-        s.synchronize()
-        ms_t = s.step_timed(steps)
-    cf_time = dict(value=nodes * steps / (ms_t * 1e3), ms_per_coarse_step=ms_t / steps,
-                   note="CF TIME: linear, one more coarse-to-fine interpolation per coarse step")
-    return dict(workload="C3 two-level refinement: coarse 256x128x64 + fine 96x64x128 (ratio 2, full z), "
-                         "MRT-LES, circular cylinder D=12, tau0=0.52 (RE=90), CS=0.01, 1% inlet noise",
-                metric="MLUPS (coarse + 2 x fine nodes per coarse step)", value=nodes * steps / (ms * 1e3),
-                unit="MLUPS", steps=steps, warmup=warmup, ms_per_coarse_step=ms / steps,
-                kernel_ms=dict(coarse_stream_collide=kc, fine_stream_collide=kf,
-                               interface_and_force=ms / steps - kc - 2 * kf),
-                gpu_launches=launches, audit_mass=float(audit[0]), cf_time_linear=cf_time)
+    def run(lr_dims, lr_origin, cf_time):
+        text = lbm.make_inputs(256, 128, 64, obst1=(64.5, 63.5, 0.0), r1=6.0, re=90.0, umax=0.05,
+                               tmax=steps + warmup + 10, les=1, cs=0.01, geometry="channel_circle", refinement=1,
+                               lr_dims=lr_dims, lr_factor=0.5, lr_origin=lr_origin, inlet_noise=0.01,
+                               cf_time=cf_time)
+        with lbm.Solver(text) as s:
+            s.step(warmup)
+            s.synchronize()
+            n0 = s.launch_count()
+            ms = s.step_timed(steps)
+            launches = s.launch_count() - n0
+            kc = s.time_stream_collide(20, 0)
+            kf = s.time_stream_collide(20, 1)
+            audit = s.audit(0)
+        nodes = 256 * 128 * 64 + lr_dims[0] * lr_dims[1] * lr_dims[2] * 2
+        return dict(value=nodes * steps / (ms * 1e3), ms_per_coarse_step=ms / steps,
+                    kernel_ms=dict(coarse_stream_collide=kc, fine_stream_collide=kf,
+                                   interface_and_force=ms / steps - kc - 2 * kf),
+                    gpu_launches=launches, audit_mass=float(audit[0]))
+
+    main = run((96, 64, 64), (48.25, 47.25, 16.25), "linear")
+    ref = run((96, 64, 128), (48.25, 47.25, -0.75), "none")
+    return dict(workload="C3 two-level refinement: coarse 256x128x64 + fine 96x64x64 (ratio 2, bounded in z from "
+                         "coarse z 16.25), linear temporal interpolation, MRT-LES, circular cylinder D=12, tau0=0.52 "
+                         "(RE=90), CS=0.01, 1% inlet noise",
+                metric="MLUPS (coarse + 2 x fine nodes per coarse step)", unit="MLUPS", steps=steps, warmup=warmup,
+                **main,
+                reference_layout=dict(ref, note="fine 96x64x128 spanning the periodic z extent, no time "
+                                                "interpolation (LR7's layout and schedule)"))
 
 
 def workload_c4(steps: int) -> dict:

@@ -981,14 +981,20 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
         const int lev = int(std::lround(1.0 / c.lrfactor));
         if (std::fabs(c.lrfactor - 1.f / lev) > 0.001f || lev < 2)
             return fail(LBM_ERR_CONFIG, "LR factor %g is not 1/LRLEVEL", c.lrfactor);
-        if (c.lrz != lev * c.nz)
-            return fail(LBM_ERR_CONFIG, "the refinement patch must span the periodic z extent: LR nz %d != %d * %d", c.lrz,
-                        lev, c.nz);
-        if (std::fabs((c.lrx0 - std::floor(c.lrx0)) - 0.5f * c.lrfactor) > 1e-6f ||
-            std::fabs((c.lry0 - std::floor(c.lry0)) - 0.5f * c.lrfactor) > 1e-6f ||
-            std::fabs(c.lrz0 + (1.f - 0.5f * c.lrfactor)) > 1e-6f)
-            return fail(LBM_ERR_CONFIG, "LR location must sit at half a fine spacing past a coarse node (z at %g)",
-                        -(1.f - 0.5f * c.lrfactor));
+        /* the reference's patch spans the periodic z extent from
+         * z = -(1 - LRFACTOR/2); a patch bounded in z (an extension) sits in z
+         * as in x and y */
+        const bool full_z = c.lrz == lev * c.nz && std::fabs(c.lrz0 + (1.f - 0.5f * c.lrfactor)) <= 1e-6f;
+        auto half_past = [&](float v) { return std::fabs((v - std::floor(v)) - 0.5f * c.lrfactor) <= 1e-6f; };
+        if (!half_past(c.lrx0) || !half_past(c.lry0) || (!full_z && !half_past(c.lrz0)))
+            return fail(LBM_ERR_CONFIG, "LR location must sit at half a fine spacing past a coarse node (or, spanning "
+                                        "z, at z = %g)", -(1.f - 0.5f * c.lrfactor));
+        if (!full_z) {
+            const int ez = int(c.lrz * c.lrfactor) + 1;
+            if (c.lrz0 < 0.f || int(c.lrz0) + ez > c.nz || c.lrz >= lev * c.nz)
+                return fail(LBM_ERR_CONFIG, "a z-bounded refinement patch must lie inside the base grid's z extent");
+            if (c.lrz < 2 * lev + 2) return fail(LBM_ERR_CONFIG, "refinement patch too small");
+        }
         const int ex = int(c.lrx * c.lrfactor) + 1, ey = int(c.lry * c.lrfactor) + 1;
         if (int(c.lrx0) < 0 || int(c.lry0) < 0 || int(c.lrx0) + ex > c.nx || int(c.lry0) + ey > c.ny)
             return fail(LBM_ERR_CONFIG, "refinement patch does not fit in the base grid");
@@ -1070,6 +1076,8 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
         r.omega_c = h->omega;
         r.omega_f = h->omegaLR;
         r.quirk_fc_top_zflip = c.fc_zflip;
+        r.zbounded = c.lrz != r.lrlevel * c.nz || std::fabs(c.lrz0 + (1.f - 0.5f * c.lrfactor)) > 1e-6f;
+        r.cz0 = r.zbounded ? int(c.lrz0) : 0;
         r.enx = h->enx;
         r.eny = h->eny;
     }

@@ -666,19 +666,30 @@ __global__ void k_interp_cf(const RefineParams r, const Level F, const float* __
     const int nb_x = r.fny * 2 * L;                /* x-band nodes per plane */
     const int nb_y = (r.fnx - 2 * L) * 2 * L;      /* y-band nodes per plane (x-band excluded) */
     const int per_plane = nb_x + nb_y;
+    const int inner = (r.fnx - 2 * L) * (r.fny - 2 * L);  /* z-band nodes per plane (bounded patch) */
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long long)per_plane * r.fnz) return;
-    const int k = int(idx / per_plane);
-    int i = int(idx % per_plane), xf, yf;
-    if (i < nb_x) {
-        yf = i / (2 * L);
-        const int b = i % (2 * L);
-        xf = b < L ? b : r.fnx - 2 * L + b;
+    const long long nxy = (long long)per_plane * r.fnz;
+    if (idx >= nxy + (r.zbounded ? 2LL * L * inner : 0LL)) return;
+    int k, xf, yf;
+    if (idx < nxy) {
+        k = int(idx / per_plane);
+        int i = int(idx % per_plane);
+        if (i < nb_x) {
+            yf = i / (2 * L);
+            const int b = i % (2 * L);
+            xf = b < L ? b : r.fnx - 2 * L + b;
+        } else {
+            i -= nb_x;
+            xf = L + i / (2 * L);
+            const int b = i % (2 * L);
+            yf = b < L ? b : r.fny - 2 * L + b;
+        }
     } else {
-        i -= nb_x;
-        xf = L + i / (2 * L);
-        const int b = i % (2 * L);
-        yf = b < L ? b : r.fny - 2 * L + b;
+        /* the L bottom and L top planes of a bounded patch, x/y band excluded */
+        const int j = int(idx - nxy), b = j / inner, rem = j % inner;
+        k = b < L ? b : r.fnz - 2 * L + b;
+        xf = L + rem % (r.fnx - 2 * L);
+        yf = L + rem / (r.fnx - 2 * L);
     }
     const long long cf = k * F.plane + (long long)yf * F.pitch + xf;
     const int t = mask_f[cf] & TYPE_MASK;
@@ -686,8 +697,18 @@ __global__ void k_interp_cf(const RefineParams r, const Level F, const float* __
     const float xr = xf * r.lrfactor + r.lrfactor * 0.5f, yr = yf * r.lrfactor + r.lrfactor * 0.5f;
     const int xm = int(xr), ym = int(yr);
     const float fx = xr - xm, fy = yr - ym;
-    int zb = k / L - 1;
-    const float fz = (k % L) * r.lrfactor + r.lrfactor * 0.5f;
+    /* z: periodic full-depth patch (fine plane k at coarse z k / L - 1 +
+     * ...), or, bounded, as x and y from the coarse plane cz0 */
+    int zb;
+    float fz;
+    if (r.zbounded) {
+        const float zr = k * r.lrfactor + r.lrfactor * 0.5f;
+        zb = r.cz0 + int(zr);
+        fz = zr - int(zr);
+    } else {
+        zb = k / L - 1;
+        fz = (k % L) * r.lrfactor + r.lrfactor * 0.5f;
+    }
     const long long ne = (long long)r.enx * r.eny * r.cnz;
     float mc[8][9], Sc[8][6];
 #pragma unroll
@@ -740,8 +761,10 @@ __global__ void k_interp_cf(const RefineParams r, const Level F, const float* __
  * margin) are replaced by the restriction of their 8 fine children. */
 template <class S>
 __global__ void k_interp_fc(const RefineParams r, const Level C, const Level F, const S* __restrict__ f_f,
-                            S* __restrict__ f_c, const uint8_t* __restrict__ mask_c, int x0, int y0, int nxi, int nyi) {
-    const int xi = blockIdx.x * blockDim.x + threadIdx.x, yi = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
+                            S* __restrict__ f_c, const uint8_t* __restrict__ mask_c, int x0, int y0, int nxi, int nyi,
+                            int z0) {
+    const int xi = blockIdx.x * blockDim.x + threadIdx.x, yi = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = z0 + int(blockIdx.z);
     if (xi >= nxi || yi >= nyi) return;
     const int x = x0 + xi, y = y0 + yi;
     const long long cc = z * C.plane + (long long)y * C.pitch + x;
@@ -1019,7 +1042,8 @@ cudaError_t launch_audit(const Level& L, const void* f, const uint8_t* mask, dou
 cudaError_t launch_interp_cf(const RefineParams& r, const Level& F, const float* mom_c, void* f_f,
                              const uint8_t* mask_f, cudaStream_t s, const float* mom_prev, float theta) {
     const int L = r.lrlevel;
-    const long long n = (long long)(r.fny * 2 * L + (r.fnx - 2 * L) * 2 * L) * r.fnz;
+    const long long n = (long long)(r.fny * 2 * L + (r.fnx - 2 * L) * 2 * L) * r.fnz +
+                        (r.zbounded ? 2LL * L * (r.fnx - 2 * L) * (r.fny - 2 * L) : 0LL);
     const int threads = 128;
     const unsigned blocks = unsigned((n + threads - 1) / threads);
     LBM_DISPATCH(F.storage,
@@ -1041,11 +1065,21 @@ cudaError_t launch_interp_fc(const RefineParams& r, const Level& C, const Level&
             if (y1 < y0) y0 = y;
             y1 = y;
         }
-    const int nxi = x1 - x0 + 1, nyi = y1 - y0 + 1;
-    if (nxi <= 0 || nyi <= 0) return cudaSuccess;
-    const dim3 block(32, 4), grid((nxi + 31) / 32, (nyi + 3) / 4, C.nz);
+    /* z: every plane of a full-depth patch; a bounded one as x and y */
+    int z0 = 0, z1 = C.nz - 1;
+    if (r.zbounded) {
+        z1 = -1;
+        for (int z = 0; z < C.nz; ++z)
+            if (z > r.lrz0 + 1 && z < r.lrz0 + r.fnz * r.lrfactor - 2) {
+                if (z1 < z0) z0 = z;
+                z1 = z;
+            }
+    }
+    const int nxi = x1 - x0 + 1, nyi = y1 - y0 + 1, nzi = z1 - z0 + 1;
+    if (nxi <= 0 || nyi <= 0 || nzi <= 0) return cudaSuccess;
+    const dim3 block(32, 4), grid((nxi + 31) / 32, (nyi + 3) / 4, nzi);
     LBM_DISPATCH(C.storage, (k_interp_fc<S><<<grid, block, 0, s>>>(r, C, F, (const S*)f_f, (S*)f_c, mask_c, x0, y0,
-                                                                    nxi, nyi)));
+                                                                    nxi, nyi, z0)));
     return cudaGetLastError();
 }
 

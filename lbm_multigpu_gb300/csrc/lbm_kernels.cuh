@@ -146,6 +146,10 @@ struct RefineParams {
     float omega_c, omega_f;
     int quirk_fc_top_zflip;
     int enx, eny;          /* exported coarse-moment footprint */
+    /* a patch bounded in z (an extension; the reference's spans the
+     * periodic z extent): z is treated like x and y, the fine node k at
+     * coarse z lrz0 + k lrfactor with cz0 = int(lrz0) */
+    int zbounded, cz0;
 };
 
 /* mom_prev: the previous coarse export, blended in time with weight theta

@@ -806,7 +806,9 @@ void orc_interp_cf(const orc_refine* r, const float* mom_c, float* f_f, const ui
     for (int k = 0; k < r->fnz; ++k) {
         for (int yf = 0; yf < r->fny; ++yf) {
             for (int xf = 0; xf < r->fnx; ++xf) {
-                if (!(xf < L || xf > r->fnx - L - 1 || yf < L || yf > r->fny - L - 1)) continue;
+                if (!(xf < L || xf > r->fnx - L - 1 || yf < L || yf > r->fny - L - 1 ||
+                      (r->zbounded && (k < L || k > r->fnz - L - 1))))
+                    continue;
                 long cf = (long(k) * r->fny + yf) * r->fnx + xf;
                 if (mask_f[cf] == ORC_WALL || mask_f[cf] == ORC_BODY) continue;
                 /* coarse cell containing the fine node: base corner and offsets
@@ -817,6 +819,12 @@ void orc_interp_cf(const orc_refine* r, const float* mom_c, float* f_f, const ui
                 float fx_ = xr - xm, fy_ = yr - ym;
                 int zb = k / L - 1;
                 float fz_ = (k % L) * r->lrfactor + r->lrfactor * 0.5f;
+                if (r->zbounded) {
+                    /* as x and y, from the coarse plane cz0 */
+                    const float zr = k * r->lrfactor + r->lrfactor * 0.5f;
+                    zb = r->cz0 + int(zr);
+                    fz_ = zr - int(zr);
+                }
                 float mc[8][9], S[8][6];
                 for (int cz = 0; cz < 2; ++cz)
                     for (int cy = 0; cy < 2; ++cy)
@@ -888,6 +896,7 @@ void orc_interp_fc(const orc_refine* r, const float* f_f, float* f_c, const uint
                 if (!(x > r->lrx0 + 1 && x < r->lrx0 + r->fnx * r->lrfactor - 2 && y > r->lry0 + 1 &&
                       y < r->lry0 + r->fny * r->lrfactor - 2))
                     continue;
+                if (r->zbounded && !(z > r->lrz0 + 1 && z < r->lrz0 + r->fnz * r->lrfactor - 2)) continue;
                 long cc = (long(z) * r->cny + y) * r->cnx + x;
                 if (mask_c[cc] == ORC_WALL || mask_c[cc] == ORC_BODY) continue;
                 int xm = int(L * (x - r->lrx0)), ym = int(L * (y - r->lry0));

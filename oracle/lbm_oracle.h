@@ -110,6 +110,9 @@ typedef struct {
     float cs;
     float omega_c, omega_f;
     int quirk_fc_top_zflip;   /* reproduce LR7:2195-2229 corner order on the top plane */
+    /* a patch bounded in z (an extension): z as x and y from coarse plane
+     * cz0 = int(lrz0); 0 for the reference's periodic full-depth patch */
+    int zbounded, cz0;
 } orc_refine;
 
 /* per-cell kernels on arrays of n cells stored cell-major (n x 19) */

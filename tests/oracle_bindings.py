@@ -45,7 +45,8 @@ class Refine(ctypes.Structure):
     _fields_ = [("cnx", ctypes.c_int), ("cny", ctypes.c_int), ("cnz", ctypes.c_int), ("fnx", ctypes.c_int),
                 ("fny", ctypes.c_int), ("fnz", ctypes.c_int), ("lrx0", _F), ("lry0", _F), ("lrz0", _F),
                 ("lrfactor", _F), ("lrlevel", ctypes.c_int), ("order", ctypes.c_int), ("cs", _F),
-                ("omega_c", _F), ("omega_f", _F), ("quirk_fc_top_zflip", ctypes.c_int)]
+                ("omega_c", _F), ("omega_f", _F), ("quirk_fc_top_zflip", ctypes.c_int), ("zbounded", ctypes.c_int),
+                ("cz0", ctypes.c_int)]
 
 
 _oracle = None

@@ -147,6 +147,34 @@ def test_refinement_temporal_interpolation_vs_oracle(product):
     assert rel_l2(jf[:, mf != 2], j0[:, mf != 2]) > 100 * RTOL
 
 
+@pytest.mark.parametrize("cf_time", ["none", "linear"])
+def test_z_bounded_patch_vs_oracle(product, cf_time):
+    """a fine patch bounded in z (an extension; the reference's spans the
+    periodic z extent): 32x32x12 fine from coarse z = 2.25 in a 64x24x12
+    channel, the band also on its bottom and top planes and the restriction
+    with a z margin too; against the oracle, with and without linear temporal
+    interpolation"""
+    lbm = product
+    steps = 50
+    text = lbm.make_inputs(64, 24, 12, obst1=(20.5, 11.5, 0.0), r1=3.0, re=60.0, umax=0.05, tmax=steps, les=1,
+                           cs=0.01, refinement=1, lr_dims=(32, 32, 12), lr_factor=0.5, lr_origin=(12.25, 4.25, 2.25),
+                           geometry="channel_square", cf_time=cf_time)
+    with lbm.Solver(text) as s:
+        s.step(steps)
+        fc, ff, mc, mf, pr = s.populations(0), s.populations(1), s.mask(0), s.mask(1), s.params()
+    assert np.isfinite(ff).all()
+    r = Refine(cnx=64, cny=24, cnz=12, fnx=32, fny=32, fnz=12, lrx0=12.25, lry0=4.25, lrz0=2.25, lrfactor=0.5,
+               lrlevel=2, order=2, cs=0.01, omega_c=pr["omega"], omega_f=pr["omega_lr"], quirk_fc_top_zflip=1,
+               zbounded=1, cz0=2)
+    o = OracleRun(64, 24, 12, mc, pr["omega"], les=1, cs=0.01, refine=dict(r=r, mask=mf, omega_f=pr["omega_lr"]),
+                  cf_time=cf_time == "linear")
+    o.step(steps)
+    assert _compare(fc, o.fa, mc)[0] < RTOL
+    _, jf = moments(ff)
+    _, jo = moments(o.ffa)
+    assert rel_l2(jf[:, mf != 2], jo[:, mf != 2]) < RTOL
+
+
 def test_checkpoint_with_temporal_interpolation_is_bit_exact(product, tmp_path):
     """the kept coarse export travels in the checkpoint: a restart continues
     bit for bit"""
