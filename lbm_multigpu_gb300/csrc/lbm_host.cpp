@@ -560,6 +560,7 @@ struct lbm_handle {
      * stream: forked after the previous step, joined before the next */
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_cf_fork = nullptr, ev_cf_join = nullptr; /* CF TIME linear: the last band fill beside InterpFC */
     long long launches = 0;         /* kernels this handle has launched */
     /* learned subgrid closure: device weight blob and its error flag */
     unsigned char* mlp_blob = nullptr;
@@ -856,8 +857,22 @@ int one_step(lbm_handle* h) {
             if (pf.force_on) CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
             Fn.cur = 1 - Fn.cur;
         }
-        CUDA_TRY(launch_interp_cf(h->rp, Fn.L, h->mom, Fn.f[Fn.cur], Fn.mask, h->stream));
-        CUDA_TRY(launch_interp_fc(h->rp, C.L, Fn.L, Fn.f[Fn.cur], C.f[C.cur], C.mask, h->stream));
+        if (c.cf_time) {
+            /* the band fill and the restriction touch disjoint fine nodes
+             * (band vs children of the interior with its 2-node margin) and
+             * the next coarse step exports into the other buffer: the fill
+             * runs on the second stream beside the restriction, joined
+             * before the step ends */
+            CUDA_TRY(cudaEventRecord(h->ev_cf_fork, h->stream));
+            CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_cf_fork, 0));
+            CUDA_TRY(launch_interp_cf(h->rp, Fn.L, h->mom, Fn.f[Fn.cur], Fn.mask, h->side));
+            CUDA_TRY(cudaEventRecord(h->ev_cf_join, h->side));
+            CUDA_TRY(launch_interp_fc(h->rp, C.L, Fn.L, Fn.f[Fn.cur], C.f[C.cur], C.mask, h->stream));
+            CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_cf_join, 0));
+        } else {
+            CUDA_TRY(launch_interp_cf(h->rp, Fn.L, h->mom, Fn.f[Fn.cur], Fn.mask, h->stream));
+            CUDA_TRY(launch_interp_fc(h->rp, C.L, Fn.L, Fn.f[Fn.cur], C.f[C.cur], C.mask, h->stream));
+        }
         h->launches += 2;
     }
     h->t = t + 1;
@@ -1033,7 +1048,9 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
         cudaDeviceGetStreamPriorityRange(&lo, &hi);
         if (cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, hi) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess)
+            cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_cf_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_cf_join, cudaEventDisableTiming) != cudaSuccess)
             return bail(fail(LBM_ERR_CUDA, "cannot create the force stream"));
     }
     /* reference velocity of the FP16/BF16 offsets: the inlet velocity of a channel */
@@ -1108,6 +1125,8 @@ int lbm_destroy(lbm_handle* h) {
     cudaFree(h->dyn_hist);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->ev_cf_fork) cudaEventDestroy(h->ev_cf_fork);
+    if (h->ev_cf_join) cudaEventDestroy(h->ev_cf_join);
     if (h->side) cudaStreamDestroy(h->side);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
