@@ -8,6 +8,8 @@ kernels, csrc/lbm_sgs.cpp host side), and the ensemble of periodic boxes
 (csrc/ensemble.cu, csrc/lbm_ensemble.cpp), and the post-processing of the
 outputs (csrc/lbm_post.cpp).  Host code is built with -ffp-contract=off so geometry
 masks and the text writers give identical results on x86 and aarch64 hosts.
+Beside the library: the command lbm_run (csrc/lbm_run.cpp), the reference
+programs' main() over the C ABI.
 """
 from __future__ import annotations
 
@@ -22,6 +24,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 INCLUDE = PKG.parent / "include"
 LIB = BUILD / "liblbm_gb300.so"
+RUN = BUILD / "lbm_run"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", f"-I{INCLUDE}"]
@@ -43,9 +46,25 @@ def _stale(out: Path, deps: list[Path]) -> bool:
     return not out.exists() or out.stat().st_mtime < max(d.stat().st_mtime for d in deps)
 
 
+def build_run(force: bool = False) -> Path:
+    """the lbm_run command, linked against the library next to it"""
+    src = CSRC / "lbm_run.cpp"
+    if not force and not _stale(RUN, [src, LIB, *sorted(INCLUDE.glob("*.h"))]):
+        return RUN
+    tmp = RUN.with_name(f"lbm_run.{os.getpid()}.tmp")
+    r = subprocess.run([nvcc(), "-O2", "-std=c++17", f"-I{INCLUDE}", "-x", "c++", str(src), "-o", str(tmp),
+                        f"-L{BUILD}", "-llbm_gb300", "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"lbm_run build failed:\n{r.stdout}{r.stderr}")
+    os.replace(tmp, RUN)
+    return RUN
+
+
 def build(force: bool = False, verbose: bool = False) -> Path:
     deps = sources() + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
     if not force and not _stale(LIB, deps):
+        build_run()
         return LIB
     BUILD.mkdir(parents=True, exist_ok=True)
     cc = nvcc()
@@ -69,6 +88,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}{r.stderr}")
     os.replace(tmp, LIB)
+    build_run(force=True)
     return LIB
 
 

@@ -686,3 +686,29 @@ def test_fp16_bf16_one_step_vs_oracle(product, prec, rel, halfway):
     n = fl.sum()
     assert ((np.abs(g0 - o.fa) > bound) & fl).sum() > 0.05 * n
     assert ((np.abs(np.roll(o.fa, 1, axis=-1) - o.fa) > bound) & fl).sum() > 0.3 * n
+
+
+def test_lbm_run_command_writes_the_reference_outputs(product, tmp_path):
+    """lbm_run, the reference programs' main() as a command: a run record in,
+    the reference's timing line out, and the same output files as the
+    handle writes after the same steps"""
+    import subprocess
+
+    from lbm_multigpu_gb300 import build
+
+    lbm = product
+    text = _chan_inputs(lbm, 30)
+    (tmp_path / "case.inputs").write_text(text)
+    exe = build.build_run()
+    r = subprocess.run([str(exe), "case.inputs"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.startswith("Time taken for main kernel: ") and r.stdout.rstrip().endswith("MLUPS)")
+    ref = tmp_path / "api"
+    ref.mkdir()
+    with lbm.Solver(text) as s:
+        s.step(30)
+        s.write_outputs(str(ref / "case"))
+    for name in ("case.inputs", "case_part0.dat", "case_slice.dat", "case.force"):
+        assert (tmp_path / name).read_bytes() == (ref / name).read_bytes(), name
+    bad = subprocess.run([str(exe), "missing.inputs"], cwd=tmp_path, capture_output=True, text=True, timeout=60)
+    assert bad.returncode == 1 and "cannot read" in bad.stderr
