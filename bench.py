@@ -150,6 +150,24 @@ def time_precision(precision: str, steps: int, warmup: int, world: int, dist, wi
     return ms, kernel_ms, clocks, audit, launches
 
 
+def worst_over_ranks(ms: float, dist) -> float:
+    """the slowest rank's time: the job's time for replicas run in lockstep"""
+    if not dist:
+        return ms
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_mlups(world: int, cells: int, steps: int, ms: float) -> float:
+    """whole-job MLUPS of `world` replicas that each updated `cells` nodes
+    `steps` times in `ms` (the slowest rank's time)"""
+    return world * cells * steps / (ms * 1e-3) / 1e6
+
+
 def time_e2e(steps: int, world: int, dist) -> dict:
     """the same workload through the public API with host buffers in the
     timed region: pinned initial populations in, each step's force out
@@ -467,11 +485,7 @@ def main():
         full = (msf, kmsf)
 
     def worst(ms):
-        if not dist:
-            return ms
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return worst_over_ranks(ms, dist)
 
     ms32 = worst(ms32)
     for prec in res:
@@ -484,7 +498,7 @@ def main():
             dist.destroy_process_group()
         return
     pk = peaks()
-    mlups = world * CELLS * args.steps / (ms32 * 1e-3) / 1e6
+    mlups = replica_mlups(world, CELLS, args.steps, ms32)
     kernel_gbs = CELLS * BYTES_PER_CELL[main_prec] / (kms32 * 1e-3) / 1e9
     traffic = None
     prof = ROOT / "profiles" / "traffic.json"
