@@ -13,7 +13,20 @@ import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
 GOLDEN = ROOT / "tests" / "golden"
-REFERENCE = Path("/root/reference")
+
+
+def _reference_root() -> Path:
+    """the reference's sources as the oracle's recipe finds them (present only
+    where the reference is checked out)"""
+    import sys
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import ref_recipe
+
+    return ref_recipe.REF_ROOT
+
+
+REFERENCE = _reference_root()
 
 
 def header_symbols():
