@@ -62,6 +62,10 @@ LR7_CONFIGS = {
                    OBSTY1="11.5f", RE="20.f", UMAX="0.05f", SmagLES=0, CS="0.01f", REFINEMENT=1,
                    LRFACTOR="0.5f", LRLEVEL=2, LRX0="12.25f", XLRDIM=32, LRY0="4.25f", YLRDIM=32,
                    LRZ0="-0.75f", ZLRDIM=8, ORDER=2, BLOCKSIZELRX=32, VELAV=0, START_VELAV=100000, START_VELFLUC=250000),
+    # the MRT + Smagorinsky channel over 1000 steps (the 1e-5 gate after 1000 steps)
+    "chan_les_1k": dict(XDIM=64, YDIM=24, ZDIM=6, TMAX=1000, STARTF=0, OBSTR1="4.f", OBSTX1="20.5f",
+                        OBSTY1="11.5f", RE="60.f", UMAX="0.05f", SmagLES=1, CS="0.01f", REFINEMENT=0,
+                        VELAV=0, START_VELAV=100000, START_VELFLUC=250000),
     # tiny channel for the output-writer fixtures (statistics switch on at t = 5 and 12)
     "tiny": dict(XDIM=64, YDIM=8, ZDIM=4, TMAX=20, STARTF=0, OBSTR1="2.f", OBSTX1="20.5f", OBSTY1="3.5f",
                  RE="40.f", UMAX="0.05f", SmagLES=1, CS="0.01f", REFINEMENT=0, VELAV=1, START_VELAV=5,
@@ -75,9 +79,10 @@ CPU3D_PROGRAMS = {
     "c2_long": dict(XDIM=512, YDIM=128, ZDIM=128, TMAX=24),
     # its own lid-driven cavity, small, with the final output.dat kept (parity)
     "cav24": dict(XDIM=24, YDIM=24, ZDIM=24, TMAX=100),
+    "cav24_1k": dict(XDIM=24, YDIM=24, ZDIM=24, TMAX=1000),
 }
 # programs whose output.dat is kept
-CPU3D_KEEP_OUTPUT = {"cav24"}
+CPU3D_KEEP_OUTPUT = {"cav24", "cav24_1k"}
 
 
 # the reference's post-processing programs, staged with small constants

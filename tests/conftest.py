@@ -18,6 +18,9 @@ for p in (ROOT, ROOT / "tests", ROOT / "oracle"):
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    # the tests' temporary files stay inside the working tree (git-ignored)
+    if not config.option.basetemp:
+        config.option.basetemp = str(ROOT / ".pytest_tmp")
 
 
 @pytest.fixture(scope="session")
@@ -58,6 +61,11 @@ def cellops(tmp_path_factory):
 def golden():
     import numpy as np
 
+    import json
+
     g = ROOT / "tests" / "golden"
-    return dict(cells=np.load(g / "cells.npz"), runs=np.load(g / "runs.npz"),
-                meta=__import__("json").loads((g / "runs.json").read_text()), dir=g)
+    runs, meta = {}, {}
+    for stem in ("runs", "runs_1k"):  # the 1000-step channel is its own file
+        runs.update(dict(np.load(g / f"{stem}.npz")))
+        meta.update(json.loads((g / f"{stem}.json").read_text()))
+    return dict(cells=np.load(g / "cells.npz"), runs=runs, meta=meta, dir=g)

@@ -116,10 +116,10 @@ def write_inputs_text(L):
     return buf.value.decode()
 
 
-def runs():
+def runs(cases=(("chan_les", 200), ("chan_mrt", 200), ("lr", 100)), stem="runs"):
     meta = {}
     arrays = {}
-    for name, steps in (("chan_les", 200), ("chan_mrt", 200), ("lr", 100)):
+    for name, steps in cases:
         cfg = ref_recipe.LR7_CONFIGS[name]
         L = lib(f"lr7_{name}.so")
         L.ref_setup(None, None)
@@ -146,8 +146,8 @@ def runs():
             imgf = np.zeros((fz, fy, fx), np.int32)
             L.ref_image_lr(ptr(imgf))
             arrays[f"{name}_fine_image"] = imgf.astype(np.int16)
-    np.savez_compressed(HERE / "runs.npz", **arrays)
-    (HERE / "runs.json").write_text(json.dumps(meta, indent=1))
+    np.savez_compressed(HERE / f"{stem}.npz", **arrays)
+    (HERE / f"{stem}.json").write_text(json.dumps(meta, indent=1))
 
 
 def writer():
@@ -177,24 +177,24 @@ def writer():
     (HERE / "writer_tiny.inputs").write_text(write_inputs_text(L))
 
 
-def cpu3d_cavity():
+def cpu3d_cavity(name="cav24", steps=100, out="cpu3d_cavity24.npz"):
     """the reference CPU program's own lid-driven cavity (24^3, MRT with its
-    quirks, 100 steps): u, v, rho of its output.dat"""
+    quirks, `steps` steps): u, v, rho of its output.dat"""
     import os
     import subprocess
     import tempfile
 
-    exe = ref_recipe.REF_DIR / "cpu3d_cav24"
-    with tempfile.TemporaryDirectory() as d:
-        r = subprocess.run([str(exe)], cwd=d, capture_output=True, text=True, timeout=120)
+    exe = ref_recipe.REF_DIR / f"cpu3d_{name}"
+    with tempfile.TemporaryDirectory(dir=ref_recipe.REF_DIR) as d:
+        r = subprocess.run([str(exe)], cwd=d, capture_output=True, text=True, timeout=600)
         assert r.returncode == 0, r.stderr
         lines = open(os.path.join(d, "output.dat")).read().splitlines()[2:]
     n = 24
-    out = np.zeros((3, n, n, n), np.float32)
+    uvrho = np.zeros((3, n, n, n), np.float32)
     for line in lines:
         x, y, z, u, v, w, rho = (float(t) for t in line.split(","))
-        out[:, int(z), int(y), int(x)] = (u, v, rho)
-    np.savez_compressed(HERE / "cpu3d_cavity24.npz", uvrho=out, steps=100)
+        uvrho[:, int(z), int(y), int(x)] = (u, v, rho)
+    np.savez_compressed(HERE / out, uvrho=uvrho, steps=steps)
 
 
 def alt_bc():
@@ -244,7 +244,9 @@ def alt_bc():
 
 
 PARTS = dict(cells=lambda: cells(), runs=lambda: runs(), writer=lambda: writer(),
-             cpu3d_cavity=lambda: cpu3d_cavity(), alt_bc=lambda: alt_bc())
+             cpu3d_cavity=lambda: cpu3d_cavity(), alt_bc=lambda: alt_bc(),
+             runs_1k=lambda: runs((("chan_les_1k", 1000),), "runs_1k"),
+             cpu3d_cavity_1k=lambda: cpu3d_cavity("cav24_1k", 1000, "cpu3d_cavity24_1k.npz"))
 
 if __name__ == "__main__":
     if not ref_recipe.staged():

@@ -149,9 +149,10 @@ def _oracle_run(golden, name):
     return o, mask
 
 
-@pytest.mark.parametrize("name", ["chan_les", "chan_mrt", "lr"])
+@pytest.mark.parametrize("name", ["chan_les", "chan_mrt", "lr", "chan_les_1k"])
 def test_oracle_whole_run_vs_reference_kernels(golden, name):
-    """the oracle's restated time loop against the reference's own kernels"""
+    """the oracle's restated time loop against the reference's own kernels
+    (chan_les_1k: the MRT-LES channel over 1000 steps)"""
     o, mask = _oracle_run(golden, name)
     want = golden["runs"][f"{name}_fields"]
     fluid = (mask != 1) & (mask != 2)
@@ -186,11 +187,13 @@ def _cpu3d_cavity_inputs(product, n=24):
                                edge_pull="clamp", lid_bc="cpu3d")
 
 
-def test_oracle_vs_reference_cpu_program(golden, product):
+@pytest.mark.parametrize("fixture", ["cpu3d_cavity24.npz", "cpu3d_cavity24_1k.npz"])
+def test_oracle_vs_reference_cpu_program(golden, product, fixture):
     """the oracle in CPU_3D's semantics (clamped edge pulls, its regularised
     lid as written, its MRT, every node initialised at UMAX) against the
-    output.dat of the reference CPU program itself (24^3 cavity, 100 steps)"""
-    d = np.load(golden["dir"] / "cpu3d_cavity24.npz")
+    output.dat of the reference CPU program itself (24^3 cavity, 100 and
+    1000 steps)"""
+    d = np.load(golden["dir"] / fixture)
     want, steps = d["uvrho"], int(d["steps"])
     n = 24
     mask = product.inputs_mask(_cpu3d_cavity_inputs(product)).reshape(n, n, n)

@@ -58,9 +58,10 @@ def test_channel_vs_oracle(product, model, les, re, dpdy):
     assert rel_l2(F[:, 0], np.array(o.forces)[: len(F), 0]) < FTOL
 
 
-@pytest.mark.parametrize("name", ["chan_les", "chan_mrt"])
+@pytest.mark.parametrize("name", ["chan_les", "chan_mrt", "chan_les_1k"])
 def test_channel_vs_reference_kernels(product, golden, name):
-    """the CUDA path against the fields the reference's own kernels produced"""
+    """the CUDA path against the fields the reference's own kernels produced
+    (chan_les_1k: the MRT-LES channel after 1000 steps, the 1e-5 gate)"""
     lbm = product
     meta = golden["meta"][name]
     want = golden["runs"][f"{name}_fields"]
@@ -257,10 +258,12 @@ def test_halfway_bounceback_vs_oracle(product, model, les):
     assert abs(F_full[-1, 0] - F[-1, 0]) > 1e-3 * abs(F[-1, 0])   # a different wall position, a different drag
 
 
-def test_reference_cpu_program_cavity(product, golden):
-    """CPU_3D semantics on the GPU against the reference CPU program's output"""
+@pytest.mark.parametrize("fixture", ["cpu3d_cavity24.npz", "cpu3d_cavity24_1k.npz"])
+def test_reference_cpu_program_cavity(product, golden, fixture):
+    """CPU_3D semantics on the GPU against the reference CPU program's output
+    (100 and 1000 steps)"""
     lbm = product
-    d = np.load(golden["dir"] / "cpu3d_cavity24.npz")
+    d = np.load(golden["dir"] / fixture)
     n = 24
     text = lbm.make_inputs(n, n, n, r1=5.0, re=50.0, umax=0.04, model="MRT_CPU3D", geometry="cavity", lid_face="-x",
                            lid_velocity=(0.0, 0.04, 0.0), init=2, init_velocity=0.04, edge_pull="clamp",
