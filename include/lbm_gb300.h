@@ -97,6 +97,10 @@ int lbm_get_time(const lbm_handle* h, int* t);
 /* node mask of a level, uint8[nz][ny][nx] of lbm_node values */
 int lbm_get_mask(const lbm_handle* h, int level, uint8_t* mask);
 int lbm_set_mask(lbm_handle* h, int level, const uint8_t* mask);
+/* the base level's geometry (ImageFcn, LR7:88-127): mask as lbm_set_mask on
+ * level 0, or NULL for the record's analytic geometry on every level (at
+ * the handle's time, for the dynamic inlet's timed trip blocks) */
+int lbm_set_geometry(lbm_handle* h, const uint8_t* mask);
 
 /* equilibrium at rho = 1 and the configured initial velocity */
 int lbm_init_equilibrium(lbm_handle* h);
@@ -159,6 +163,9 @@ int lbm_write_inputs(const lbm_handle* h, char* buf, size_t cap, size_t* len);
  * CASENAME.force, CASENAME.inputs (WriteResults, WriteResultsLR,
  * WriteForces, WriteInputs) */
 int lbm_write_outputs(lbm_handle* h, const char* casename);
+/* the tecplot files alone: CASENAME_part<n>.dat and CASENAME_slice.dat
+ * (WriteResults, WriteResultsLR, LR7:2350-2535) */
+int lbm_write_tecplot(lbm_handle* h, const char* casename);
 
 /* ---- kernel-level API on caller-owned device buffers ---- */
 

@@ -78,6 +78,8 @@ SIGNATURES = [
                                     _P, _P, _P]),
     ("lbm_wall_profile", _I, [_P, _P, _P, _P, _I, _F, _F, _P, _P, _P, _P, _P]),
     ("lbm_stats_profiles", _I, [_P, _I, _I, _I, _I, _P]),
+    ("lbm_set_geometry", _I, [_P, _P]),
+    ("lbm_write_tecplot", _I, [_P, ctypes.c_char_p]),
     ("lbm_centerline_profiles", _I, [_P, _I, _I, _I, ctypes.c_double, _P, _P, _P, _P]),
     ("lbm_ensemble_create", _I, [_I, _P, _P, _I, _F, _P]),
     ("lbm_ensemble_destroy", _I, [_P]),
@@ -445,6 +447,17 @@ class Solver:
 
     def write_outputs(self, casename: str) -> None:
         _check(self._lib.lbm_write_outputs(self._h, casename.encode()))
+
+    def write_tecplot(self, casename: str) -> None:
+        """CASENAME_part<n>.dat and CASENAME_slice.dat only"""
+        _check(self._lib.lbm_write_tecplot(self._h, casename.encode()))
+
+    def set_geometry(self, mask: np.ndarray | None = None) -> None:
+        """the base level's mask, or None for the record's analytic geometry"""
+        if mask is None:
+            _check(self._lib.lbm_set_geometry(self._h, None))
+        else:
+            self.set_mask(mask, 0)
 
 
 SGS = {"none": 0, "smagorinsky": 1, "mlp": 2}

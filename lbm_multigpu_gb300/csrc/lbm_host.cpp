@@ -1179,6 +1179,20 @@ int lbm_set_mask(lbm_handle* h, int level, const uint8_t* mask) {
     return upload_mask(h, level);
 }
 
+int lbm_set_geometry(lbm_handle* h, const uint8_t* mask) {
+    if (!h) return fail(LBM_ERR_ARG, "null handle");
+    if (mask) return lbm_set_mask(h, 0, mask);
+    /* the record's analytic geometry (ImageFcn / ImageFcnLR) at the handle's time */
+    mask_base(h->cfg, h->lv[0].hmask, h->t);
+    if (int rc = upload_mask(h, 0)) return rc;
+    h->trip_in_mask = h->cfg.geometry == "dyninlet" && h->t < h->cfg.trip_end;
+    if (h->nlevels > 1) {
+        mask_fine(h->cfg, h->lv[1].hmask);
+        if (int rc = upload_mask(h, 1)) return rc;
+    }
+    return LBM_OK;
+}
+
 int lbm_init_equilibrium(lbm_handle* h) {
     if (!h) return fail(LBM_ERR_ARG, "null handle");
     return do_init(h);
@@ -1662,13 +1676,12 @@ static void write_level(std::ostream& out, std::ostream* slice, const Config& c,
             }
 }
 
-int lbm_write_outputs(lbm_handle* h, const char* casename) {
-    if (!h || !casename) return fail(LBM_ERR_ARG, "null argument");
+/* WriteResults / WriteResultsLR: <base>_part<level>.dat and the slices of
+ * every level appended to <base>_slice.dat */
+static int write_tecplot_files(lbm_handle* h, const std::string& base) {
     const Config& c = h->cfg;
-    std::string base(casename);
-    std::ofstream dat(base + ".dat"), force(base + ".force"), inputs(base + ".inputs"), slice(base + "_slice.dat");
-    if (!dat || !force || !inputs || !slice) return fail(LBM_ERR_ARG, "cannot open output files for '%s'", casename);
-    inputs << write_inputs(c, h->omega, h->omegaLR);
+    std::ofstream slice(base + "_slice.dat");
+    if (!slice) return fail(LBM_ERR_ARG, "cannot open '%s_slice.dat'", base.c_str());
     for (int l = 0; l < h->nlevels; ++l) {
         LevelState& s = h->lv[l];
         const size_t N = size_t(s.L.nx) * s.L.ny * s.L.nz;
@@ -1680,9 +1693,26 @@ int lbm_write_outputs(lbm_handle* h, const char* casename) {
         }
         /* WriteResults / WriteResultsLR append their slice to one file */
         std::ofstream part(base + "_part" + std::to_string(l) + ".dat");
+        if (!part) return fail(LBM_ERR_ARG, "cannot open '%s_part%d.dat'", base.c_str(), l);
         write_level(part, &slice, c, l, f, st, s.L.nx, s.L.ny, s.L.nz);
         part << std::endl;
     }
+    return LBM_OK;
+}
+
+int lbm_write_tecplot(lbm_handle* h, const char* casename) {
+    if (!h || !casename) return fail(LBM_ERR_ARG, "null argument");
+    return write_tecplot_files(h, casename);
+}
+
+int lbm_write_outputs(lbm_handle* h, const char* casename) {
+    if (!h || !casename) return fail(LBM_ERR_ARG, "null argument");
+    const Config& c = h->cfg;
+    std::string base(casename);
+    std::ofstream dat(base + ".dat"), force(base + ".force"), inputs(base + ".inputs");
+    if (!dat || !force || !inputs) return fail(LBM_ERR_ARG, "cannot open output files for '%s'", casename);
+    inputs << write_inputs(c, h->omega, h->omegaLR);
+    if (int rc = write_tecplot_files(h, base)) return rc;
     const int nf = std::max(0, c.tmax - c.startf);
     std::vector<double> F(size_t(std::max(nf, 1)) * 3, 0.0);
     int got = 0;

@@ -715,3 +715,24 @@ def test_lbm_run_command_writes_the_reference_outputs(product, tmp_path):
         assert (tmp_path / name).read_bytes() == (ref / name).read_bytes(), name
     bad = subprocess.run([str(exe), "missing.inputs"], cwd=tmp_path, capture_output=True, text=True, timeout=60)
     assert bad.returncode == 1 and "cannot read" in bad.stderr
+
+
+def test_set_geometry_and_write_tecplot(product, tmp_path):
+    """lbm_set_geometry: a caller's mask on the base level, NULL back to the
+    record's analytic geometry; lbm_write_tecplot: the same tecplot files as
+    lbm_write_outputs writes"""
+    lbm = product
+    with lbm.Solver(_chan_inputs(lbm, 10)) as s:
+        m0 = s.mask()
+        m1 = m0.copy()
+        m1[:, 5:8, 40:44] = lbm.NODE["BODY"]
+        s.set_geometry(m1)
+        assert np.array_equal(s.mask(), m1)
+        s.set_geometry(None)
+        assert np.array_equal(s.mask(), m0)
+        s.step(3)
+        s.write_tecplot(str(tmp_path / "t"))
+        s.write_outputs(str(tmp_path / "o"))
+    for suffix in ("_part0.dat", "_slice.dat"):
+        assert (tmp_path / f"t{suffix}").read_bytes() == (tmp_path / f"o{suffix}").read_bytes()
+    assert not (tmp_path / "t.force").exists()
