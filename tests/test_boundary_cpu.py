@@ -150,3 +150,19 @@ def test_checkpoint_rejects_other_files(product, tmp_path):
     assert lib.lbm_create_from_state(str(bad).encode(), ctypes.byref(h)) == 3
     assert b"not a checkpoint" in lib.lbm_last_error()
     assert lib.lbm_create_from_state(str(tmp_path / "missing").encode(), ctypes.byref(h)) == 1
+
+
+def test_lbm_run_command_arguments(product, tmp_path):
+    """lbm_run (the reference programs' main() as a command) reports usage
+    and unreadable records before any device work"""
+    import subprocess
+
+    from lbm_multigpu_gb300 import build
+
+    exe = build.build_run()
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "usage: lbm_run" in r.stderr
+    r = subprocess.run([str(exe), "case.inputs", "--bogus"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2
+    r = subprocess.run([str(exe), str(tmp_path / "missing.inputs")], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "cannot read" in r.stderr
