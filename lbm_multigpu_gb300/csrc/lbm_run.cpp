@@ -12,6 +12,7 @@
  * and CASENAME.force as the reference does (LR7:2963-3027).  CASENAME
  * defaults to the record's file name without its extension.
  */
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -89,7 +90,8 @@ int main(int argc, char** argv) {
         int nx = 0, ny = 0, nz = 0;
         lbm_get_dims(h, l, &nx, &ny, &nz);
         /* the fine patch updates LRLEVEL times per step (LR7:2959) */
-        const double factor = l == 0 ? 1.0 : std::lround(1.0 / std::atof(record_value(text, "LR factor").c_str()));
+        const double lrf = std::atof(record_value(text, "LR factor").c_str());
+        const double factor = l == 0 || lrf <= 0 ? 1.0 : double(std::lround(1.0 / lrf));
         nodes += double(nx) * ny * nz * factor;
     }
     /* the loop in chunks, timed on the device */
