@@ -208,14 +208,16 @@ int lbm_body_force_f32_noalloc(const float* fA, const uint8_t* mask, int nx, int
 /* ------------------------------------------------------------------------
  * Learned subgrid closure.  No counterpart in the reference (its LES is the
  * constant-Cs Smagorinsky model, LR7:683-685): a per-node MLP
- * 16 -> 64 -> 64 -> 1 (GELU, softplus output) gives the eddy viscosity from
+ * 16 -> 64 -> 64 -> 1 (ReLU, softplus output) gives the eddy viscosity from
  * the node's non-equilibrium stress.  Parameters are a float vector of
  * lbm_mlp_param_count() entries: W1[64][16] (column 15 = bias), W2[64][64],
- * b2[64], w3[64], b3.  Samples are X[n][16] features and T[n] target eddy
- * viscosities (lattice units).
+ * b2[64], w3[64], b3.  Hidden unit 63 of the first layer is the constant 1
+ * (row 63 of W1 takes no part).  Samples are X[n][16] features (x15 = 1) and
+ * T[n] target eddy viscosities (lattice units).
  * ------------------------------------------------------------------------ */
 int lbm_mlp_param_count(void);
-/* Glorot-uniform weights, zero biases, from a seed (host memory) */
+/* He-uniform hidden weights, Glorot-uniform output weights, zero biases,
+ * from a seed (host memory) */
 int lbm_mlp_init_params(uint32_t seed, float* params);
 /* gradient of the mean squared error of nu_t / 1e-4 over n samples, and the
  * loss; device pointers, synchronous on stream */
@@ -228,8 +230,9 @@ int lbm_mlp_predict(const float* d_params, const float* d_X, int n, float* d_nu,
 int lbm_mlp_train(const float* d_X, const float* d_T, int n, int batch, int steps, float lr, uint32_t seed,
                   float* params, float* loss_hist, void* stream);
 /* nu_t of n samples through the tensor-core path the collide kernels use:
- * BF16 weights and activations, FP32 accumulation (tcgen05.mma), GELU by
- * tanh.approx; params in host memory, samples and output on the device;
+ * BF16 weights and activations, FP32 accumulation (tcgen05.mma, all three
+ * layers), b2 folded into W2 against the constant unit; params in host
+ * memory, samples and output on the device;
  * synchronous on stream */
 int lbm_mlp_predict_tc(const float* params, const float* d_X, int n, float* d_nu, void* stream);
 /* tensor-core self-check: D[128][64] = A[128][16 kc] * B[64][16 kc]^T with

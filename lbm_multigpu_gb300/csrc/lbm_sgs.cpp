@@ -68,15 +68,20 @@ void mlp_make_blob(const float* P, unsigned char* blob) {
         const uint16_t b = bf16_rne(v);
         std::memcpy(base + off, &b, 2);
     };
+    /* W1 with row HC = e15: the MMA makes the constant unit relu(x15) = 1 */
     for (int j = 0; j < sgs::NH; ++j)
         for (int k = 0; k < sgs::NIN; ++k)
-            put(blob, tc::core_off(j, k, sgs::W1_LBO, sgs::W1_SBO), P[sgs::OFF_W1 + j * sgs::NIN + k]);
+            put(blob, tc::core_off(j, k, sgs::W1_LBO, sgs::W1_SBO),
+                j == sgs::HC ? float(k == sgs::NIN - 1) : P[sgs::OFF_W1 + j * sgs::NIN + k]);
+    /* W2 with b2 folded into column HC */
     for (int j = 0; j < sgs::NH; ++j)
         for (int k = 0; k < sgs::NH; ++k)
-            put(blob + sgs::W1_BYTES, tc::core_off(j, k, sgs::W2_LBO, sgs::W2_SBO), P[sgs::OFF_W2 + j * sgs::NH + k]);
-    std::memcpy(blob + sgs::BLOB_B2, &P[sgs::OFF_B2], sgs::NH * 4);
-    std::memcpy(blob + sgs::BLOB_B2 + sgs::NH * 4, &P[sgs::OFF_B3], 4);
-    std::memcpy(blob + sgs::BLOB_B2 + sgs::NH * 4 + 16, &P[sgs::OFF_W3], sgs::NH * 4);
+            put(blob + sgs::BLOB_W2, tc::core_off(j, k, sgs::W2_LBO, sgs::W2_SBO),
+                P[sgs::OFF_W2 + j * sgs::NH + k] + (k == sgs::HC ? P[sgs::OFF_B2 + j] : 0.f));
+    /* the output layer as the B operand of an N = 16 MMA: row 0 = w3 */
+    for (int k = 0; k < sgs::NH; ++k)
+        put(blob + sgs::BLOB_W3, tc::core_off(0, k, sgs::W2_LBO, sgs::W2_SBO), P[sgs::OFF_W3 + k]);
+    std::memcpy(blob + sgs::BLOB_B3, &P[sgs::OFF_B3], 4);
 }
 }  // namespace lbm
 
@@ -87,16 +92,18 @@ int lbm_mlp_param_count(void) { return sgs::NPARAM; }
 int lbm_mlp_init_params(uint32_t seed, float* params) {
     if (!params) return set_error(LBM_ERR_ARG, "params is null", cudaSuccess);
     Rng r(seed);
-    auto glorot = [&](int off, int fan_out, int fan_in, int ncols) {
-        const double a = std::sqrt(6.0 / (fan_in + fan_out));
-        for (int j = 0; j < fan_out; ++j)
+    /* uniform(-a, a): He (a = sqrt(6 / fan_in)) for the ReLU layers,
+     * Glorot for the output */
+    auto uniform = [&](int off, int rows, int ncols, double a) {
+        for (int j = 0; j < rows; ++j)
             for (int k = 0; k < ncols; ++k) params[off + j * ncols + k] = float((2 * r.uniform() - 1) * a);
     };
-    glorot(sgs::OFF_W1, sgs::NH, sgs::NIN - 1, sgs::NIN);
+    uniform(sgs::OFF_W1, sgs::NH, sgs::NIN, std::sqrt(6.0 / (sgs::NIN - 1)));
     for (int j = 0; j < sgs::NH; ++j) params[sgs::OFF_W1 + j * sgs::NIN + sgs::NIN - 1] = 0.f; /* b1 */
-    glorot(sgs::OFF_W2, sgs::NH, sgs::NH, sgs::NH);
+    for (int k = 0; k < sgs::NIN; ++k) params[sgs::OFF_W1 + sgs::HC * sgs::NIN + k] = k == sgs::NIN - 1; /* unused */
+    uniform(sgs::OFF_W2, sgs::NH, sgs::NH, std::sqrt(6.0 / sgs::NH));
     for (int j = 0; j < sgs::NH; ++j) params[sgs::OFF_B2 + j] = 0.f;
-    glorot(sgs::OFF_W3, 1, sgs::NH, sgs::NH);
+    uniform(sgs::OFF_W3, 1, sgs::NH, std::sqrt(6.0 / (sgs::NH + 1)));
     params[sgs::OFF_B3] = 0.f;
     return LBM_OK;
 }

@@ -24,11 +24,10 @@ namespace sgs {
 constexpr int GT = 128;        /* samples (threads) per block */
 constexpr int RS = NH + 1;     /* padded row stride of the per-sample arrays */
 
-__device__ __forceinline__ float gelu(float z, float& dg) {
-    const float u = GELU_A * (z + GELU_B * z * z * z);
-    const float t = tanhf(u);
-    dg = 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * GELU_A * (1.f + 3.f * GELU_B * z * z);
-    return 0.5f * z * (1.f + t);
+/* ReLU and its slope (0 at z = 0) */
+__device__ __forceinline__ float relu(float z, float& dg) {
+    dg = z > 0.f ? 1.f : 0.f;
+    return z > 0.f ? z : 0.f;
 }
 __device__ __forceinline__ float softplus(float y) { return y > 20.f ? y : log1pf(expf(y)); }
 __device__ __forceinline__ float sigmoid(float y) { return 1.f / (1.f + expf(-y)); }
@@ -83,9 +82,11 @@ __global__ void __launch_bounds__(GT) k_mlp_grad(const float* __restrict__ param
 #pragma unroll
             for (int k = 0; k < NIN; ++k) z = fmaf(s.W1[j * NIN + k], x[k], z);
             float dg;
-            h1[j] = gelu(z, dg);
-            z1[j] = dg; /* keep GELU'(z1) */
+            h1[j] = relu(z, dg);
+            z1[j] = dg; /* keep relu'(z1) */
         }
+        h1[HC] = 1.f; /* the constant unit */
+        z1[HC] = 0.f;
         /* layer 2 + output */
         float* z2 = s.Z2 + t * RS;
         float* h2 = s.H2 + t * RS;
@@ -94,7 +95,7 @@ __global__ void __launch_bounds__(GT) k_mlp_grad(const float* __restrict__ param
             float z = s.b2[j];
             for (int k = 0; k < NH; ++k) z = fmaf(s.W2[j * NH + k], h1[k], z);
             float dg;
-            h2[j] = gelu(z, dg);
+            h2[j] = relu(z, dg);
             z2[j] = dg;
             y = fmaf(s.w3[j], h2[j], y);
         }
@@ -105,9 +106,9 @@ __global__ void __launch_bounds__(GT) k_mlp_grad(const float* __restrict__ param
         const float dy = 2.f * err * inv_n * sigmoid(y);
         s.DY[t] = dy;
         gd3 += dy;
-        /* dz2 = dy w3 * GELU'(z2), in place */
+        /* dz2 = dy w3 * relu'(z2), in place */
         for (int j = 0; j < NH; ++j) z2[j] = dy * s.w3[j] * z2[j];
-        /* dz1 = (W2^T dz2) * GELU'(z1), in place */
+        /* dz1 = (W2^T dz2) * relu'(z1), in place */
         for (int k = 0; k < NH; ++k) {
             float a = 0.f;
             for (int j = 0; j < NH; ++j) a = fmaf(s.W2[j * NH + k], z2[j], a);
@@ -196,15 +197,14 @@ __global__ void __launch_bounds__(GT) k_mlp_predict(const float* __restrict__ pa
             float z = 0.f;
 #pragma unroll
             for (int k = 0; k < NIN; ++k) z = fmaf(W1[j * NIN + k], x[k], z);
-            float dg;
-            h1[j] = gelu(z, dg);
+            h1[j] = fmaxf(z, 0.f);
         }
+        h1[HC] = 1.f;
         float y = b3;
         for (int j = 0; j < NH; ++j) {
             float z = b2[j];
             for (int k = 0; k < NH; ++k) z = fmaf(W2[j * NH + k], h1[k], z);
-            float dg;
-            y = fmaf(w3[j], gelu(z, dg), y);
+            y = fmaf(w3[j], fmaxf(z, 0.f), y);
         }
         nu[i] = NU_SCALE * softplus(y);
     }

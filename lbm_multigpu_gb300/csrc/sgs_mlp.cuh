@@ -1,6 +1,11 @@
-/* The learned subgrid closure: a per-cell MLP 15 -> 64 -> 64 -> 1 (GELU,
+/* The learned subgrid closure: a per-cell MLP 16 -> 64 -> 64 -> 1 (ReLU,
  * softplus output) giving the eddy viscosity nu_t that replaces the
  * constant-Cs Smagorinsky model in the collision.
+ *
+ * Hidden unit HC = 63 of the first layer is the constant 1 (whatever row 63
+ * of W1 holds; that row takes no part).  It carries the second layer's bias
+ * on the tensor cores: the weight blob stores W2[j][HC] + b2[j] in column HC
+ * and W1 row HC = e15, so that the MMA itself makes h1[HC] = relu(x15) = 1.
  *
  * Inputs, all local to a node (what the collide kernel has in registers):
  * with the non-equilibrium stress Pi_neq of the pulled populations,
@@ -15,7 +20,7 @@
  * Output: nu_t = NU_SCALE * softplus(y), and tau_eff = tau0 + 3 nu_t.
  *
  * Parameter vector (FP32 master copy, PyTorch Linear order [out][in]):
- *   W1[64][16] (column 15 = b1) | W2[64][64] | b2[64] | w3[64] | b3
+ *   W1[64][16] (column 15 = b1, row HC unused) | W2[64][64] | b2[64] | w3[64] | b3
  */
 #pragma once
 #include <cstdint>
@@ -23,11 +28,10 @@
 namespace lbm {
 namespace sgs {
 
-constexpr int NIN = 16, NH = 64;
+constexpr int NIN = 16, NH = 64, HC = NH - 1;
 constexpr int OFF_W1 = 0, OFF_W2 = OFF_W1 + NH * NIN, OFF_B2 = OFF_W2 + NH * NH, OFF_W3 = OFF_B2 + NH,
               OFF_B3 = OFF_W3 + NH, NPARAM = OFF_B3 + 1;
 constexpr float P_REF = 0.01f, S_REF = 0.01f, NU_SCALE = 1e-4f;
-constexpr float GELU_A = 0.7978845608f, GELU_B = 0.044715f;
 
 /* features of one node from p_ij (xx, yy, zz, xy, xz, yz), tau0 and
  * inv_t0 = 1 / tau0 (a kernel computes it once) */

@@ -5,7 +5,8 @@
  * The closure is not part of the reference (its LES is the constant-Cs
  * Smagorinsky model of LRTurbTest/LRMultiGPU7.cu:683-685); this file restates
  * the definitions the GPU code implements:
- *   MLP 16 -> 64 -> 64 -> 1, GELU (tanh form), softplus output,
+ *   MLP 16 -> 64 -> 64 -> 1, ReLU, softplus output, hidden unit 63 of
+ *   the first layer the constant 1 (row 63 of W1 takes no part),
  *   nu_t = 1e-4 * softplus(y); loss = mean over samples of
  *   (softplus(y) - nu_target / 1e-4)^2;
  *   features of p_ij = -3/2 Pi_neq_ij / rho and tau0 (x0..x15, x15 = 1);
@@ -19,17 +20,13 @@
 #include <vector>
 
 namespace {
-constexpr int NIN = 16, NH = 64;
+constexpr int NIN = 16, NH = 64, HC = NH - 1;
 constexpr int OFF_W1 = 0, OFF_W2 = OFF_W1 + NH * NIN, OFF_B2 = OFF_W2 + NH * NH, OFF_W3 = OFF_B2 + NH,
               OFF_B3 = OFF_W3 + NH, NPARAM = OFF_B3 + 1;
 constexpr double P_REF = 0.01, S_REF = 0.01, NU_SCALE = 1e-4;
-constexpr double GA = 0.7978845608028654, GB = 0.044715;
-
-double gelu(double z, double* dg) {
-    const double u = GA * (z + GB * z * z * z);
-    const double t = std::tanh(u);
-    if (dg) *dg = 0.5 * (1 + t) + 0.5 * z * (1 - t * t) * GA * (1 + 3 * GB * z * z);
-    return 0.5 * z * (1 + t);
+double relu(double z, double* dg) {
+    if (dg) *dg = z > 0 ? 1 : 0;
+    return z > 0 ? z : 0;
 }
 double softplus(double y) { return y > 30 ? y : std::log1p(std::exp(y)); }
 double sigmoid(double y) { return 1 / (1 + std::exp(-y)); }
@@ -43,14 +40,15 @@ void forward(const float* P, const float* x, Fwd& a) {
         double z = 0;
         for (int k = 0; k < NIN; ++k) z += double(P[OFF_W1 + j * NIN + k]) * x[k];
         a.z1[j] = z;
-        a.h1[j] = gelu(z, &a.g1[j]);
+        a.h1[j] = relu(z, &a.g1[j]);
     }
+    a.h1[HC] = 1, a.g1[HC] = 0;
     a.y = P[OFF_B3];
     for (int j = 0; j < NH; ++j) {
         double z = P[OFF_B2 + j];
         for (int k = 0; k < NH; ++k) z += double(P[OFF_W2 + j * NH + k]) * a.h1[k];
         a.z2[j] = z;
-        a.h2[j] = gelu(z, &a.g2[j]);
+        a.h2[j] = relu(z, &a.g2[j]);
         a.y += double(P[OFF_W3 + j]) * a.h2[j];
     }
 }

@@ -117,8 +117,8 @@ def test_training_reduces_loss(product):
 
 def test_tensor_core_inference_matches_oracle(product):
     """the inference path of the collide kernels: BF16 weights and
-    activations through tcgen05.mma, FP32 accumulation, GELU by tanh.approx;
-    against the FP64 oracle forward.  Tolerance: 2% relative L2 over the
+    activations through tcgen05.mma for all three layers, FP32 accumulation,
+    ReLU with the bf16 pack; against the FP64 oracle forward.  Tolerance: 2% relative L2 over the
     samples (BF16 keeps 8 mantissa bits)"""
     torch = pytest.importorskip("torch")
     lib = product.library()
