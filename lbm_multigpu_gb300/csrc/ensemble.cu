@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(32 * TY) k_ens_step(const Table T, const float
             const float s = -1.5f / rho;
 #pragma unroll
             for (int k = 0; k < 6; ++k) p6[k] *= s;
-            sgs::features<float>(p6, M.tau0, xf);
+            sgs::features_fast(p6, M.tau0, M.omega, xf); /* omega = 1 / tau0 */
             const float nu = sgs::infer_nu<ROWS>(smem, xf, err);
             omega = 1.f / (M.tau0 + 3.f * nu);
         }

@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, 6) k_stream_collide_mlp(const L
         const float sc = -1.5f / rho;
 #pragma unroll
         for (int k = 0; k < 6; ++k) p6[k] *= sc;
-        sgs::features<float>(p6, tau0, inv_t0, xf);
+        sgs::features_fast(p6, tau0, inv_t0, xf);
         const float nu = sgs::infer_nu<ROWS>(sm, xf, err);
         if (!live) continue;
         if (type == WALL || type == BODY) {

@@ -15,9 +15,9 @@
  * Thread t of the block owns row t: MMA h = t / 128 covers rows 128 h ..
  * 128 h + 127 in TMEM lanes 0..127 of columns 64 h .. 64 h + 63, and warp w
  * reads lanes 32 (w % 4) .. + 31, which are exactly its threads' rows.
- * One elected thread issues the MMAs; completion arrives on an mbarrier whose
- * wait is bounded (on a timeout the block reports an error code and returns
- * nu_t = 0 so that the caller's state stays finite).
+ * One elected thread issues the MMAs; completion arrives on an mbarrier that
+ * every warp polls with a bounded wait (on a timeout the warp reports an
+ * error code and returns nu_t = 0 so that the caller's state stays finite).
  */
 #pragma once
 #include <cuda_bf16.h>
@@ -129,15 +129,15 @@ __device__ __forceinline__ uint32_t relu_bf16x2(uint32_t z0, uint32_t z1) {
     return d;
 }
 
-/* every thread of the block must call it (uniformly); returns false when
- * the wait for the completion of the given parity ran out */
+/* every warp polls the mbarrier for the completion of the given parity
+ * (no block barrier: a warp goes on to its TMEM reads as soon as it sees the
+ * MMA done); returns false when the wait ran out.  The verdict is
+ * warp-uniform, as the warp-collective tcgen05.ld after it needs.  No
+ * parity is reused before every warp has passed its wait: the next MMA is
+ * issued only behind the block barrier of infer_publish */
 template <int ROWS> __device__ __forceinline__ bool infer_mma_wait(InferSmem<ROWS>& s, uint32_t parity) {
-    /* one warp polls the mbarrier; the others wait at the block barrier
-     * without taking issue slots.  The verdict is block-uniform (tcgen05.ld
-     * below is warp-collective) */
-    bool w = true;
-    if (row_index() < 32) w = tc::mbar_wait(&s.mbar, parity, 1u << 20);
-    const bool ok = __syncthreads_and(w);
+    const bool w = tc::mbar_wait(&s.mbar, parity, 1u << 20);
+    const bool ok = __all_sync(0xffffffffu, w);
     tc::fence_after_sync();
     return ok;
 }
@@ -228,9 +228,9 @@ template <int ROWS> __device__ __forceinline__ float infer_nu(InferSmem<ROWS>& s
     tc::tmem_wait_ld();
     tc::tmem_fence_regs<1>(&r0);
     const float y = __uint_as_float(r0) + s.b3;
-    if (t == 0) s.phase = ph ^ 1u; /* read by every thread before the last wait */
+    if (t == 0) s.phase = ph ^ 1u; /* every thread read it before the second infer_publish */
     if (!ok) {
-        if (t == 0) atomicExch(err, 2);
+        if ((t & 31) == 0) atomicExch(err, 2);
         return 0.f;
     }
     const float sp = y > 20.f ? y : log1pf(__expf(y));

@@ -51,6 +51,26 @@ template <class T> __host__ __device__ inline void features(const T p[6], T tau0
     x[15] = T(1);
 }
 
+#if defined(__CUDACC__)
+/* the same features in FP32 with one rsqrt for |p| and the invariant (the
+ * inference rounds them to bf16, far above the rsqrt's 2 ulp) */
+__device__ __forceinline__ void features_fast(const float p[6], float tau0, float inv_t0, float x[NIN]) {
+    const float pp = p[0] * p[0] + p[1] * p[1] + p[2] * p[2] + 2.f * (p[3] * p[3] + p[4] * p[4] + p[5] * p[5]);
+    const float xx = p[0], yy = p[1], zz = p[2], xy = p[3], xz = p[4], yz = p[5];
+    const float tr3 = xx * xx * xx + yy * yy * yy + zz * zz * zz + 3.f * xx * (xy * xy + xz * xz) +
+                      3.f * yy * (xy * xy + yz * yz) + 3.f * zz * (xz * xz + yz * yz) + 6.f * xy * xz * yz;
+    for (int i = 0; i < 6; ++i) {
+        x[i] = p[i] * (1.f / P_REF);
+        x[6 + i] = p[i] * inv_t0 * (1.f / S_REF);
+    }
+    const float r = pp > 1e-30f ? rsqrtf(pp) : 0.f;
+    x[12] = pp * r * (1.41421356f / P_REF);
+    x[13] = tr3 * (r * r * r);
+    x[14] = (tau0 - 0.5f) * 100.f;
+    x[15] = 1.f;
+}
+#endif
+
 template <class T> __host__ __device__ inline void features(const T p[6], T tau0, T x[NIN]) {
     features<T>(p, tau0, T(1) / tau0, x);
 }
