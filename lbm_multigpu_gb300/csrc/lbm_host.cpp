@@ -561,6 +561,10 @@ struct lbm_handle {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t ev_cf_fork = nullptr, ev_cf_join = nullptr; /* CF TIME linear: the last band fill beside InterpFC */
+    /* refinement steps are launch-bound (a dozen small launches and events
+     * each): lbm_step captures batches of them into one CUDA graph, updated
+     * in place from batch to batch */
+    cudaGraphExec_t gexec = nullptr;
     long long launches = 0;         /* kernels this handle has launched */
     /* learned subgrid closure: device weight blob and its error flag */
     unsigned char* mlp_blob = nullptr;
@@ -879,6 +883,55 @@ int one_step(lbm_handle* h) {
     return LBM_OK;
 }
 
+constexpr int GRAPH_STEPS = 16; /* steps per captured graph */
+
+/* k steps from h->t on can be captured: a refinement run (the uniform step
+ * is two launches of ~0.2 ms, not launch-bound) whose steps call nothing that
+ * synchronises (the trip leaving the mask does) */
+bool graph_ok(const lbm_handle* h, int k) {
+    const Config& c = h->cfg;
+    if (!c.refinement || c.sgs_mlp) return false;
+    if (h->trip_in_mask && h->t + k - 1 >= c.trip_end) return false;
+    return true;
+}
+
+/* k steps captured from the main stream into one graph (the force and
+ * band-fill stream forks from it and joins it again inside every step), then
+ * launched.  The executable graph of the previous batch is updated in place
+ * when the topology is the same (an update leaves launches already queued as
+ * they were), else instantiated anew. */
+int run_graph(lbm_handle* h, int k) {
+    const Config& c = h->cfg;
+    /* what could allocate or synchronise happens before the capture */
+    const int last_fidx = h->t + k - 1 - c.startf;
+    if (last_fidx >= 0)
+        if (int rc = ensure_force_cap(h, last_fidx + 1)) return rc;
+    CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = LBM_OK;
+    for (int j = 0; j < k && rc == LBM_OK; ++j) rc = one_step(h);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+    if (rc != LBM_OK || ec != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc != LBM_OK ? rc : fail(LBM_ERR_CUDA, "step capture: %s", cudaGetErrorString(ec));
+    }
+    cudaError_t e = cudaSuccess;
+    if (h->gexec) {
+        cudaGraphExecUpdateResultInfo info{};
+        if (cudaGraphExecUpdate(h->gexec, g, &info) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(h->gexec);
+            h->gexec = nullptr;
+        }
+    }
+    if (!h->gexec) e = cudaGraphInstantiate(&h->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e == cudaSuccess) e = cudaGraphLaunch(h->gexec, h->stream);
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "step graph: %s", cudaGetErrorString(e));
+    return LBM_OK;
+}
+
 int check_level(const lbm_handle* h, int level) {
     if (!h) return fail(LBM_ERR_ARG, "null handle");
     if (level < 0 || level >= h->nlevels) return fail(LBM_ERR_ARG, "level %d does not exist", level);
@@ -1127,6 +1180,7 @@ int lbm_destroy(lbm_handle* h) {
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->ev_cf_fork) cudaEventDestroy(h->ev_cf_fork);
     if (h->ev_cf_join) cudaEventDestroy(h->ev_cf_join);
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
     if (h->side) cudaStreamDestroy(h->side);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -1248,8 +1302,18 @@ int lbm_set_populations(lbm_handle* h, int level, const float* f) {
 int lbm_step(lbm_handle* h, int nsteps) {
     if (!h) return fail(LBM_ERR_ARG, "null handle");
     if (nsteps < 0) return fail(LBM_ERR_ARG, "nsteps %d < 0", nsteps);
-    for (int i = 0; i < nsteps; ++i)
-        if (int rc = one_step(h)) return rc;
+    for (int i = 0; i < nsteps;) {
+        const int k = std::min(GRAPH_STEPS, nsteps - i);
+        int rc;
+        if (k >= 2 && graph_ok(h, k)) {
+            rc = run_graph(h, k);
+            i += k;
+        } else {
+            rc = one_step(h);
+            ++i;
+        }
+        if (rc) return rc;
+    }
     return LBM_OK;
 }
 
