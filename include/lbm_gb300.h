@@ -109,8 +109,9 @@ int lbm_set_populations(lbm_handle* h, int level, const float* f);
 
 /* Advance n base-grid steps; with refinement every base step runs LRLEVEL
  * patch sub-steps and the two interpolations (the loop of LR7:2849-2950).
- * Refinement steps are captured in batches of 16 into a CUDA graph and
- * replayed; the results equal those of single steps bit for bit. */
+ * Steps are captured in batches of 16 into a CUDA graph and replayed
+ * (except with the learned closure); the results equal those of single
+ * steps bit for bit. */
 int lbm_step(lbm_handle* h, int nsteps);
 /* Same, timed on the handle's stream with CUDA events; *ms = elapsed time */
 int lbm_step_timed(lbm_handle* h, int nsteps, float* ms);

@@ -562,8 +562,9 @@ struct lbm_handle {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t ev_cf_fork = nullptr, ev_cf_join = nullptr; /* CF TIME linear: the last band fill beside InterpFC */
     /* refinement steps are launch-bound (a dozen small launches and events
-     * each): lbm_step captures batches of them into one CUDA graph, updated
-     * in place from batch to batch */
+     * each): lbm_step captures batches of steps into one CUDA graph, updated
+     * in place from batch to batch (uniform runs too: it removes the gaps
+     * between their launches) */
     cudaGraphExec_t gexec = nullptr;
     long long launches = 0;         /* kernels this handle has launched */
     /* learned subgrid closure: device weight blob and its error flag */
@@ -885,12 +886,12 @@ int one_step(lbm_handle* h) {
 
 constexpr int GRAPH_STEPS = 16; /* steps per captured graph */
 
-/* k steps from h->t on can be captured: a refinement run (the uniform step
- * is two launches of ~0.2 ms, not launch-bound) whose steps call nothing that
- * synchronises (the trip leaving the mask does) */
+/* k steps from h->t on can be captured: their steps call nothing that
+ * synchronises (the trip leaving the mask does) or sets kernel attributes
+ * on first use (the learned-closure launcher does) */
 bool graph_ok(const lbm_handle* h, int k) {
     const Config& c = h->cfg;
-    if (!c.refinement || c.sgs_mlp) return false;
+    if (c.sgs_mlp) return false;
     if (h->trip_in_mask && h->t + k - 1 >= c.trip_end) return false;
     return true;
 }

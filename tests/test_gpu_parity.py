@@ -204,6 +204,28 @@ def test_refinement_step_graphs_are_bit_exact(product, cf_time):
         np.testing.assert_array_equal(x, y)
 
 
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+def test_uniform_step_graphs_are_bit_exact(product, precision):
+    """the same for a uniform channel: 40 steps in one call (graphs of 16,
+    16 and 8 steps, the drag/lift reduction forked to the side stream and
+    joined inside each step) against 40 single steps: populations,
+    statistics and the per-step force history bit for bit"""
+    lbm = product
+    steps = 40
+    text = _chan_inputs(lbm, steps, velav=1, start_velav=10, start_velfluc=25, inlet_noise=0.01, seed=3,
+                        precision=precision, bounceback="halfway")
+    with lbm.Solver(text) as a:
+        a.step(steps)
+        ra = [a.populations(), a.stats(), a.forces(steps)]
+    with lbm.Solver(text) as b:
+        for _ in range(steps):
+            b.step(1)
+        rb = [b.populations(), b.stats(), b.forces(steps)]
+    assert np.abs(ra[2]).max() > 0
+    for x, y in zip(ra, rb):
+        np.testing.assert_array_equal(x, y)
+
+
 def test_checkpoint_with_temporal_interpolation_is_bit_exact(product, tmp_path):
     """the kept coarse export travels in the checkpoint: a restart continues
     bit for bit"""
