@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
  * full-way bounce-back, inlet/outlet rebuild with inlet noise, running
  * statistics; no lid, no clamped edges, no refinement export), with the
  * eddy viscosity of every node from the MLP evaluated on the tensor cores
- * for the whole 32 x 8 tile at once.  Persistent blocks walk the tiles so
+ * for the whole 32 x 4 tile at once.  Persistent blocks walk the tiles so
  * that each block stages the weights and allocates its TMEM once per launch.
  * MRT collision (LR7:583-711) at tau_eff = tau0 + 3 nu_t; FP32 arithmetic. */
 constexpr int MLP_BY = 4; /* tile 32 x 4: one M = 128 MMA per layer */
@@ -879,12 +879,12 @@ template <class S, bool HW> static cudaError_t sc_mlp_t(const Level& L, const St
         attr = cudaFuncSetAttribute(k_stream_collide_mlp<S, HW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     int(smem));
         /* all of the unified L1 / shared array as shared memory, so that the
-         * register limit (2 blocks of 256 threads at 128 registers) decides */
+         * register limit (6 blocks of 128 threads at 80 registers) decides */
         if (attr == cudaSuccess)
             attr = cudaFuncSetAttribute(k_stream_collide_mlp<S, HW>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                         100);
         /* resident blocks per SM from the kernel's own limits: registers,
-         * shared memory, threads, and TMEM (128 columns of 512 per block) */
+         * shared memory, threads, and TMEM (64 columns of 512 per block) */
         cudaFuncAttributes fa{};
         int dev = 0, sms = 0, regs_sm = 0, smem_sm = 0;
         if (attr == cudaSuccess) attr = cudaFuncGetAttributes(&fa, k_stream_collide_mlp<S, HW>);

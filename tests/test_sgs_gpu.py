@@ -139,7 +139,7 @@ def test_tensor_core_inference_matches_oracle(product):
 @pytest.mark.parametrize("bounceback", ["halfway", "fullway"])
 def test_channel_with_learned_closure_vs_oracle(product, bounceback):
     """the channel stream-collide with the learned closure in place of
-    Smagorinsky (tensor-core MLP per 32 x 8 tile, persistent blocks) against
+    Smagorinsky (tensor-core MLP per 32 x 4 tile, persistent blocks) against
     the oracle's step with the same closure in FP64; the BF16 inference error
     stays under 5% of the closure's own effect (its distance to Smagorinsky)"""
     from oracle_bindings import OracleRun, moments, rel_l2
