@@ -929,6 +929,10 @@ int run_graph(lbm_handle* h, int k) {
     if (!h->gexec) e = cudaGraphInstantiate(&h->gexec, g, 0);
     cudaGraphDestroy(g);
     if (e == cudaSuccess) e = cudaGraphLaunch(h->gexec, h->stream);
+    /* the graph's side-stream nodes replay on the main stream: later work
+     * queued on the side stream (lbm_get_last_force_async) waits for it */
+    if (e == cudaSuccess) e = cudaEventRecord(h->ev_fork, h->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->side, h->ev_fork, 0);
     if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "step graph: %s", cudaGetErrorString(e));
     return LBM_OK;
 }

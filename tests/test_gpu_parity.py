@@ -226,6 +226,24 @@ def test_uniform_step_graphs_are_bit_exact(product, precision):
         np.testing.assert_array_equal(x, y)
 
 
+def test_async_force_read_after_graph_steps(product):
+    """lbm_get_last_force_async after a graph-replayed lbm_step(n): the copy
+    on the force stream waits for the replayed steps, so it reads the same
+    value as the synchronous read on the main stream, step after step"""
+    torch = pytest.importorskip("torch")
+
+    lbm = product
+    with lbm.Solver(_chan_inputs(lbm, 400)) as s:
+        out = torch.zeros(3, dtype=torch.float64, pin_memory=True).numpy()
+        for _ in range(8):
+            s.step(48)
+            s.last_force_async(out)
+            s.synchronize()
+            want = s.last_force()
+            assert np.abs(want).max() > 0
+            np.testing.assert_array_equal(out, want)
+
+
 def test_checkpoint_with_temporal_interpolation_is_bit_exact(product, tmp_path):
     """the kept coarse export travels in the checkpoint: a restart continues
     bit for bit"""
