@@ -907,6 +907,17 @@ int run_graph(lbm_handle* h, int k) {
     const int last_fidx = h->t + k - 1 - c.startf;
     if (last_fidx >= 0)
         if (int rc = ensure_force_cap(h, last_fidx + 1)) return rc;
+    /* the host-side step state the captured steps advance, put back when
+     * the batch does not reach the GPU (its steps never ran) */
+    const int t0 = h->t, cur0 = h->lv[0].cur, cur1 = h->lv[1].cur, dyn_n0 = h->dyn_n;
+    float* const mom0 = h->mom;
+    float* const mom_prev0 = h->mom_prev;
+    const bool have_mom0 = h->have_mom;
+    const long long launches0 = h->launches;
+    auto restore = [&] {
+        h->t = t0, h->lv[0].cur = cur0, h->lv[1].cur = cur1, h->dyn_n = dyn_n0;
+        h->mom = mom0, h->mom_prev = mom_prev0, h->have_mom = have_mom0, h->launches = launches0;
+    };
     CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     int rc = LBM_OK;
     for (int j = 0; j < k && rc == LBM_OK; ++j) rc = one_step(h);
@@ -915,6 +926,7 @@ int run_graph(lbm_handle* h, int k) {
     if (rc != LBM_OK || ec != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
         cudaGetLastError();
+        restore();
         return rc != LBM_OK ? rc : fail(LBM_ERR_CUDA, "step capture: %s", cudaGetErrorString(ec));
     }
     cudaError_t e = cudaSuccess;
@@ -929,9 +941,13 @@ int run_graph(lbm_handle* h, int k) {
     if (!h->gexec) e = cudaGraphInstantiate(&h->gexec, g, 0);
     cudaGraphDestroy(g);
     if (e == cudaSuccess) e = cudaGraphLaunch(h->gexec, h->stream);
+    if (e != cudaSuccess) {
+        restore();
+        return fail(LBM_ERR_CUDA, "step graph: %s", cudaGetErrorString(e));
+    }
     /* the graph's side-stream nodes replay on the main stream: later work
      * queued on the side stream (lbm_get_last_force_async) waits for it */
-    if (e == cudaSuccess) e = cudaEventRecord(h->ev_fork, h->stream);
+    e = cudaEventRecord(h->ev_fork, h->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(h->side, h->ev_fork, 0);
     if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "step graph: %s", cudaGetErrorString(e));
     return LBM_OK;
