@@ -58,6 +58,44 @@ def test_oracle_gradient_matches_finite_differences():
     assert L0 > 0
 
 
+def _forward_np(P, X):
+    """the network restated in numpy: W1 (column 15 the bias against x15 =
+    1), ReLU, hidden unit 63 the constant 1 whatever row 63 of W1 holds, W2
+    + b2, ReLU, w3 + b3, softplus, times 1e-4"""
+    W1 = P[: NH * NIN].reshape(NH, NIN).astype(np.float64)
+    o = NH * NIN
+    W2 = P[o: o + NH * NH].reshape(NH, NH).astype(np.float64)
+    o += NH * NH
+    b2, w3, b3 = P[o: o + NH].astype(np.float64), P[o + NH: o + 2 * NH].astype(np.float64), float(P[-1])
+    h1 = np.maximum(X.astype(np.float64) @ W1.T, 0)
+    h1[:, NH - 1] = 1
+    h2 = np.maximum(h1 @ W2.T + b2, 0)
+    y = h2 @ w3 + b3
+    return 1e-4 * np.logaddexp(0, y)
+
+
+def test_oracle_forward_matches_numpy():
+    """the oracle's MLP against the numpy restatement above, on parameters
+    whose row 63 of W1 is not e15 (the constant unit ignores it) and on
+    samples that drive units to both sides of the ReLU kink"""
+    o = oracle()
+    P = _params(seed=11, scale=0.4)
+    X, _ = _samples(257, seed=12)
+    got = np.zeros(len(X))
+    o.orc_mlp_forward(ptr(P), ptr(X), len(X), ptr(got))
+    want = _forward_np(P, X)
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-18)
+    # the constant unit: changing row 63 of W1 changes nothing
+    P2 = P.copy()
+    P2[(NH - 1) * NIN: NH * NIN] = 5.0
+    got2 = np.zeros(len(X))
+    o.orc_mlp_forward(ptr(P2), ptr(X), len(X), ptr(got2))
+    np.testing.assert_array_equal(got, got2)
+    # and both ReLU branches are live in layer 1
+    z1 = X.astype(np.float64) @ P[: NH * NIN].reshape(NH, NIN).astype(np.float64).T
+    assert (z1 > 0).mean() > 0.2 and (z1 < 0).mean() > 0.2
+
+
 def _features_np(p, tau0):
     m = np.array([[p[0], p[3], p[4]], [p[3], p[1], p[5]], [p[4], p[5], p[2]]])
     pp = float((m * m).sum())
