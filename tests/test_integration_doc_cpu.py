@@ -70,3 +70,24 @@ def test_fragments_compile(tmp_path):
                             "-Werror=incompatible-pointer-types", "-Werror=int-conversion", str(src),
                             f"-I{ROOT / 'include'}"], capture_output=True, text=True)
         assert r.returncode == 0, (frag, r.stderr)
+
+
+def test_python_examples_use_the_package_api(product):
+    """the Python examples parse, and every `lbm.X` and every method they
+    call on a Solver (`s.`) or an Ensemble (`e.`) exists; every `lib.X` is a
+    symbol the library exports"""
+    import ast
+    import ctypes
+
+    text = (ROOT / "INTEGRATION.md").read_text()
+    blocks = [b for lang, b in re.findall(r"```(\w*)\n(.*?)```", text, re.S) if lang == "python"]
+    assert len(blocks) >= 3
+    owners = {"lbm": product, "s": product.Solver, "e": product.Ensemble,
+              "lib": ctypes.CDLL(str(Path(product.__file__).parent / "_build" / "liblbm_gb300.so"))}
+    seen = 0
+    for b in blocks:
+        for node in ast.walk(ast.parse(b)):
+            if isinstance(node, ast.Attribute) and isinstance(node.value, ast.Name) and node.value.id in owners:
+                assert hasattr(owners[node.value.id], node.attr), (node.value.id, node.attr)
+                seen += 1
+    assert seen >= 10
