@@ -238,6 +238,16 @@ int lbm_mlp_train(const float* d_X, const float* d_T, int n, int batch, int step
  * memory, samples and output on the device;
  * synchronous on stream */
 int lbm_mlp_predict_tc(const float* params, const float* d_X, int n, float* d_nu, void* stream);
+/* the weight blob the tensor-core inference stages in shared memory, from
+ * a parameter vector (host memory, lbm_mlp_blob_bytes() bytes):
+ * W1 [64][16] with row 63 = e15 (the constant unit), W2 [64][64] with
+ * column 63 = W2[:,63] + b2, W3 [16][64] with row 0 = w3 and the rest zero,
+ * all bf16 (round to nearest even) in the K-major core-matrix layout (core
+ * matrix (i, j), rows 8i..8i+7 and columns 8j..8j+7, at i * SBO + j * 128
+ * bytes with SBO 256 for W1 and 1024 for W2 and W3, row r of a core matrix
+ * at 16 r), then b3 as FP32 and 12 zero bytes */
+size_t lbm_mlp_blob_bytes(void);
+int lbm_mlp_make_blob(const float* params, unsigned char* blob);
 /* tensor-core self-check: D[128][64] = A[128][16 kc] * B[64][16 kc]^T with
  * BF16 operands (raw 16-bit patterns) and an FP32 accumulator, through
  * tcgen05.mma; kc = 1..4; host pointers */

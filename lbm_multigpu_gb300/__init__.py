@@ -62,6 +62,8 @@ SIGNATURES = [
     ("lbm_get_last_force", _I, [_P, _P]),
     ("lbm_get_last_force_async", _I, [_P, _P]),
     ("lbm_mlp_param_count", _I, []),
+    ("lbm_mlp_blob_bytes", _SZ, []),
+    ("lbm_mlp_make_blob", _I, [_P, _P]),
     ("lbm_mlp_init_params", _I, [ctypes.c_uint32, _P]),
     ("lbm_mlp_grad", _I, [_P, _P, _P, _I, _P, _P, _P]),
     ("lbm_mlp_predict", _I, [_P, _P, _I, _P, _P]),

@@ -89,6 +89,14 @@ extern "C" {
 
 int lbm_mlp_param_count(void) { return sgs::NPARAM; }
 
+size_t lbm_mlp_blob_bytes(void) { return sgs::BLOB_BYTES; }
+
+int lbm_mlp_make_blob(const float* params, unsigned char* blob) {
+    if (!params || !blob) return set_error(LBM_ERR_ARG, "null argument", cudaSuccess);
+    mlp_make_blob(params, blob);
+    return LBM_OK;
+}
+
 int lbm_mlp_init_params(uint32_t seed, float* params) {
     if (!params) return set_error(LBM_ERR_ARG, "params is null", cudaSuccess);
     Rng r(seed);

@@ -181,3 +181,51 @@ def test_host_samples_stay_clear_of_solids():
     fluid[:, 10:12, 10:12] = False       # one coarse column solid
     X2, _ = samples_from_velocity(u, fluid, 0.505, margin=2)
     assert len(X2) == 4 * (64 - 25)      # the 5 x 5 cells around it drop out (all inside the interior)
+
+
+def _bf16(a):
+    """round FP32 to bf16 (nearest even) and back to FP32"""
+    u = np.asarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16
+    return (u.astype(np.uint32) << 16).view(np.float32)
+
+
+def _core(blob, rows, k, sbo):
+    """a bf16 matrix [rows][k] read back from the K-major core-matrix layout"""
+    out = np.zeros((rows, k), np.float32)
+    for r in range(rows):
+        for c in range(k):
+            off = (r // 8) * sbo + (c // 8) * 128 + (r % 8) * 16 + (c % 8) * 2
+            out[r, c] = (np.frombuffer(blob[off: off + 2], "<u2").astype(np.uint32) << 16).view(np.float32)[0]
+    return out
+
+
+def test_weight_blob_folds_the_biases(product):
+    """the tensor-core weight blob from a parameter vector: W1 with the
+    constant unit's row e15, W2 with b2 folded into column 63, the output
+    layer as row 0 of a 16-row W3, b3 in FP32 -- all bf16 in the core-matrix
+    layout the MMA descriptors read"""
+    lib = product.library()
+    P = _params(seed=5, scale=0.5)
+    nb = lib.lbm_mlp_blob_bytes()
+    blob = np.zeros(nb, np.uint8)
+    assert lib.lbm_mlp_make_blob(ptr(P), ptr(blob)) == 0
+    raw = blob.tobytes()
+    o = NH * NIN
+    W1, W2 = P[:o].reshape(NH, NIN), P[o: o + NH * NH].reshape(NH, NH)
+    b2, w3, b3 = P[o + NH * NH: o + NH * NH + NH], P[o + NH * NH + NH: o + NH * NH + 2 * NH], P[-1]
+    want1 = W1.copy()
+    want1[NH - 1] = 0
+    want1[NH - 1, NIN - 1] = 1
+    np.testing.assert_array_equal(_core(raw[: NH * NIN * 2], NH, NIN, 256), _bf16(want1))
+    w2_off = NH * NIN * 2
+    want2 = W2.copy()
+    want2[:, NH - 1] = W2[:, NH - 1] + b2
+    np.testing.assert_array_equal(_core(raw[w2_off: w2_off + NH * NH * 2], NH, NH, 1024), _bf16(want2))
+    w3_off = w2_off + NH * NH * 2
+    got3 = _core(raw[w3_off: w3_off + 16 * NH * 2], 16, NH, 1024)
+    np.testing.assert_array_equal(got3[0], _bf16(w3))
+    assert not got3[1:].any()
+    b3_off = w3_off + 16 * NH * 2
+    assert np.frombuffer(raw[b3_off: b3_off + 4], "<f4")[0] == b3
+    assert nb == b3_off + 16 and not blob[b3_off + 4:].any()
