@@ -229,3 +229,35 @@ def test_weight_blob_folds_the_biases(product):
     b3_off = w3_off + 16 * NH * 2
     assert np.frombuffer(raw[b3_off: b3_off + 4], "<f4")[0] == b3
     assert nb == b3_off + 16 and not blob[b3_off + 4:].any()
+
+
+def test_bf16_inference_error_is_within_the_gpu_tolerance(product):
+    """the tensor-core inference's rounding, emulated: bf16 features, the
+    blob's bf16 weights, FP32 accumulation, ReLU then bf16 for each hidden
+    layer, b3 in FP32.  Its distance to the FP64 oracle forward on the GPU
+    test's inputs stays inside that test's 2 % (rounding alone accounts
+    for it) and is not zero (the tolerance is not slack)"""
+    lib = product.library()
+    rng = np.random.default_rng(8)
+    P = np.zeros(NPARAM, np.float32)
+    assert lib.lbm_mlp_init_params(13, ptr(P)) == 0
+    P[NH * NIN + NH * NH: NH * NIN + NH * NH + NH] = 0.1
+    X = (rng.standard_normal((3000, NIN)) * 0.7).astype(np.float32)
+    X[:, 15] = 1
+    blob = np.zeros(lib.lbm_mlp_blob_bytes(), np.uint8)
+    assert lib.lbm_mlp_make_blob(ptr(P), ptr(blob)) == 0
+    raw = blob.tobytes()
+    w2_off = NH * NIN * 2
+    w3_off = w2_off + NH * NH * 2
+    W1 = _core(raw[:w2_off], NH, NIN, 256).astype(np.float64)
+    W2 = _core(raw[w2_off:w3_off], NH, NH, 1024).astype(np.float64)
+    w3 = _core(raw[w3_off: w3_off + 16 * NH * 2], 16, NH, 1024)[0].astype(np.float64)
+    b3 = float(np.frombuffer(raw[w3_off + 16 * NH * 2: w3_off + 16 * NH * 2 + 4], "<f4")[0])
+    h1 = _bf16(np.maximum((_bf16(X).astype(np.float64) @ W1.T).astype(np.float32), 0)).astype(np.float64)
+    h2 = _bf16(np.maximum((h1 @ W2.T).astype(np.float32), 0)).astype(np.float64)
+    y = (h2 @ w3).astype(np.float32).astype(np.float64) + b3
+    emulated = 1e-4 * np.logaddexp(0, y)
+    want = np.zeros(len(X))
+    oracle().orc_mlp_forward(ptr(P), ptr(X), len(X), ptr(want))
+    err = np.linalg.norm(emulated - want) / np.linalg.norm(want)
+    assert 1e-5 < err < 2e-2, err
