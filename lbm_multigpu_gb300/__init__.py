@@ -170,6 +170,7 @@ def make_inputs(nx: int, ny: int, nz: int, *, obst1=(0.0, 0.0, 0.0), r1=1.0, obs
     arguments named after the record keys: geometry="cavity", tau=0.6,
     lid_velocity=(0.05, 0, 0), lid_face="+z", precision="fp16",
     inlet_noise=0.01, seed=12345, velav=1, init=1, init_velocity=0.0,
+    layout="blocked" (population layout: "soa", "blocked" or "auto"),
     faces=("DIR_WEST", "NEU_EAST", "YSYM_BOT", "YSYM_TOP", "-", "-") (a node
     type name from NODE per face x = 0, x = nx-1, y = 0, y = ny-1, z = 0,
     z = nz-1; "-" keeps the geometry's own).
@@ -212,7 +213,7 @@ def make_inputs(nx: int, ny: int, nz: int, *, obst1=(0.0, 0.0, 0.0), r1=1.0, obs
              "edge_pull": "EDGE PULL:", "lid_bc": "LID BC:", "bounceback": "BOUNCEBACK:", "sgs": "SGS:",
              "sgs_weights": "SGS weights:", "dyny1": "DYNY1:", "dyn_every": "DYN every:",
              "dyn_start": "DYN start:", "trip_end": "TRIP end:", "kp": "KP:", "faces": "FACES:",
-             "cf_time": "CF TIME:"}
+             "cf_time": "CF TIME:", "layout": "LAYOUT:"}
     for k, v in ext.items():
         if k not in names:
             raise KeyError(f"unknown .inputs extension key {k!r}")

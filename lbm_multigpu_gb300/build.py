@@ -1,7 +1,8 @@
 """Build liblbm_gb300.so in-tree (lbm_multigpu_gb300/_build/) with nvcc for sm_103a.
 
 Translation units compiled in parallel and linked into one shared library:
-the CUDA kernels (csrc/lbm_kernels.cu), the C ABI host side
+the CUDA kernels (csrc/lbm_kernels.cu, and csrc/lbm_blocked.cu for the
+blocked population layout), the C ABI host side
 (csrc/lbm_host.cpp), the allocation-free force entry point
 (csrc/lbm_noalloc.cu), and the learned subgrid closure (csrc/sgs_mlp.cu
 kernels, csrc/lbm_sgs.cpp host side), and the ensemble of periodic boxes
@@ -38,7 +39,7 @@ def nvcc() -> str:
 
 
 def sources() -> list[Path]:
-    return [CSRC / "lbm_kernels.cu", CSRC / "lbm_host.cpp", CSRC / "lbm_noalloc.cu", CSRC / "sgs_mlp.cu",
+    return [CSRC / "lbm_kernels.cu", CSRC / "lbm_blocked.cu", CSRC / "lbm_host.cpp", CSRC / "lbm_noalloc.cu", CSRC / "sgs_mlp.cu",
             CSRC / "lbm_sgs.cpp", CSRC / "ensemble.cu", CSRC / "lbm_ensemble.cpp", CSRC / "lbm_post.cpp"]
 
 

@@ -77,6 +77,10 @@ struct Config {
     /* extension keys (not in the reference record) */
     std::string geometry = "channel_square";
     std::string precision = "fp32";
+    /* "LAYOUT: soa | blocked | auto": population layout in HBM; auto keeps
+     * FP32 and FP64 in the reference's structure-of-arrays layout and stores
+     * FP16 / BF16 in blocks of 32 nodes */
+    std::string pop_layout = "auto";
     float tau = 0;                  /* > 0: tau0 given directly instead of RE */
     float lid_u[3] = {0, 0, 0};
     bool lid_u_set = false;
@@ -214,6 +218,10 @@ int parse_inputs(const char* text, Config& c) {
         /* extension keys */
         else if (key == "GEOMETRY") c.geometry = val;
         else if (key == "PRECISION") c.precision = val;
+        else if (key == "LAYOUT") {
+            ok = (val == "soa" || val == "blocked" || val == "auto");
+            c.pop_layout = val;
+        }
         else if (key == "TAU") F(c.tau);
         else if (key == "LID velocity") { ok = parse_tuple(val, c.lid_u); c.lid_u_set = true; }
         else if (key == "LID face") {
@@ -331,6 +339,7 @@ std::string value_of(const Config& c, const std::string& key, float omega, float
     else if (key == "GPUs per node") o << c.gpus;
     else if (key == "GEOMETRY") o << c.geometry;
     else if (key == "PRECISION") o << c.precision;
+    else if (key == "LAYOUT") o << c.pop_layout;
     else if (key == "TAU") o << c.tau;
     else if (key == "LID velocity") o << "(" << c.lid_u[0] << "," << c.lid_u[1] << "," << c.lid_u[2] << ")";
     else if (key == "LID face") o << faces[c.lid_face];
@@ -396,6 +405,7 @@ std::string write_inputs(const Config& c, float omega, float omegaLR) {
     Config d;
     if (c.geometry != d.geometry) line("GEOMETRY: ", "GEOMETRY");
     if (c.precision != d.precision) line("PRECISION: ", "PRECISION");
+    if (c.pop_layout != d.pop_layout) line("LAYOUT: ", "LAYOUT");
     if (c.tau > 0.f) line("TAU: ", "TAU");
     if (c.lid_u_set) line("LID velocity: ", "LID velocity");
     if (c.lid_face != d.lid_face) line("LID face: ", "LID face");
@@ -607,7 +617,7 @@ void set_offsets(Level& L, float u0) {
     }
 }
 
-int alloc_level(LevelState& s, int nx, int ny, int nz, int storage, bool stats, float u_ref) {
+int alloc_level(LevelState& s, int nx, int ny, int nz, int storage, bool blocked, bool stats, float u_ref) {
     Level& L = s.L;
     L.nx = nx;
     L.ny = ny;
@@ -616,6 +626,7 @@ int alloc_level(LevelState& s, int nx, int ny, int nz, int storage, bool stats, 
     L.plane = (long long)L.pitch * ny;
     L.qstride = L.plane * nz;
     L.storage = storage;
+    L.blocked = blocked ? 1 : 0;
     set_offsets(L, u_ref);
     if (L.qstride * 19 >= (1LL << 31))
         return fail(LBM_ERR_CONFIG, "level %dx%dx%d too large: 19 populations must index below 2^31", nx, ny, nz);
@@ -1062,6 +1073,8 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
     if (model < 0) return fail(LBM_ERR_CONFIG, "MODEL '%s' is not one of MRT, MRT_DI3, BGK, MRT_CPU3D", c.model.c_str());
     const int storage = storage_id(c.precision);
     if (storage < 0) return fail(LBM_ERR_CONFIG, "PRECISION '%s' is not one of fp32, fp16, bf16, fp64", c.precision.c_str());
+    const bool blocked = c.pop_layout == "blocked" || (c.pop_layout == "auto" && (storage == STORE_F16 || storage == STORE_BF16));
+    if (blocked && storage == STORE_F64) return fail(LBM_ERR_CONFIG, "LAYOUT blocked is for FP32, FP16 and BF16 storage");
     static const char* geoms[] = {"channel_square", "channel_circle", "channel", "cavity", "periodic", "dyninlet", "duct"};
     if (std::find(std::begin(geoms), std::end(geoms), c.geometry) == std::end(geoms))
         return fail(LBM_ERR_CONFIG, "GEOMETRY '%s' is not supported", c.geometry.c_str());
@@ -1129,7 +1142,7 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
     }
     /* reference velocity of the FP16/BF16 offsets: the inlet velocity of a channel */
     const float u_ref = c.geometry.rfind("channel", 0) == 0 || c.geometry == "duct" ? c.umax : 0.f;
-    if ((rc = alloc_level(h->lv[0], c.nx, c.ny, c.nz, storage, c.velav != 0, u_ref))) return bail(rc);
+    if ((rc = alloc_level(h->lv[0], c.nx, c.ny, c.nz, storage, blocked, c.velav != 0, u_ref))) return bail(rc);
     mask_base(c, h->lv[0].hmask);
     h->trip_in_mask = c.geometry == "dyninlet" && c.trip_end > 0;
     if (c.dyny1 >= 0) {
@@ -1143,7 +1156,7 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
     }
     if ((rc = upload_mask(h, 0))) return bail(rc);
     if (c.refinement) {
-        if ((rc = alloc_level(h->lv[1], c.lrx, c.lry, c.lrz, storage, c.velav != 0, u_ref))) return bail(rc);
+        if ((rc = alloc_level(h->lv[1], c.lrx, c.lry, c.lrz, storage, blocked, c.velav != 0, u_ref))) return bail(rc);
         mask_fine(c, h->lv[1].hmask);
         if ((rc = upload_mask(h, 1))) return bail(rc);
         h->enx = int(c.lrx * c.lrfactor) + 1;
@@ -1278,7 +1291,7 @@ int lbm_get_populations(lbm_handle* h, int level, float* f) {
     if (!f) return fail(LBM_ERR_ARG, "f is null");
     LevelState& s = h->lv[level];
     const size_t n = size_t(s.L.nx) * s.L.ny * s.L.nz * 19;
-    if (s.L.storage == STORE_F32 && s.L.pitch == s.L.nx) {
+    if (s.L.storage == STORE_F32 && s.L.pitch == s.L.nx && !s.L.blocked) {
         /* FP32 without row padding: the stored layout is the caller's */
         cudaError_t e = cudaMemcpyAsync(f, s.f[s.cur], n * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -1301,7 +1314,7 @@ int lbm_set_populations(lbm_handle* h, int level, const float* f) {
     if (!f) return fail(LBM_ERR_ARG, "f is null");
     LevelState& s = h->lv[level];
     const size_t n = size_t(s.L.nx) * s.L.ny * s.L.nz * 19;
-    if (s.L.storage == STORE_F32 && s.L.pitch == s.L.nx) {
+    if (s.L.storage == STORE_F32 && s.L.pitch == s.L.nx && !s.L.blocked) {
         /* FP32 without row padding: straight into both buffers */
         cudaError_t e = cudaMemcpyAsync(s.f[0], f, n * sizeof(float), cudaMemcpyHostToDevice, h->stream);
         if (e == cudaSuccess)
@@ -1400,7 +1413,9 @@ int lbm_save_state(lbm_handle* h, const char* path) {
     for (int l = 0; l < h->nlevels; ++l) {
         const LevelState& s = h->lv[l];
         const Level& L = s.L;
-        const int32_t hdr[6] = {L.nx, L.ny, L.nz, L.pitch, h->storage, s.stats ? 1 : 0};
+        /* storage code + 256 for the blocked layout: the raw populations are
+         * only readable back into the same layout */
+        const int32_t hdr[6] = {L.nx, L.ny, L.nz, L.pitch, h->storage + 256 * L.blocked, s.stats ? 1 : 0};
         for (int32_t v : hdr) put(o, v);
         /* the stored populations as they are (raw FP16 / BF16 / FP32 / FP64) */
         std::vector<char> raw(size_t(L.qstride) * 19 * storage_bytes(h->storage));
@@ -1474,9 +1489,11 @@ int lbm_restore_state(lbm_handle* h, const char* path) {
         int32_t hdr[6];
         for (int32_t& v : hdr)
             if (!get(in, v)) return fail(LBM_ERR_PARSE, "checkpoint: truncated level header");
-        if (hdr[0] != L.nx || hdr[1] != L.ny || hdr[2] != L.nz || hdr[3] != L.pitch || hdr[4] != h->storage)
-            return fail(LBM_ERR_CONFIG, "checkpoint: level %d is %dx%dx%d (pitch %d, storage %d), the handle's %dx%dx%d",
-                        l, hdr[0], hdr[1], hdr[2], hdr[3], hdr[4], L.nx, L.ny, L.nz);
+        if (hdr[0] != L.nx || hdr[1] != L.ny || hdr[2] != L.nz || hdr[3] != L.pitch ||
+            hdr[4] != h->storage + 256 * L.blocked)
+            return fail(LBM_ERR_CONFIG, "checkpoint: level %d is %dx%dx%d (pitch %d, storage %d, layout %s), the "
+                        "handle's %dx%dx%d (storage %d, layout %s)", l, hdr[0], hdr[1], hdr[2], hdr[3], hdr[4] & 255,
+                        hdr[4] >= 256 ? "blocked" : "soa", L.nx, L.ny, L.nz, h->storage, L.blocked ? "blocked" : "soa");
         std::vector<char> raw(size_t(L.qstride) * 19 * storage_bytes(h->storage));
         if (!in.read(raw.data(), std::streamsize(raw.size()))) return fail(LBM_ERR_PARSE, "checkpoint: truncated level");
         for (int b = 0; b < 2; ++b) CUDA_TRY(cudaMemcpy(s.f[b], raw.data(), raw.size(), cudaMemcpyHostToDevice));

@@ -47,16 +47,32 @@ enum Model : int { MRT = 0, MRT_DI3 = 1, BGK = 2, MRT_CPU3D = 3 };
 
 enum Storage : int { STORE_F32 = 0, STORE_F16 = 1, STORE_BF16 = 2, STORE_F64 = 3 };
 
-/* One grid level in HBM.  Populations are structure-of-arrays,
- * f[q][z][y][x] with a padded x pitch; q-planes are qstride elements apart. */
+/* One grid level in HBM.  Nodes are numbered c = z plane + y pitch + x with
+ * a padded x pitch (a multiple of 32).  Populations are stored either
+ *   structure-of-arrays: f[q][z][y][x], q-planes qstride elements apart (the
+ *     reference's layout, LR7:210-216), or
+ *   blocked: the 32 nodes x = 32 b .. 32 b + 31 of a row keep their 19
+ *     populations together as 19 rows of 32, f[z][y][x / 32][q][x % 32], so
+ *     that the offset of population q from a node's population 0 is the
+ *     constant 32 q. */
 struct Level {
     int nx, ny, nz;
     int pitch;            /* elements per row, a multiple of 32 */
     long long plane;      /* pitch * ny */
     long long qstride;    /* plane * nz */
     int storage;          /* Storage */
+    int blocked;          /* 0: structure-of-arrays, 1: blocks of 32 nodes */
     float off[19];        /* FP16/BF16 store f - off[q] (equilibrium at the reference velocity) */
 };
+
+/* elements of one 32-node block of the blocked layout */
+constexpr unsigned BLOCK_ELEMS = 19u * 32u;
+
+/* element offset of population q of node c in either layout */
+__host__ __device__ __forceinline__ unsigned pidx(const Level& L, int q, unsigned c) {
+    return L.blocked ? (c >> 5) * BLOCK_ELEMS + (unsigned(q) << 5) + (c & 31u)
+                     : unsigned(q) * unsigned(L.qstride) + c;
+}
 
 struct StepParams {
     int model;

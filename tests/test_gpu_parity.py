@@ -804,3 +804,63 @@ def test_set_geometry_and_write_tecplot(product, tmp_path):
     for suffix in ("_part0.dat", "_slice.dat"):
         assert (tmp_path / f"t{suffix}").read_bytes() == (tmp_path / f"o{suffix}").read_bytes()
     assert not (tmp_path / "t.force").exists()
+
+
+def _run_layout(lbm, text, steps, levels=1):
+    with lbm.Solver(text) as s:
+        s.step(steps)
+        out = [s.populations(l) for l in range(levels)] + [s.forces(steps)]
+        if "\nVELAV: \t1\n" in text:
+            out.append(s.stats())
+    return out
+
+
+@pytest.mark.parametrize("case", ["channel_fp32", "channel_fp16", "channel_bf16", "refine_fp16", "cavity_fp32",
+                                  "duct_fp16"])
+def test_population_layouts_are_bit_exact(product, case):
+    """the blocked population layout (the 19 populations of 32 x-consecutive
+    nodes together) runs the same arithmetic as the structure-of-arrays
+    layout: identical populations, statistics and force histories after 40
+    steps for half-way channels with inlet noise and statistics, a two-level
+    refinement, the lid-driven cavity and a duct with alternate boundaries"""
+    lbm = product
+    steps = 40
+    prec = case.split("_")[1]
+    levels = 1
+    if case.startswith("channel"):
+        kw = dict(precision=prec, bounceback="halfway", inlet_noise=0.01, seed=5, velav=1, start_velav=10,
+                  start_velfluc=25)
+        make = lambda lay: _chan_inputs(lbm, steps, layout=lay, **kw)  # noqa: E731
+    elif case.startswith("refine"):
+        levels = 2
+        make = lambda lay: lbm.make_inputs(  # noqa: E731
+            128, 48, 8, obst1=(40.5, 23.5, 0.0), r1=3.0, re=60.0, umax=0.05, tmax=steps, les=1, cs=0.01,
+            refinement=1, lr_dims=(48, 48, 16), lr_factor=0.5, lr_origin=(28.25, 12.25, -0.75),
+            geometry="channel_square", cf_time="linear", precision=prec, layout=lay)
+    elif case.startswith("cavity"):
+        make = lambda lay: lbm.make_inputs(40, 40, 40, umax=0.05, tmax=steps, model="BGK", geometry="cavity",  # noqa
+                                           tau=0.6, lid_velocity=(0.05, 0, 0), lid_face="+z", precision=prec,
+                                           layout=lay)
+    else:
+        make = lambda lay: lbm.make_inputs(  # noqa: E731
+            48, 24, 12, obst1=(12.5, 11.5, 0.0), r1=4.0, re=40.0, umax=0.04, tmax=steps, les=1, cs=0.02,
+            model="MRT", geometry="duct", faces=("DIR_WEST", "NEU_EAST", "YSYM_BOT", "YSYM_TOP", "ZSYM_BOT",
+                                                 "ZSYM_TOP"), precision=prec, layout=lay)
+    a = _run_layout(lbm, make("soa"), steps, levels)
+    b = _run_layout(lbm, make("blocked"), steps, levels)
+    assert np.isfinite(a[0]).all()
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_checkpoint_layout_must_match(product, tmp_path):
+    """raw populations of a blocked-layout checkpoint are not read back into
+    a structure-of-arrays handle"""
+    lbm = product
+    path = str(tmp_path / "blk.ckpt")
+    with lbm.Solver(_chan_inputs(lbm, 10, precision="fp16", layout="blocked")) as s:
+        s.step(5)
+        s.save_state(path)
+    with lbm.Solver(_chan_inputs(lbm, 10, precision="fp16", layout="soa")) as s:
+        with pytest.raises(lbm.LbmError, match="layout"):
+            s.restore_state(path)
