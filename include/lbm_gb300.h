@@ -91,6 +91,11 @@ int lbm_get_dims(const lbm_handle* h, int level, int* nx, int* ny, int* nz);
 int lbm_get_nlevels(const lbm_handle* h, int* nlevels);
 /* relaxation rates (LR7:2607-2619): omega, omegaLR, SF_cf, SF_fc */
 int lbm_get_params(const lbm_handle* h, float* omega4);
+/* the 19 offsets a level's FP16 / BF16 storage subtracts before rounding
+ * (the collision model's equilibrium at density 1 and the reference
+ * velocity); zeros for FP32 / FP64.  No counterpart in the reference, which
+ * stores FP32 populations (LR7:2676-2678). */
+int lbm_get_storage_offsets(const lbm_handle* h, int level, float* off19);
 /* steps taken so far */
 int lbm_get_time(const lbm_handle* h, int* t);
 

@@ -47,6 +47,7 @@ SIGNATURES = [
     ("lbm_get_dims", _I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("lbm_get_nlevels", _I, [_P, ctypes.POINTER(_I)]),
     ("lbm_get_params", _I, [_P, _P]),
+    ("lbm_get_storage_offsets", _I, [_P, _I, _P]),
     ("lbm_get_time", _I, [_P, ctypes.POINTER(_I)]),
     ("lbm_get_mask", _I, [_P, _I, _P]),
     ("lbm_set_mask", _I, [_P, _I, _P]),
@@ -309,6 +310,12 @@ class Solver:
         o = np.zeros(4, np.float32)
         _check(self._lib.lbm_get_params(self._h, _ptr(o)))
         return dict(omega=float(o[0]), omega_lr=float(o[1]), sf_cf=float(o[2]), sf_fc=float(o[3]))
+
+    def storage_offsets(self, level: int = 0) -> np.ndarray:
+        """the offsets FP16 / BF16 storage subtracts (zeros for FP32 / FP64)"""
+        o = np.zeros(19, np.float32)
+        _check(self._lib.lbm_get_storage_offsets(self._h, level, _ptr(o)))
+        return o
 
     @property
     def time(self) -> int:

@@ -215,6 +215,118 @@ __host__ __device__ __forceinline__ void collide_mrt(T f[19], T omega, bool les,
     }
 }
 
+/* LR7's MRT collision with Smagorinsky (LR7:583-711) in projected form, on
+ * the deviations h = f - feq(1, (U, 0, 0)) of the populations from the
+ * model's own equilibrium at density 1 and the reference velocity U along x
+ * (the offsets of FP16 / BF16 storage), updated in place as such.
+ *
+ * The same map as collide_mrt<MRT>: there every non-conserved moment except
+ * the five stresses m9, m11, m13, m14, m15 relaxes at rate 1, that is to its
+ * equilibrium, so the post-collision moments are meq(rho, j) plus (1 - omega)
+ * times the stress non-equilibrium, and the populations follow from them by
+ * the inverse basis M^T diag(1 / |M_k|^2).  Only rho, j, the five stresses
+ * and (for the eddy viscosity) m1 need the populations; even and odd parts
+ * of each opposite pair are then rebuilt directly.  Subtracting the
+ * equilibrium at (1, U) leaves the deviations: rho - 1, j - (U, 0, 0) in the
+ * linear terms, j^2 - U^2 in the quadratic ones, meq(J) in the stresses.
+ * Equilibrium moments (incompressible, rho0 = 1): meq1 = -11 rho + 19 j^2,
+ * meq2 = 7.53968254 j^2 (LR7's sign), meq4,6,8 = -2/3 j, meq9 = 2 jx^2 -
+ * jy^2 - jz^2, meq11 = jy^2 - jz^2, meq13,14,15 = jx jy, jy jz, jx jz,
+ * meq10 = meq12 = meq16,17,18 = 0. */
+template <class T> __host__ __device__ __forceinline__ void collide_mrt_dev(T f[19], T omega, bool les, T cs, T U) {
+    const T sx = f[1] + f[3], dx = f[1] - f[3];
+    const T sy = f[2] + f[4], dy = f[2] - f[4];
+    const T sz = f[9] + f[14], dz = f[9] - f[14];
+    const T a5 = f[5] + f[7], b5 = f[5] - f[7];
+    const T a6 = f[6] + f[8], b6 = f[6] - f[8];
+    const T a10 = f[10] + f[17], b10 = f[10] - f[17];
+    const T a12 = f[12] + f[15], b12 = f[12] - f[15];
+    const T a11 = f[11] + f[18], b11 = f[11] - f[18];
+    const T a13 = f[13] + f[16], b13 = f[13] - f[16];
+    const T axy = a5 + a6, axz = a10 + a12, ayz = a11 + a13;
+    const T sdi = axy + axz + ayz;
+    const T rho = f[0] + (sx + sy + sz) + sdi;                 /* rho - 1 */
+    const T jx = dx + (b5 - b6) + (b10 - b12);                 /* jx - U */
+    const T jy = dy + (b5 + b6) + (b11 - b13);
+    const T jz = dz + (b10 + b12) + (b11 + b13);
+    const T Jx = jx + U;                                       /* the momentum */
+    const T jxx = Jx * Jx, jyy = jy * jy, jzz = jz * jz;
+    const T U2 = U * U;
+    const T q2 = (jxx - U2) + (jyy + jzz);                     /* j^2 - U^2 */
+    const T m9eq = T(2) * jxx - (jyy + jzz), m11eq = jyy - jzz;
+    const T jxy = Jx * jy, jyz = jy * jz, jxz = Jx * jz;
+    /* stress non-equilibrium moments (the linear parts of the deviations
+     * plus those of the equilibrium at (1, U): 2 U^2 for m9, 0 else) */
+    const T n9 = (T(2) * sx - sy - sz + axy + axz - T(2) * ayz) + (T(2) * U2 - m9eq);
+    const T n11 = (sy - sz + axy - axz) - m11eq;
+    const T n13 = (a5 - a6) - jxy, n14 = (a11 - a13) - jyz, n15 = (a10 - a12) - jxz;
+    if (les) {
+        /* Pi_neq as collide_mrt forms it: n1 = 19 (sdi - f0 - j^2) with the
+         * equilibrium's 19 U^2 */
+        const T n1 = T(19) * ((sdi - f[0]) - q2);
+        const T tr = n1 * T(1.0 / 19.0);
+        const T pxx = n1 * T(1.0 / 57.0) + n9 * T(1.0 / 3.0);
+        const T pyy = T(0.5) * (tr - pxx + n11), pzz = T(0.5) * (tr - pxx - n11);
+        const T qn = lsqrt(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (n13 * n13 + n14 * n14 + n15 * n15));
+        omega = smag_omega(omega, cs, qn);
+    }
+    const T c1 = T(1) - omega;
+    /* post-collision stresses less their value at (1, U), over the row norms */
+    const T t9 = ((m9eq - T(2) * U2) + c1 * n9) * T(1.0 / 36.0);
+    const T t11 = (m11eq + c1 * n11) * T(1.0 / 12.0);
+    const T t13 = (jxy + c1 * n13) * T(0.25), t14 = (jyz + c1 * n14) * T(0.25), t15 = (jxz + c1 * n15) * T(0.25);
+    /* rho / 19 + meq1 M1 / 2394 + meq2 M2 / 252 for the rest, axis and
+     * diagonal rows (M1 = -30, -11, 8; M2 = 12, -4, 1) */
+    const T A0 = T(1.0 / 19.0 + 330.0 / 2394.0) * rho + T(-570.0 / 2394.0 + 12.0 * 7.53968254 / 252.0) * q2;
+    const T Aa = T(1.0 / 19.0 + 121.0 / 2394.0) * rho + T(-209.0 / 2394.0 - 4.0 * 7.53968254 / 252.0) * q2;
+    const T Ad = T(1.0 / 19.0 - 88.0 / 2394.0) * rho + T(152.0 / 2394.0 + 7.53968254 / 252.0) * q2;
+    /* odd parts: c.j / 6 on the axes, c.j / 12 on the diagonals */
+    const T ox = jx * T(1.0 / 6.0), oy = jy * T(1.0 / 6.0), oz = jz * T(1.0 / 6.0);
+    const T hx = jx * T(1.0 / 12.0), hy = jy * T(1.0 / 12.0), hz = jz * T(1.0 / 12.0);
+    f[0] = A0;
+    {
+        const T e = Aa + T(2) * t9;
+        f[1] = e + ox;
+        f[3] = e - ox;
+    }
+    const T ayz9 = Aa - t9;
+    {
+        const T e = ayz9 + t11;
+        f[2] = e + oy;
+        f[4] = e - oy;
+    }
+    {
+        const T e = ayz9 - t11;
+        f[9] = e + oz;
+        f[14] = e - oz;
+    }
+    const T d9 = Ad + t9;
+    {   /* xy: (5,7) c = (1,1,0), (6,8) c = (-1,1,0) */
+        const T b = d9 + t11;
+        const T e5 = b + t13, o5 = hx + hy, e6 = b - t13, o6 = hy - hx;
+        f[5] = e5 + o5;
+        f[7] = e5 - o5;
+        f[6] = e6 + o6;
+        f[8] = e6 - o6;
+    }
+    {   /* xz: (10,17) c = (1,0,1), (12,15) c = (-1,0,1) */
+        const T b = d9 - t11;
+        const T e10 = b + t15, o10 = hx + hz, e12 = b - t15, o12 = hz - hx;
+        f[10] = e10 + o10;
+        f[17] = e10 - o10;
+        f[12] = e12 + o12;
+        f[15] = e12 - o12;
+    }
+    {   /* yz: (11,18) c = (0,1,1), (13,16) c = (0,-1,1) */
+        const T b = Ad - T(2) * t9;
+        const T e11 = b + t14, o11 = hy + hz, e13 = b - t14, o13 = hz - hy;
+        f[11] = e11 + o11;
+        f[18] = e11 - o11;
+        f[13] = e13 + o13;
+        f[16] = e13 - o13;
+    }
+}
+
 /* BGK with the incompressible equilibrium w (rho + 3 c.j + 4.5 (c.j)^2 - 1.5 j^2)
  * (DI3:806-827, CPU:116-162), optional Smagorinsky and AddForce (DI3:830). */
 template <class T> __host__ __device__ __forceinline__ void collide_bgk(T f[19], T omega, bool les, T cs, T dpdy) {

@@ -11,13 +11,13 @@ namespace lbm {
 
 cudaError_t launch_sc_blocked(const Level& L, const StepParams& p, const void* fA, void* fB, const uint8_t* mask,
                               float* stats, float* mom_export, cudaStream_t s, const uint32_t* links) {
-    return launch_sc_layout<true>(L, p, fA, fB, mask, stats, mom_export, s, links);
+    return launch_sc_layout<1>(L, p, fA, fB, mask, stats, mom_export, s, links);
 }
 
 cudaError_t launch_sc_mlp_blocked(const Level& L, const StepParams& p, const void* fA, void* fB,
                                   const uint8_t* mask, float* stats, const uint32_t* links, const void* blob, int* err,
                                   cudaStream_t s) {
-    return launch_sc_mlp_layout<true>(L, p, fA, fB, mask, stats, links, blob, err, s);
+    return launch_sc_mlp_layout<1>(L, p, fA, fB, mask, stats, links, blob, err, s);
 }
 
 }  // namespace lbm

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "../../include/lbm_gb300.h"
+#include "d3q19.cuh"
 #include "lbm_kernels.cuh"
 #include "sgs_infer.cuh"
 
@@ -219,7 +220,7 @@ int parse_inputs(const char* text, Config& c) {
         else if (key == "GEOMETRY") c.geometry = val;
         else if (key == "PRECISION") c.precision = val;
         else if (key == "LAYOUT") {
-            ok = (val == "soa" || val == "blocked" || val == "auto");
+            ok = (val == "soa" || val == "blocked" || val == "pairs" || val == "auto");
             c.pop_layout = val;
         }
         else if (key == "TAU") F(c.tau);
@@ -604,20 +605,26 @@ void free_level(LevelState& s) {
     s = LevelState();
 }
 
-/* FP16/BF16 offsets: the incompressible equilibrium at rho = 1 and the
- * reference velocity u0 (the inlet velocity of a channel, rest otherwise) */
-void set_offsets(Level& L, float u0) {
-    static const int CX[19] = {0, 1, 0, -1, 0, 1, -1, -1, 1, 0, 1, 0, -1, 0, 0, 1, 0, -1, 0};
+/* FP16/BF16 offsets: the collision model's own equilibrium at rho = 1 and
+ * the reference velocity u0 along x (the inlet velocity of a channel, rest
+ * otherwise), so that the stored deviations f - off vanish in the free
+ * stream.  It is the model's collision at omega = 1 of any state with that
+ * density and momentum (every moment then takes its equilibrium value); for
+ * LR7's MRT it differs from the lattice weights at rest (m2 has no density
+ * term there, LR7:583-711), for BGK it is the BGK equilibrium. */
+void set_offsets(Level& L, float u0, int model) {
+    const bool reduced = L.storage == STORE_F16 || L.storage == STORE_BF16;
+    double f[19];
     for (int q = 0; q < 19; ++q) {
-        const float w = q == 0 ? 1.f / 3.f : (q <= 4 || q == 9 || q == 14) ? 1.f / 18.f : 1.f / 36.f;
-        const float cu = float(CX[q]) * u0;
-        L.off[q] = (L.storage == STORE_F16 || L.storage == STORE_BF16)
-                       ? w * (1.f + 3.f * cu + 4.5f * cu * cu - 1.5f * u0 * u0)
-                       : 0.f;
+        const double cu = double(cx(q)) * u0;
+        f[q] = double(wq(q)) * (1.0 + 3.0 * cu + 4.5 * cu * cu - 1.5 * double(u0) * u0);
     }
+    collide<double>(model, f, 1.0, false, 0.0, 0.0);
+    for (int q = 0; q < 19; ++q) L.off[q] = reduced ? float(f[q]) : 0.f;
+    L.u_ref = reduced ? u0 : 0.f;
 }
 
-int alloc_level(LevelState& s, int nx, int ny, int nz, int storage, bool blocked, bool stats, float u_ref) {
+int alloc_level(LevelState& s, int nx, int ny, int nz, int storage, int blocked, bool stats, float u_ref, int model) {
     Level& L = s.L;
     L.nx = nx;
     L.ny = ny;
@@ -626,8 +633,8 @@ int alloc_level(LevelState& s, int nx, int ny, int nz, int storage, bool blocked
     L.plane = (long long)L.pitch * ny;
     L.qstride = L.plane * nz;
     L.storage = storage;
-    L.blocked = blocked ? 1 : 0;
-    set_offsets(L, u_ref);
+    L.blocked = blocked;
+    set_offsets(L, u_ref, model);
     if (L.qstride * 19 >= (1LL << 31))
         return fail(LBM_ERR_CONFIG, "level %dx%dx%d too large: 19 populations must index below 2^31", nx, ny, nz);
     const size_t bytes = size_t(L.qstride) * 19 * storage_bytes(storage);
@@ -978,7 +985,9 @@ int check_level(const lbm_handle* h, int level) {
 
 namespace {
 const char CKPT_MAGIC[12] = {'L', 'B', 'M', 'G', 'B', '3', '0', '0', 'C', 'K', 'P', 'T'};
-constexpr uint32_t CKPT_VERSION = 1;
+/* version 2: FP16 / BF16 levels store deviations from the collision model's
+ * equilibrium (version 1 stored them from the BGK equilibrium) */
+constexpr uint32_t CKPT_VERSION = 2;
 
 template <class V> void put(std::ostream& o, const V& v) { o.write(reinterpret_cast<const char*>(&v), sizeof v); }
 template <class V> bool get(std::istream& i, V& v) { return bool(i.read(reinterpret_cast<char*>(&v), sizeof v)); }
@@ -1073,7 +1082,8 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
     if (model < 0) return fail(LBM_ERR_CONFIG, "MODEL '%s' is not one of MRT, MRT_DI3, BGK, MRT_CPU3D", c.model.c_str());
     const int storage = storage_id(c.precision);
     if (storage < 0) return fail(LBM_ERR_CONFIG, "PRECISION '%s' is not one of fp32, fp16, bf16, fp64", c.precision.c_str());
-    const bool blocked = c.pop_layout == "blocked" || (c.pop_layout == "auto" && (storage == STORE_F16 || storage == STORE_BF16));
+    const int blocked = c.pop_layout == "blocked" ? 1 : c.pop_layout == "pairs" ? 2
+                        : (c.pop_layout == "auto" && (storage == STORE_F16 || storage == STORE_BF16)) ? 1 : 0;
     if (blocked && storage == STORE_F64) return fail(LBM_ERR_CONFIG, "LAYOUT blocked is for FP32, FP16 and BF16 storage");
     static const char* geoms[] = {"channel_square", "channel_circle", "channel", "cavity", "periodic", "dyninlet", "duct"};
     if (std::find(std::begin(geoms), std::end(geoms), c.geometry) == std::end(geoms))
@@ -1142,7 +1152,7 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
     }
     /* reference velocity of the FP16/BF16 offsets: the inlet velocity of a channel */
     const float u_ref = c.geometry.rfind("channel", 0) == 0 || c.geometry == "duct" ? c.umax : 0.f;
-    if ((rc = alloc_level(h->lv[0], c.nx, c.ny, c.nz, storage, blocked, c.velav != 0, u_ref))) return bail(rc);
+    if ((rc = alloc_level(h->lv[0], c.nx, c.ny, c.nz, storage, blocked, c.velav != 0, u_ref, model))) return bail(rc);
     mask_base(c, h->lv[0].hmask);
     h->trip_in_mask = c.geometry == "dyninlet" && c.trip_end > 0;
     if (c.dyny1 >= 0) {
@@ -1156,7 +1166,8 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
     }
     if ((rc = upload_mask(h, 0))) return bail(rc);
     if (c.refinement) {
-        if ((rc = alloc_level(h->lv[1], c.lrx, c.lry, c.lrz, storage, blocked, c.velav != 0, u_ref))) return bail(rc);
+        if ((rc = alloc_level(h->lv[1], c.lrx, c.lry, c.lrz, storage, blocked, c.velav != 0, u_ref, model)))
+            return bail(rc);
         mask_fine(c, h->lv[1].hmask);
         if ((rc = upload_mask(h, 1))) return bail(rc);
         h->enx = int(c.lrx * c.lrfactor) + 1;
@@ -1242,6 +1253,13 @@ int lbm_get_params(const lbm_handle* h, float* o) {
     o[1] = h->omegaLR;
     o[2] = h->sf_cf;
     o[3] = h->sf_fc;
+    return LBM_OK;
+}
+
+int lbm_get_storage_offsets(const lbm_handle* h, int level, float* off19) {
+    if (int rc = check_level(h, level)) return rc;
+    if (!off19) return fail(LBM_ERR_ARG, "off19 is null");
+    std::memcpy(off19, h->lv[level].L.off, sizeof(float) * 19);
     return LBM_OK;
 }
 
@@ -1459,6 +1477,8 @@ int lbm_save_state(lbm_handle* h, const char* path) {
     if (!o) return fail(LBM_ERR_ARG, "checkpoint: write to '%s' failed", path);
     return LBM_OK;
 }
+
+static const char* layout_name(int b) { return b == 0 ? "soa" : b == 1 ? "blocked" : b == 2 ? "pairs" : "unknown"; }
 
 static int read_checkpoint_record(std::istream& in, std::string& rec) {
     char magic[sizeof CKPT_MAGIC];
@@ -1842,7 +1862,7 @@ static int kernel_level(Level& L, int nx, int ny, int nz, int pitch) {
     L.plane = (long long)pitch * ny;
     L.qstride = L.plane * nz;
     L.storage = STORE_F32;
-    set_offsets(L, 0.f);
+    set_offsets(L, 0.f, MRT);
     if (L.qstride * 19 >= (1LL << 31)) return fail(LBM_ERR_ARG, "level too large: 19 populations must index below 2^31");
     return LBM_OK;
 }

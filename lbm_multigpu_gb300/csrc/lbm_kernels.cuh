@@ -49,29 +49,52 @@ enum Storage : int { STORE_F32 = 0, STORE_F16 = 1, STORE_BF16 = 2, STORE_F64 = 3
 
 /* One grid level in HBM.  Nodes are numbered c = z plane + y pitch + x with
  * a padded x pitch (a multiple of 32).  Populations are stored either
- *   structure-of-arrays: f[q][z][y][x], q-planes qstride elements apart (the
- *     reference's layout, LR7:210-216), or
- *   blocked: the 32 nodes x = 32 b .. 32 b + 31 of a row keep their 19
- *     populations together as 19 rows of 32, f[z][y][x / 32][q][x % 32], so
- *     that the offset of population q from a node's population 0 is the
- *     constant 32 q. */
+ *   0, structure-of-arrays: f[q][z][y][x], q-planes qstride elements apart
+ *     (the reference's layout, LR7:210-216), or in blocks of the 32 nodes
+ *     x = 32 b .. 32 b + 31 of a row, each block 19 x 32 elements holding
+ *     their 19 populations together:
+ *   1, rows: population q of lane l at 32 q + l;
+ *   2, pairs: population 0 at l, then the nine opposite pairs (q, opp(q))
+ *     interleaved, pair k at 32 + 64 k + 2 l (+1 for the second), so that a
+ *     node stores a pair with one wide store.
+ * In the blocked layouts the offset of a population from a node's block
+ * position is a compile-time constant. */
 struct Level {
     int nx, ny, nz;
     int pitch;            /* elements per row, a multiple of 32 */
     long long plane;      /* pitch * ny */
     long long qstride;    /* plane * nz */
     int storage;          /* Storage */
-    int blocked;          /* 0: structure-of-arrays, 1: blocks of 32 nodes */
+    int blocked;          /* 0: structure-of-arrays, 1: blocks of rows, 2: blocks of pairs */
     float off[19];        /* FP16/BF16 store f - off[q] (equilibrium at the reference velocity) */
+    float u_ref;          /* that reference velocity (along x) */
 };
 
-/* elements of one 32-node block of the blocked layout */
+/* elements of one 32-node block of the blocked layouts */
 constexpr unsigned BLOCK_ELEMS = 19u * 32u;
 
-/* element offset of population q of node c in either layout */
+/* the pairs of the pair layout: (q, opp(q)) for the first members
+ * 1, 2, 9, 5, 6, 10, 12, 11, 13 */
+__host__ __device__ constexpr int pair_first(int k) {
+    return k == 0 ? 1 : k == 1 ? 2 : k == 2 ? 9 : k == 3 ? 5 : k == 4 ? 6 : k == 5 ? 10 : k == 6 ? 12 : k == 7 ? 11 : 13;
+}
+__host__ __device__ constexpr int pair_of(int q) {
+    return (q == 1 || q == 3) ? 0 : (q == 2 || q == 4) ? 1 : (q == 9 || q == 14) ? 2 : (q == 5 || q == 7) ? 3 :
+           (q == 6 || q == 8) ? 4 : (q == 10 || q == 17) ? 5 : (q == 12 || q == 15) ? 6 : (q == 11 || q == 18) ? 7 : 8;
+}
+__host__ __device__ constexpr int pair_slot(int q) {
+    return (q == 3 || q == 4 || q == 14 || q == 7 || q == 8 || q == 17 || q == 15 || q == 18 || q == 16) ? 1 : 0;
+}
+/* offset of population q from its block's start, lane 0 */
+__host__ __device__ constexpr unsigned pair_qoff(int q) {
+    return q == 0 ? 0u : 32u + 64u * unsigned(pair_of(q)) + unsigned(pair_slot(q));
+}
+
+/* element offset of population q of node c in any layout */
 __host__ __device__ __forceinline__ unsigned pidx(const Level& L, int q, unsigned c) {
-    return L.blocked ? (c >> 5) * BLOCK_ELEMS + (unsigned(q) << 5) + (c & 31u)
-                     : unsigned(q) * unsigned(L.qstride) + c;
+    if (L.blocked == 1) return (c >> 5) * BLOCK_ELEMS + (unsigned(q) << 5) + (c & 31u);
+    if (L.blocked == 2) return (c >> 5) * BLOCK_ELEMS + pair_qoff(q) + (q == 0 ? 1u : 2u) * (c & 31u);
+    return unsigned(q) * unsigned(L.qstride) + c;
 }
 
 struct StepParams {

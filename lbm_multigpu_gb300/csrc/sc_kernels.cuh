@@ -1,9 +1,9 @@
 /*
  * sc_kernels.cuh -- the stream-collide kernels, templated on the storage
- * format S and on the population layout BLK (structure-of-arrays or blocks of
- * 32 nodes, Level::blocked).  lbm_kernels.cu instantiates the
- * structure-of-arrays kernels and lbm_blocked.cu the blocked ones, so the two
- * sets compile in parallel.
+ * format S and on the population layout LAY (Level::blocked: structure of
+ * arrays, or blocks of 32 nodes as rows or pairs).  lbm_kernels.cu
+ * instantiates the structure-of-arrays kernels, lbm_blocked.cu and
+ * lbm_pairs.cu the blocked ones, so that the sets compile in parallel.
  *
  * k_stream_collide is the hot kernel: one thread per lattice node, a warp
  * spans 32 consecutive x of one row, so every population load and store of a
@@ -37,71 +37,255 @@ namespace lbm {
 
 /* ---- storage formats: FP32, FP64, and FP16/BF16 holding f - off with FP32
  * math; off is the equilibrium at the level's reference velocity (Level::off),
- * so the stored numbers are small deviations and keep their relative precision */
+ * so the stored numbers are small deviations and keep their relative precision.
+ * ld / st convert between stored values and populations; ldr / str / st2 move
+ * stored values as they are (st2: two adjacent elements with one store). */
 template <class S> struct Fmt;
 template <> struct Fmt<float> {
     using T = float;
+    static __device__ __forceinline__ float ldr(const float* p) { return __ldg(p); }
+    static __device__ __forceinline__ void str(float* p, float v) { *p = v; }
+    static __device__ __forceinline__ void st2(float* p, float a, float b) {
+        *reinterpret_cast<float2*>(p) = make_float2(a, b);
+    }
     static __device__ __forceinline__ float ld(const float* p, float) { return __ldg(p); }
     static __device__ __forceinline__ void st(float* p, float v, float) { *p = v; }
 };
 template <> struct Fmt<double> {
     using T = double;
+    static __device__ __forceinline__ double ldr(const double* p) { return __ldg(p); }
+    static __device__ __forceinline__ void str(double* p, double v) { *p = v; }
+    static __device__ __forceinline__ void st2(double* p, double a, double b) {
+        *reinterpret_cast<double2*>(p) = make_double2(a, b);
+    }
     static __device__ __forceinline__ double ld(const double* p, float) { return __ldg(p); }
     static __device__ __forceinline__ void st(double* p, double v, float) { *p = v; }
 };
 template <> struct Fmt<__half> {
     using T = float;
-    static __device__ __forceinline__ float ld(const __half* p, float off) { return __half2float(__ldg(p)) + off; }
-    static __device__ __forceinline__ void st(__half* p, float v, float off) { *p = __float2half_rn(v - off); }
+    static __device__ __forceinline__ float ldr(const __half* p) { return __half2float(__ldg(p)); }
+    static __device__ __forceinline__ void str(__half* p, float v) { *p = __float2half_rn(v); }
+    static __device__ __forceinline__ void st2(__half* p, float a, float b) {
+        *reinterpret_cast<__half2*>(p) = __floats2half2_rn(a, b);
+    }
+    static __device__ __forceinline__ float ld(const __half* p, float off) { return ldr(p) + off; }
+    static __device__ __forceinline__ void st(__half* p, float v, float off) { str(p, v - off); }
 };
 template <> struct Fmt<__nv_bfloat16> {
     using T = float;
-    static __device__ __forceinline__ float ld(const __nv_bfloat16* p, float off) {
-        return __bfloat162float(__ldg(p)) + off;
+    static __device__ __forceinline__ float ldr(const __nv_bfloat16* p) { return __bfloat162float(__ldg(p)); }
+    static __device__ __forceinline__ void str(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
+    static __device__ __forceinline__ void st2(__nv_bfloat16* p, float a, float b) {
+        *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(a, b);
     }
-    static __device__ __forceinline__ void st(__nv_bfloat16* p, float v, float off) {
-        *p = __float2bfloat16_rn(v - off);
-    }
+    static __device__ __forceinline__ float ld(const __nv_bfloat16* p, float off) { return ldr(p) + off; }
+    static __device__ __forceinline__ void st(__nv_bfloat16* p, float v, float off) { str(p, v - off); }
 };
 
 /* Element offsets of the pulled populations, split into a z term, a y term,
  * an x term and a population term so that a pull is the sum of four table
- * entries:
- *   structure-of-arrays  q qstride + z plane + y pitch + x
- *   blocked              32 q + 19 (z plane + y pitch) + (x / 32) 608 + x % 32
- * In the blocked layout the population term is a compile-time constant, so
+ * entries (Level describes the layouts):
+ *   0 structure-of-arrays  q qstride + z plane + y pitch + x
+ *   1 blocks of rows       32 q + 19 (z plane + y pitch) + (x / 32) 608 + x % 32
+ *   2 blocks of pairs      pair_qoff(q) + 19 (z plane + y pitch) + (x / 32) 608
+ *                          + (q ? 2 : 1) (x % 32)
+ * In the blocked layouts the population term is a compile-time constant, so
  * the 19 pulls and the 19 stores of a node need no per-population address
- * arithmetic beyond an immediate offset. */
-template <bool BLK> struct Lay;
-template <> struct Lay<false> {
+ * arithmetic beyond an immediate offset.  xt is the x term of population 0,
+ * xtp that of the others. */
+template <int LAY> struct Lay;
+template <> struct Lay<0> {
     static __device__ __forceinline__ unsigned zt(const Level& L, unsigned z) { return z * unsigned(L.plane); }
     static __device__ __forceinline__ unsigned yt(const Level& L, unsigned y) { return y * unsigned(L.pitch); }
     static __device__ __forceinline__ unsigned xt(unsigned x) { return x; }
+    static __device__ __forceinline__ unsigned xtp(unsigned x) { return x; }
     static __device__ __forceinline__ unsigned qt(const Level& L, int q) { return unsigned(q) * unsigned(L.qstride); }
 };
-template <> struct Lay<true> {
+template <> struct Lay<1> {
     static __device__ __forceinline__ unsigned zt(const Level& L, unsigned z) { return z * unsigned(L.plane) * 19u; }
     static __device__ __forceinline__ unsigned yt(const Level& L, unsigned y) { return y * unsigned(L.pitch) * 19u; }
     static __device__ __forceinline__ unsigned xt(unsigned x) { return (x >> 5) * BLOCK_ELEMS + (x & 31u); }
+    static __device__ __forceinline__ unsigned xtp(unsigned x) { return xt(x); }
     static __device__ __forceinline__ unsigned qt(const Level&, int q) { return unsigned(q) << 5; }
 };
+template <> struct Lay<2> {
+    static __device__ __forceinline__ unsigned zt(const Level& L, unsigned z) { return z * unsigned(L.plane) * 19u; }
+    static __device__ __forceinline__ unsigned yt(const Level& L, unsigned y) { return y * unsigned(L.pitch) * 19u; }
+    static __device__ __forceinline__ unsigned xt(unsigned x) { return (x >> 5) * BLOCK_ELEMS + (x & 31u); }
+    static __device__ __forceinline__ unsigned xtp(unsigned x) { return (x >> 5) * BLOCK_ELEMS + 2u * (x & 31u); }
+    static __device__ __forceinline__ unsigned qt(const Level&, int q) { return pair_qoff(q); }
+};
+
+/* the element offsets of one node: its own (population 0 and the others) and
+ * the z, y and x terms of its pull sources (index 1 - c_q) */
+template <int LAY> struct NodeIdx {
+    unsigned zb[3], yb[3], xs[3], xq[3];
+    unsigned self0, selfp;
+    __device__ __forceinline__ NodeIdx(const Level& L, unsigned xm, unsigned x, unsigned xp, unsigned ym, unsigned y,
+                                       unsigned yp, unsigned zm, unsigned z, unsigned zp) {
+        using A = Lay<LAY>;
+        zb[0] = A::zt(L, zm), zb[1] = A::zt(L, z), zb[2] = A::zt(L, zp);
+        yb[0] = A::yt(L, ym), yb[1] = A::yt(L, y), yb[2] = A::yt(L, yp);
+        xs[0] = A::xt(xm), xs[1] = A::xt(x), xs[2] = A::xt(xp);
+        xq[0] = A::xtp(xm), xq[1] = A::xtp(x), xq[2] = A::xtp(xp);
+        self0 = zb[1] + yb[1] + xs[1];
+        selfp = zb[1] + yb[1] + xq[1];
+    }
+    /* population q pulled from x - c_q */
+    __device__ __forceinline__ unsigned pull(const Level& L, int q) const {
+        return Lay<LAY>::qt(L, q) + zb[1 - cz(q)] + yb[1 - cy(q)] + (q == 0 ? xs : xq)[1 - cx(q)];
+    }
+    /* population q of this node */
+    __device__ __forceinline__ unsigned own(const Level& L, int q) const {
+        return Lay<LAY>::qt(L, q) + (q == 0 ? self0 : selfp);
+    }
+    /* population q of the node in the same row / plane at x term index dx,
+     * y term index dy (the neighbours of the inlet / outlet rebuilds) */
+    __device__ __forceinline__ unsigned at(const Level& L, int q, int dx, int dy) const {
+        return Lay<LAY>::qt(L, q) + zb[1] + yb[dy] + (q == 0 ? xs : xq)[dx];
+    }
+};
+
+/* the 19 values g of this node into buffer f: raw stored values (RAW) or
+ * populations with the format's offsets removed; the pair layout writes each
+ * opposite pair with one store */
+template <class S, int LAY, bool RAW>
+__device__ __forceinline__ void store19(const Level& L, S* __restrict__ f, const NodeIdx<LAY>& n,
+                                        const typename Fmt<S>::T g[19]) {
+    using F = Fmt<S>;
+    if constexpr (LAY == 2) {
+        F::str(f + n.own(L, 0), RAW ? g[0] : g[0] - L.off[0]);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const int q1 = pair_first(k), q2 = opp(q1);
+            F::st2(f + n.own(L, q1), RAW ? g[q1] : g[q1] - L.off[q1], RAW ? g[q2] : g[q2] - L.off[q2]);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            if (RAW) F::str(f + n.own(L, q), g[q]);
+            else F::st(f + n.own(L, q), g[q], L.off[q]);
+        }
+    }
+}
 
 /* FEAT: compile-time features, chosen at launch from the configuration and
  * the node types present, so a channel kernel carries no lid code (whose
  * 19-entry temporaries would otherwise set every variant's register count) */
 constexpr int FEAT_HALFWAY = 1, FEAT_LID = 2, FEAT_CLAMP = 4, FEAT_XBC = 8;
-/* the node update of one node (x, y, z) inside the level */
-template <class S, int FEAT, bool BLK>
+/* FP16 / BF16 with LR7's MRT and no body force: the deviation collision
+ * only (other models convert to populations and back) */
+constexpr int FEAT_DEVMRT = 16;
+
+/* nodes per thread along z in k_stream_collide (the x/y index work of a
+ * thread is done once for all of them) */
+#ifndef LBM_SC_ZN
+#define LBM_SC_ZN 1
+#endif
+constexpr int SC_ZN = LBM_SC_ZN;
+/* a straight-line path for warps whose nodes are all plain fluid */
+#ifndef LBM_SC_FAST
+#define LBM_SC_FAST 0
+#endif
+/* FP16 / BF16 nodes collide their stored deviations (no offsets on the way
+ * in and out) */
+#ifndef LBM_SC_DEV
+#define LBM_SC_DEV 1
+#endif
+/* resident blocks per SM the register allocation must allow (0: no bound) */
+#ifndef LBM_SC_MINB
+#define LBM_SC_MINB 0
+#endif
+
+/* the collision, statistics, store and moment export of a non-solid node;
+ * f holds populations, or for DEV their stored deviations */
+template <class S, int LAY, bool DEVMRT>
+__device__ __forceinline__ void sc_collide_store(const Level& L, const StepParams& p, S* __restrict__ fB,
+                                                 float* __restrict__ stats, float* __restrict__ mom_export,
+                                                 const NodeIdx<LAY>& n, typename Fmt<S>::T f[19], unsigned c,
+                                                 const int x, const int y, const int z) {
+    using T = typename Fmt<S>::T;
+    constexpr bool DEV = LBM_SC_DEV && sizeof(S) == 2;
+    const unsigned qs = unsigned(L.qstride);
+    if constexpr (DEV && DEVMRT) {
+        collide_mrt_dev<T>(f, T(p.omega), p.les != 0, T(p.cs), T(L.u_ref));
+    } else {
+        T dp = T(p.dpdy_dev ? *p.dpdy_dev : p.dpdy);
+        if (y > p.dyn_y1) dp = T(0);
+        if (DEV) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) f[q] += L.off[q];
+        }
+        collide<T>(p.model, f, T(p.omega), p.les != 0, T(p.cs), dp);
+        if (DEV) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) f[q] -= L.off[q];
+        }
+    }
+    if (p.stats_on && p.t >= p.start_av) {
+        /* vel_av / vel_fluc (LR7:1018-1058): running mean, then variance */
+        T u = 0, v = 0;
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            const T g = DEV ? f[q] + L.off[q] : f[q];
+            if (cx(q)) u += T(cx(q)) * g;
+            if (cy(q)) v += T(cy(q)) * g;
+        }
+        float* au = stats;
+        float* av = stats + qs;
+        const float w = p.stats_weight;
+        if (p.t < p.start_fluc) {
+            const float nn = float(p.t - p.start_av);
+            au[c] = (au[c] * nn + float(u) * w) / (nn + w);
+            av[c] = (av[c] * nn + float(v) * w) / (nn + w);
+        } else {
+            float* fu = stats + 2 * (size_t)qs;
+            float* fv = stats + 3 * (size_t)qs;
+            const float nn = float(p.t - p.start_fluc);
+            const float du = (float(u) - au[c]) * (float(u) - au[c]);
+            const float dv = (float(v) - av[c]) * (float(v) - av[c]);
+            fu[c] = (fu[c] * nn + du * w) / (nn + w);
+            fv[c] = (fv[c] * nn + dv * w) / (nn + w);
+        }
+    }
+    store19<S, LAY, DEV>(L, fB, n, f);
+}
+
+/* moments for the coarse->fine interpolation (LR7:1590-1605): post-collision
+ * for fluid nodes, the pulled values at bounce-back nodes */
+template <class S>
+__device__ __forceinline__ void sc_export(const Level& L, const StepParams& p, float* __restrict__ mom_export,
+                                          const typename Fmt<S>::T f[19], const int x, const int y, const int z) {
+    constexpr bool DEV = LBM_SC_DEV && sizeof(S) == 2;
+    const int ex = x - p.exp_x0, ey = y - p.exp_y0;
+    if (ex >= 0 && ex < p.exp_nx && ey >= 0 && ey < p.exp_ny) {
+        float ff[19], mom[9];
+#pragma unroll
+        for (int q = 0; q < 19; ++q) ff[q] = DEV ? float(f[q]) + L.off[q] : float(f[q]);
+        physical_moments<float>(ff, mom);
+        const unsigned ne = unsigned(p.exp_nx * p.exp_ny * L.nz);
+        const unsigned ce = (unsigned(z) * p.exp_ny + ey) * p.exp_nx + ex;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) mom_export[i * ne + ce] = mom[i];
+    }
+}
+
+/* the node update of one node (x, y, z) inside the level.
+ * FP16 / BF16 storage (DEV): the node works on the stored deviations
+ * h = f - off and LR7's MRT collides them in that form (collide_mrt_dev),
+ * so no population is offset on its way in or out; boundary
+ * rebuilds, the lid, the alternate boundaries, the other collision models,
+ * the statistics and the moment export see populations f = h + off. */
+template <class S, int FEAT, int LAY>
 __device__ __forceinline__ void sc_node(const Level& L, const StepParams& p, const S* __restrict__ fA,
                                         S* __restrict__ fB, const uint8_t* __restrict__ mask,
                                         float* __restrict__ stats, float* __restrict__ mom_export,
                                         const uint32_t* __restrict__ links, const int x, const int y, const int z) {
     using F = Fmt<S>;
     using T = typename F::T;
-    using A = Lay<BLK>;
+    constexpr bool DEV = LBM_SC_DEV && sizeof(S) == 2;
     /* 32-bit element offsets: a level holds fewer than 2^31 elements per
      * buffer (checked at allocation) */
-    const unsigned qs = unsigned(L.qstride);
     const unsigned plane = unsigned(L.plane), pitch = unsigned(L.pitch);
     const unsigned c = z * plane + y * pitch + x;
     const int mbyte = mask[c];
@@ -119,19 +303,21 @@ __device__ __forceinline__ void sc_node(const Level& L, const StepParams& p, con
     const unsigned yp = (y == L.ny - 1) ? (cl ? y : 0) : y + 1;
     const unsigned zm = (z == 0) ? (cl ? 0 : L.nz - 1) : z - 1;
     const unsigned zp = (z == L.nz - 1) ? (cl ? z : 0) : z + 1;
-    const unsigned zb[3] = {A::zt(L, zm), A::zt(L, z), A::zt(L, zp)};
-    const unsigned yb[3] = {A::yt(L, ym), A::yt(L, y), A::yt(L, yp)};
-    const unsigned xs[3] = {A::xt(xm), A::xt(unsigned(x)), A::xt(xp)};
-    /* element offset of this node's population 0 */
-    const unsigned self = zb[1] + yb[1] + xs[1];
+    const NodeIdx<LAY> n(L, xm, unsigned(x), xp, ym, unsigned(y), yp, zm, unsigned(z), zp);
 
+    /* f: populations, or for DEV their stored deviations */
     T f[19];
 #pragma unroll
-    for (int q = 0; q < 19; ++q) {
-        /* pull: the value arriving from x - c_q */
-        const unsigned src = A::qt(L, q) + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)];
-        f[q] = F::ld(fA + src, L.off[q]);
+    for (int q = 0; q < 19; ++q) f[q] = DEV ? T(F::ldr(fA + n.pull(L, q))) : F::ld(fA + n.pull(L, q), L.off[q]);
+
+#if LBM_SC_FAST
+    const bool plain = type == FLUID && !(HALFWAY && (mbyte & NEAR_SOLID));
+    if (__all_sync(__activemask(), plain)) {
+        sc_collide_store<S, LAY, (FEAT & FEAT_DEVMRT) != 0>(L, p, fB, stats, mom_export, n, f, c, x, y, z);
+        if (p.exp_nx > 0) sc_export<S>(L, p, mom_export, f, x, y, z);
+        return;
     }
+#endif
     if (HALFWAY && (mbyte & NEAR_SOLID)) {
         /* a population that would come from a solid node is the node's own
          * post-collision population of the opposite direction, reflected
@@ -139,24 +325,32 @@ __device__ __forceinline__ void sc_node(const Level& L, const StepParams& p, con
         const uint32_t lk = links[c];
 #pragma unroll
         for (int q = 1; q < 19; ++q)
-            if (lk & (1u << q)) f[q] = F::ld(fA + A::qt(L, opp(q)) + self, L.off[opp(q)]);
+            if (lk & (1u << q))
+                f[q] = DEV ? F::ldr(fA + n.own(L, opp(q))) + (L.off[opp(q)] - L.off[q])
+                           : F::ld(fA + n.own(L, opp(q)), L.off[opp(q)]);
     }
 
     if (type == WALL || type == BODY) {
         /* full-way bounce-back (LR7:1493-1526); the momentum exchange of BODY
          * nodes is summed by k_force_list from the same fA */
+        T g[19];
 #pragma unroll
-        for (int q = 0; q < 19; ++q) F::st(fB + A::qt(L, q) + self, f[opp(q)], L.off[q]);
+        for (int q = 0; q < 19; ++q) g[q] = DEV ? f[opp(q)] + (L.off[opp(q)] - L.off[q]) : f[opp(q)];
+        store19<S, LAY, DEV>(L, fB, n, g);
+        if (p.exp_nx > 0) sc_export<S>(L, p, mom_export, f, x, y, z);
+        return;
     } else {
         if (type >= WEST_INLET && type <= NORTH_OUTLET) {
             /* rebuild from the neighbour's stored post-collision state */
-            unsigned nb;
-            if (type == WEST_INLET) nb = zb[1] + yb[1] + xs[2];
-            else if (type == EAST_OUTLET) nb = zb[1] + yb[1] + xs[0];
-            else if (type == SOUTH_INLET) nb = zb[1] + yb[2] + xs[1];
-            else nb = zb[1] + yb[0] + xs[1];
+            unsigned nb0, nbp;
+            if (type == WEST_INLET) nb0 = n.xs[2], nbp = n.xq[2];
+            else if (type == EAST_OUTLET) nb0 = n.xs[0], nbp = n.xq[0];
+            else nb0 = n.xs[1], nbp = n.xq[1];
+            const unsigned row = n.zb[1] + (type == SOUTH_INLET ? n.yb[2] : type == NORTH_OUTLET ? n.yb[0] : n.yb[1]);
+            nb0 += row;
+            nbp += row;
 #pragma unroll
-            for (int q = 0; q < 19; ++q) f[q] = F::ld(fA + A::qt(L, q) + nb, L.off[q]);
+            for (int q = 0; q < 19; ++q) f[q] = F::ld(fA + Lay<LAY>::qt(L, q) + (q == 0 ? nb0 : nbp), L.off[q]);
             T uin = T(p.u_in);
             if (p.noise_amp != 0.f) {
                 const uint32_t cell = uint32_t((z * L.ny + y) * L.nx + x);
@@ -164,63 +358,32 @@ __device__ __forceinline__ void sc_node(const Level& L, const StepParams& p, con
                 uin = uin + T(p.u_in) * T(p.noise_amp) * (T(2) * T(xi) - T(1));
             }
             extrap<T>(type, f, T(p.rho_out), uin);
-        } else if ((FEAT & FEAT_LID) && type == LID) {
-            lid<T>(f, p.lid_face, T(p.lid_u[0]), T(p.lid_u[1]), T(p.lid_u[2]), p.lid_quirk != 0);
-        } else if ((FEAT & FEAT_XBC) && type >= DIR_WEST) {
-            alt_boundary<T>(type, f, x, y, z, L.nx, L.ny, L.nz, T(p.u_in), p.t);
-        }
-        T dp = T(p.dpdy_dev ? *p.dpdy_dev : p.dpdy);
-        if (y > p.dyn_y1) dp = T(0);
-        collide<T>(p.model, f, T(p.omega), p.les != 0, T(p.cs), dp);
-
-        if (p.stats_on && p.t >= p.start_av) {
-            /* vel_av / vel_fluc (LR7:1018-1058): running mean, then variance */
-            T u = 0, v = 0;
+            if (DEV) {
 #pragma unroll
-            for (int q = 0; q < 19; ++q) {
-                if (cx(q)) u += T(cx(q)) * f[q];
-                if (cy(q)) v += T(cy(q)) * f[q];
+                for (int q = 0; q < 19; ++q) f[q] -= L.off[q];
             }
-            float* au = stats;
-            float* av = stats + qs;
-            const float w = p.stats_weight;
-            if (p.t < p.start_fluc) {
-                const float n = float(p.t - p.start_av);
-                au[c] = (au[c] * n + float(u) * w) / (n + w);
-                av[c] = (av[c] * n + float(v) * w) / (n + w);
-            } else {
-                float* fu = stats + 2 * (size_t)qs;
-                float* fv = stats + 3 * (size_t)qs;
-                const float n = float(p.t - p.start_fluc);
-                const float du = (float(u) - au[c]) * (float(u) - au[c]);
-                const float dv = (float(v) - av[c]) * (float(v) - av[c]);
-                fu[c] = (fu[c] * n + du * w) / (n + w);
-                fv[c] = (fv[c] * n + dv * w) / (n + w);
+        } else if (((FEAT & FEAT_LID) && type == LID) || ((FEAT & FEAT_XBC) && type >= DIR_WEST)) {
+            if (DEV) {
+#pragma unroll
+                for (int q = 0; q < 19; ++q) f[q] += L.off[q];
+            }
+            if ((FEAT & FEAT_LID) && type == LID) {
+                lid<T>(f, p.lid_face, T(p.lid_u[0]), T(p.lid_u[1]), T(p.lid_u[2]), p.lid_quirk != 0);
+            } else if (FEAT & FEAT_XBC) {
+                alt_boundary<T>(type, f, x, y, z, L.nx, L.ny, L.nz, T(p.u_in), p.t);
+            }
+            if (DEV) {
+#pragma unroll
+                for (int q = 0; q < 19; ++q) f[q] -= L.off[q];
             }
         }
-#pragma unroll
-        for (int q = 0; q < 19; ++q) F::st(fB + A::qt(L, q) + self, f[q], L.off[q]);
+        sc_collide_store<S, LAY, (FEAT & FEAT_DEVMRT) != 0>(L, p, fB, stats, mom_export, n, f, c, x, y, z);
     }
-
-    if (p.exp_nx > 0) {
-        /* moments for the coarse->fine interpolation (LR7:1590-1605):
-         * post-collision for fluid nodes, the pulled values at bounce-back nodes */
-        const int ex = x - p.exp_x0, ey = y - p.exp_y0;
-        if (ex >= 0 && ex < p.exp_nx && ey >= 0 && ey < p.exp_ny) {
-            float ff[19], mom[9];
-#pragma unroll
-            for (int q = 0; q < 19; ++q) ff[q] = float(f[q]);
-            physical_moments<float>(ff, mom);
-            const unsigned ne = unsigned(p.exp_nx * p.exp_ny * L.nz);
-            const unsigned ce = (unsigned(z) * p.exp_ny + ey) * p.exp_nx + ex;
-#pragma unroll
-            for (int i = 0; i < 9; ++i) mom_export[i * ne + ce] = mom[i];
-        }
-    }
+    if (p.exp_nx > 0) sc_export<S>(L, p, mom_export, f, x, y, z);
 }
 
-template <class S, int FEAT, bool BLK>
-__global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, const StepParams p,
+template <class S, int FEAT, int LAY>
+__global__ void __launch_bounds__(SC_BX* SC_BY, LBM_SC_MINB) k_stream_collide(const Level L, const StepParams p,
                                                                   const S* __restrict__ fA, S* __restrict__ fB,
                                                                   const uint8_t* __restrict__ mask,
                                                                   float* __restrict__ stats,
@@ -228,9 +391,14 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
                                                                   const uint32_t* __restrict__ links) {
     const int x = blockIdx.x * SC_BX + threadIdx.x;
     const int y = blockIdx.y * SC_BY + threadIdx.y;
-    const int z = blockIdx.z;
     if (x >= L.nx || y >= L.ny) return;
-    sc_node<S, FEAT, BLK>(L, p, fA, fB, mask, stats, mom_export, links, x, y, z);
+    if constexpr (SC_ZN == 1) {
+        sc_node<S, FEAT, LAY>(L, p, fA, fB, mask, stats, mom_export, links, x, y, int(blockIdx.z));
+    } else {
+        const int z0 = blockIdx.z * SC_ZN, z1 = min(z0 + SC_ZN, L.nz);
+#pragma unroll 1
+        for (int z = z0; z < z1; ++z) sc_node<S, FEAT, LAY>(L, p, fA, fB, mask, stats, mom_export, links, x, y, z);
+    }
 }
 
 /* The stream-collide step with the learned subgrid closure in place of the
@@ -242,7 +410,7 @@ __global__ void __launch_bounds__(SC_BX* SC_BY) k_stream_collide(const Level L, 
  * that each block stages the weights and allocates its TMEM once per launch.
  * MRT collision (LR7:583-711) at tau_eff = tau0 + 3 nu_t; FP32 arithmetic. */
 constexpr int MLP_BY = 4; /* tile 32 x 4: one M = 128 MMA per layer */
-template <class S, bool HALFWAY, bool BLK>
+template <class S, bool HALFWAY, int LAY>
 __global__ void __launch_bounds__(SC_BX* MLP_BY, 6) k_stream_collide_mlp(const Level L, const StepParams p,
                                                                       const S* __restrict__ fA, S* __restrict__ fB,
                                                                       const uint8_t* __restrict__ mask,
@@ -251,7 +419,6 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, 6) k_stream_collide_mlp(const L
                                                                       const unsigned char* __restrict__ blob,
                                                                       int* __restrict__ err) {
     using F = Fmt<S>;
-    using A = Lay<BLK>;
     constexpr int ROWS = SC_BX * MLP_BY;
     extern __shared__ unsigned char dsm[];
     sgs::InferSmem<ROWS>& sm = *reinterpret_cast<sgs::InferSmem<ROWS>*>(
@@ -269,35 +436,28 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, 6) k_stream_collide_mlp(const L
         const bool live = x < L.nx && y < L.ny;
         float f[19];
         int type = FLUID;
-        unsigned c = 0, self = 0;
+        unsigned c = 0;
+        const unsigned xm = (x == 0) ? L.nx - 1 : x - 1, xp = (x == L.nx - 1) ? 0 : x + 1;
+        const unsigned ym = (y == 0) ? L.ny - 1 : y - 1, yp = (y == L.ny - 1) ? 0 : y + 1;
+        const unsigned zm = (z == 0) ? L.nz - 1 : z - 1, zp = (z == L.nz - 1) ? 0 : z + 1;
+        const NodeIdx<LAY> n(L, xm, unsigned(x), xp, ym, unsigned(y), yp, zm, unsigned(z), zp);
         if (live) {
             c = unsigned(z) * plane + unsigned(y) * pitch + unsigned(x);
             const int mbyte = mask[c];
             type = mbyte & TYPE_MASK;
-            const unsigned xm = (x == 0) ? L.nx - 1 : x - 1, xp = (x == L.nx - 1) ? 0 : x + 1;
-            const unsigned ym = (y == 0) ? L.ny - 1 : y - 1, yp = (y == L.ny - 1) ? 0 : y + 1;
-            const unsigned zm = (z == 0) ? L.nz - 1 : z - 1, zp = (z == L.nz - 1) ? 0 : z + 1;
-            const unsigned zb[3] = {A::zt(L, zm), A::zt(L, z), A::zt(L, zp)};
-            const unsigned yb[3] = {A::yt(L, ym), A::yt(L, y), A::yt(L, yp)};
-            const unsigned xs[3] = {A::xt(xm), A::xt(unsigned(x)), A::xt(xp)};
-            self = zb[1] + yb[1] + xs[1];
 #pragma unroll
-            for (int q = 0; q < 19; ++q)
-                f[q] = F::ld(fA + A::qt(L, q) + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)], L.off[q]);
+            for (int q = 0; q < 19; ++q) f[q] = F::ld(fA + n.pull(L, q), L.off[q]);
             if (HALFWAY && (mbyte & NEAR_SOLID)) {
                 const uint32_t lk = links[c];
 #pragma unroll
                 for (int q = 1; q < 19; ++q)
-                    if (lk & (1u << q)) f[q] = F::ld(fA + A::qt(L, opp(q)) + self, L.off[opp(q)]);
+                    if (lk & (1u << q)) f[q] = F::ld(fA + n.own(L, opp(q)), L.off[opp(q)]);
             }
             if (type >= WEST_INLET && type <= NORTH_OUTLET) {
-                unsigned nb;
-                if (type == WEST_INLET) nb = zb[1] + yb[1] + xs[2];
-                else if (type == EAST_OUTLET) nb = zb[1] + yb[1] + xs[0];
-                else if (type == SOUTH_INLET) nb = zb[1] + yb[2] + xs[1];
-                else nb = zb[1] + yb[0] + xs[1];
+                const int dx = type == WEST_INLET ? 2 : type == EAST_OUTLET ? 0 : 1;
+                const int dy = type == SOUTH_INLET ? 2 : type == NORTH_OUTLET ? 0 : 1;
 #pragma unroll
-                for (int q = 0; q < 19; ++q) f[q] = F::ld(fA + A::qt(L, q) + nb, L.off[q]);
+                for (int q = 0; q < 19; ++q) f[q] = F::ld(fA + n.at(L, q, dx, dy), L.off[q]);
                 float uin = p.u_in;
                 if (p.noise_amp != 0.f) {
                     const uint32_t cell = uint32_t((z * L.ny + y) * L.nx + x);
@@ -320,8 +480,10 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, 6) k_stream_collide_mlp(const L
         const float nu = sgs::infer_nu<ROWS>(sm, xf, err);
         if (!live) continue;
         if (type == WALL || type == BODY) {
+            float gb[19];
 #pragma unroll
-            for (int q = 0; q < 19; ++q) F::st(fB + A::qt(L, q) + self, f[opp(q)], L.off[q]);
+            for (int q = 0; q < 19; ++q) gb[q] = f[opp(q)];
+            store19<S, LAY, false>(L, fB, n, gb);
             continue;
         }
         collide_mrt<MRT>(f, 1.f / (tau0 + 3.f * nu), false, 0.f, 0.f);
@@ -336,19 +498,18 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, 6) k_stream_collide_mlp(const L
             float* av = stats + qs;
             const float w = p.stats_weight;
             if (p.t < p.start_fluc) {
-                const float n = float(p.t - p.start_av);
-                au[c] = (au[c] * n + u * w) / (n + w);
-                av[c] = (av[c] * n + v * w) / (n + w);
+                const float nn = float(p.t - p.start_av);
+                au[c] = (au[c] * nn + u * w) / (nn + w);
+                av[c] = (av[c] * nn + v * w) / (nn + w);
             } else {
                 float* fu = stats + 2 * (size_t)qs;
                 float* fv = stats + 3 * (size_t)qs;
-                const float n = float(p.t - p.start_fluc);
-                fu[c] = (fu[c] * n + (u - au[c]) * (u - au[c]) * w) / (n + w);
-                fv[c] = (fv[c] * n + (v - av[c]) * (v - av[c]) * w) / (n + w);
+                const float nn = float(p.t - p.start_fluc);
+                fu[c] = (fu[c] * nn + (u - au[c]) * (u - au[c]) * w) / (nn + w);
+                fv[c] = (fv[c] * nn + (v - av[c]) * (v - av[c]) * w) / (nn + w);
             }
         }
-#pragma unroll
-        for (int q = 0; q < 19; ++q) F::st(fB + A::qt(L, q) + self, f[q], L.off[q]);
+        store19<S, LAY, false>(L, fB, n, f);
     }
     sgs::infer_teardown<ROWS>(sm);
 #endif
@@ -364,18 +525,20 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, 6) k_stream_collide_mlp(const L
 
 /* the stream-collide launch of one layout; FP64 storage only in the
  * structure-of-arrays layout */
-template <bool BLK>
+template <int LAY>
 inline cudaError_t launch_sc_layout(const Level& L, const StepParams& p, const void* fA, void* fB,
                                     const uint8_t* mask, float* stats, float* mom_export, cudaStream_t s,
                                     const uint32_t* links) {
-    const dim3 block(SC_BX, SC_BY), grid = sc_grid(L);
+    const dim3 block(SC_BX, SC_BY), grid(L.pitch / SC_BX, (L.ny + SC_BY - 1) / SC_BY, (L.nz + SC_ZN - 1) / SC_ZN);
+    const bool reduced = L.storage == STORE_F16 || L.storage == STORE_BF16;
     const int feat = (p.halfway ? FEAT_HALFWAY : 0) | (p.has_lid ? FEAT_LID : 0) | (p.pull_clamp ? FEAT_CLAMP : 0) |
-                     (p.has_xbc ? FEAT_XBC : 0);
+                     (p.has_xbc ? FEAT_XBC : 0) |
+                     (reduced && p.model == MRT && p.dpdy == 0.f && !p.dpdy_dev ? FEAT_DEVMRT : 0);
 #define LBM_SC_CALL(FT)                                                                                          \
-    (k_stream_collide<S, FT, BLK><<<grid, block, 0, s>>>(L, p, (const S*)fA, (S*)fB, mask, stats, mom_export, \
+    (k_stream_collide<S, FT, LAY><<<grid, block, 0, s>>>(L, p, (const S*)fA, (S*)fB, mask, stats, mom_export, \
                                                           links))
 #define LBM_SC(FT)                                                                   \
-    if constexpr (BLK) {                                                             \
+    if constexpr (LAY != 0) {                                                        \
         LBM_DISPATCH3(L.storage, LBM_SC_CALL(FT))                                    \
     } else {                                                                         \
         if (L.storage == STORE_F64) {                                                \
@@ -384,6 +547,14 @@ inline cudaError_t launch_sc_layout(const Level& L, const StepParams& p, const v
         } else {                                                                     \
             LBM_DISPATCH3(L.storage, LBM_SC_CALL(FT))                                \
         }                                                                            \
+    }
+#define LBM_SC_DEV(FT)                                                               \
+    if (L.storage == STORE_F16) {                                                    \
+        using S = __half;                                                            \
+        LBM_SC_CALL(FT);                                                             \
+    } else {                                                                         \
+        using S = __nv_bfloat16;                                                     \
+        LBM_SC_CALL(FT);                                                             \
     }
     switch (feat) {
         case 0: LBM_SC(0); break;
@@ -403,32 +574,50 @@ inline cudaError_t launch_sc_layout(const Level& L, const StepParams& p, const v
         case 13: LBM_SC(13); break;
         case 14: LBM_SC(14); break;
         case 15: LBM_SC(15); break;
+        /* FP16 / BF16 with the deviation MRT collision */
+        case 16: LBM_SC_DEV(16); break;
+        case 17: LBM_SC_DEV(17); break;
+        case 18: LBM_SC_DEV(18); break;
+        case 19: LBM_SC_DEV(19); break;
+        case 20: LBM_SC_DEV(20); break;
+        case 21: LBM_SC_DEV(21); break;
+        case 22: LBM_SC_DEV(22); break;
+        case 23: LBM_SC_DEV(23); break;
+        case 24: LBM_SC_DEV(24); break;
+        case 25: LBM_SC_DEV(25); break;
+        case 26: LBM_SC_DEV(26); break;
+        case 27: LBM_SC_DEV(27); break;
+        case 28: LBM_SC_DEV(28); break;
+        case 29: LBM_SC_DEV(29); break;
+        case 30: LBM_SC_DEV(30); break;
+        case 31: LBM_SC_DEV(31); break;
         default: return cudaErrorInvalidValue;
     }
 #undef LBM_SC
+#undef LBM_SC_DEV
 #undef LBM_SC_CALL
     return cudaGetLastError();
 }
 
-template <class S, bool HW, bool BLK>
+template <class S, bool HW, int LAY>
 static cudaError_t sc_mlp_t(const Level& L, const StepParams& p, const void* fA, void* fB, const uint8_t* mask,
                             float* stats, const uint32_t* links, const void* blob, int* err, cudaStream_t s) {
     const size_t smem = sgs::infer_dyn_smem<SC_BX * MLP_BY>();
     static cudaError_t attr = cudaErrorNotReady;
     static int grid = 0;
     if (attr == cudaErrorNotReady) {
-        attr = cudaFuncSetAttribute(k_stream_collide_mlp<S, HW, BLK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        attr = cudaFuncSetAttribute(k_stream_collide_mlp<S, HW, LAY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     int(smem));
         /* all of the unified L1 / shared array as shared memory, so that the
          * register limit (6 blocks of 128 threads at 80 registers) decides */
         if (attr == cudaSuccess)
-            attr = cudaFuncSetAttribute(k_stream_collide_mlp<S, HW, BLK>,
+            attr = cudaFuncSetAttribute(k_stream_collide_mlp<S, HW, LAY>,
                                         cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         /* resident blocks per SM from the kernel's own limits: registers,
          * shared memory, threads, and TMEM (64 columns of 512 per block) */
         cudaFuncAttributes fa{};
         int dev = 0, sms = 0, regs_sm = 0, smem_sm = 0;
-        if (attr == cudaSuccess) attr = cudaFuncGetAttributes(&fa, k_stream_collide_mlp<S, HW, BLK>);
+        if (attr == cudaSuccess) attr = cudaFuncGetAttributes(&fa, k_stream_collide_mlp<S, HW, LAY>);
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
@@ -444,26 +633,26 @@ static cudaError_t sc_mlp_t(const Level& L, const StepParams& p, const void* fA,
     }
     if (attr != cudaSuccess) return attr;
     const int ntiles = (L.pitch / SC_BX) * ((L.ny + MLP_BY - 1) / MLP_BY) * L.nz;
-    k_stream_collide_mlp<S, HW, BLK><<<grid < ntiles ? grid : ntiles, dim3(SC_BX, MLP_BY), smem, s>>>(
+    k_stream_collide_mlp<S, HW, LAY><<<grid < ntiles ? grid : ntiles, dim3(SC_BX, MLP_BY), smem, s>>>(
         L, p, (const S*)fA, (S*)fB, mask, stats, links, (const unsigned char*)blob, err);
     return cudaGetLastError();
 }
 
 /* the closure's stream-collide launch of one layout (FP32, FP16, BF16) */
-template <bool BLK>
+template <int LAY>
 inline cudaError_t launch_sc_mlp_layout(const Level& L, const StepParams& p, const void* fA, void* fB,
                                         const uint8_t* mask, float* stats, const uint32_t* links, const void* blob,
                                         int* err, cudaStream_t s) {
     switch (L.storage) {
         case STORE_F32:
-            return p.halfway ? sc_mlp_t<float, true, BLK>(L, p, fA, fB, mask, stats, links, blob, err, s)
-                             : sc_mlp_t<float, false, BLK>(L, p, fA, fB, mask, stats, links, blob, err, s);
+            return p.halfway ? sc_mlp_t<float, true, LAY>(L, p, fA, fB, mask, stats, links, blob, err, s)
+                             : sc_mlp_t<float, false, LAY>(L, p, fA, fB, mask, stats, links, blob, err, s);
         case STORE_F16:
-            return p.halfway ? sc_mlp_t<__half, true, BLK>(L, p, fA, fB, mask, stats, links, blob, err, s)
-                             : sc_mlp_t<__half, false, BLK>(L, p, fA, fB, mask, stats, links, blob, err, s);
+            return p.halfway ? sc_mlp_t<__half, true, LAY>(L, p, fA, fB, mask, stats, links, blob, err, s)
+                             : sc_mlp_t<__half, false, LAY>(L, p, fA, fB, mask, stats, links, blob, err, s);
         case STORE_BF16:
-            return p.halfway ? sc_mlp_t<__nv_bfloat16, true, BLK>(L, p, fA, fB, mask, stats, links, blob, err, s)
-                             : sc_mlp_t<__nv_bfloat16, false, BLK>(L, p, fA, fB, mask, stats, links, blob, err, s);
+            return p.halfway ? sc_mlp_t<__nv_bfloat16, true, LAY>(L, p, fA, fB, mask, stats, links, blob, err, s)
+                             : sc_mlp_t<__nv_bfloat16, false, LAY>(L, p, fA, fB, mask, stats, links, blob, err, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -474,5 +663,10 @@ cudaError_t launch_sc_blocked(const Level& L, const StepParams& p, const void* f
 cudaError_t launch_sc_mlp_blocked(const Level& L, const StepParams& p, const void* fA, void* fB,
                                   const uint8_t* mask, float* stats, const uint32_t* links, const void* blob, int* err,
                                   cudaStream_t s);
+cudaError_t launch_sc_pairs(const Level& L, const StepParams& p, const void* fA, void* fB, const uint8_t* mask,
+                            float* stats, float* mom_export, cudaStream_t s, const uint32_t* links);
+cudaError_t launch_sc_mlp_pairs(const Level& L, const StepParams& p, const void* fA, void* fB,
+                                const uint8_t* mask, float* stats, const uint32_t* links, const void* blob, int* err,
+                                cudaStream_t s);
 
 }  // namespace lbm

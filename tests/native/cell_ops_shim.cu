@@ -32,6 +32,12 @@ void cell_strain_rate(const float* mom, float* s, int n) {
 void cell_invert_scaled(const float* mom, float sf, float* f, int n) {
     for (int i = 0; i < n; ++i) invert_scaled<float>(mom + 9L * i, sf, f + 19L * i);
 }
+void cell_collide_mrt_dev_d(int les, double omega, double cs, double u, double* h, int n) {
+    for (int i = 0; i < n; ++i) collide_mrt_dev<double>(h + 19L * i, omega, les != 0, cs, u);
+}
+void cell_collide_mrt_dev(int les, float omega, float cs, float u, float* h, int n) {
+    for (int i = 0; i < n; ++i) collide_mrt_dev<float>(h + 19L * i, omega, les != 0, cs, u);
+}
 float cell_philox_uniform(uint32_t seed, uint32_t cell, uint32_t step) { return philox_uniform(seed, cell, step); }
 void cell_alt_boundary(int type, float* f, int n, const int* yz, int ny, int nz, float u, int t) {
     for (int i = 0; i < n; ++i) alt_boundary<float>(type, f + 19L * i, 0, yz[2 * i], yz[2 * i + 1], 0, ny, nz, u, t);
