@@ -39,7 +39,7 @@ def nvcc() -> str:
 
 
 def sources() -> list[Path]:
-    return [CSRC / "lbm_kernels.cu", CSRC / "lbm_blocked.cu", CSRC / "lbm_pairs.cu", CSRC / "lbm_host.cpp", CSRC / "lbm_noalloc.cu", CSRC / "sgs_mlp.cu",
+    return [CSRC / "lbm_kernels.cu", CSRC / "lbm_blocked.cu", CSRC / "lbm_host.cpp", CSRC / "lbm_noalloc.cu", CSRC / "sgs_mlp.cu",
             CSRC / "lbm_sgs.cpp", CSRC / "ensemble.cu", CSRC / "lbm_ensemble.cpp", CSRC / "lbm_post.cpp"]
 
 

@@ -215,6 +215,35 @@ __host__ __device__ __forceinline__ void collide_mrt(T f[19], T omega, bool les,
     }
 }
 
+/* the square root of a non-negative x for the deviation collision: on the
+ * device x rsqrt(x + 1e-30), which is 0 at 0 without a branch */
+template <class T> __host__ __device__ __forceinline__ T dsqrt(T x) {
+#ifdef __CUDA_ARCH__
+    if constexpr (sizeof(T) == 4) return x * rsqrtf(x + 1e-30f);
+#endif
+    return sqrt(x);
+}
+
+/* the deviation collision's opposite-pair sums and final rebuild in packed
+ * FP32 pairs (sm_100 and later: one instruction for two values) */
+#ifndef LBM_DEV_F2
+#define LBM_DEV_F2 1
+#endif
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000 && LBM_DEV_F2
+#define LBM_F2_ON 1
+#else
+#define LBM_F2_ON 0
+#endif
+#if LBM_F2_ON
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) {
+    unsigned long long ra = *reinterpret_cast<unsigned long long*>(&a);
+    unsigned long long rb = *reinterpret_cast<unsigned long long*>(&b), rd;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+    return *reinterpret_cast<float2*>(&rd);
+}
+#endif
+
 /* LR7's MRT collision with Smagorinsky (LR7:583-711) in projected form, on
  * the deviations h = f - feq(1, (U, 0, 0)) of the populations from the
  * model's own equilibrium at density 1 and the reference velocity U along x
@@ -232,8 +261,24 @@ __host__ __device__ __forceinline__ void collide_mrt(T f[19], T omega, bool les,
  * Equilibrium moments (incompressible, rho0 = 1): meq1 = -11 rho + 19 j^2,
  * meq2 = 7.53968254 j^2 (LR7's sign), meq4,6,8 = -2/3 j, meq9 = 2 jx^2 -
  * jy^2 - jz^2, meq11 = jy^2 - jz^2, meq13,14,15 = jx jy, jy jz, jx jz,
- * meq10 = meq12 = meq16,17,18 = 0. */
-template <class T> __host__ __device__ __forceinline__ void collide_mrt_dev(T f[19], T omega, bool les, T cs, T U) {
+ * meq10 = meq12 = meq16,17,18 = 0.
+ * tau0 = 1 / omega and smag_k = 18 sqrt(2) CS are the Smagorinsky constants
+ * (LR7:683-685), worked out once per launch. */
+template <class T>
+__host__ __device__ __forceinline__ void collide_mrt_dev(T f[19], T omega, bool les, T tau0, T smag_k, T U) {
+#if LBM_F2_ON
+    /* even and odd parts of the opposite pairs, two pairs per instruction */
+    const float2 S1 = padd(make_float2(f[1], f[2]), make_float2(f[3], f[4]));
+    const float2 D1 = psub(make_float2(f[1], f[2]), make_float2(f[3], f[4]));
+    const float2 S2 = padd(make_float2(f[9], f[5]), make_float2(f[14], f[7]));
+    const float2 D2 = psub(make_float2(f[9], f[5]), make_float2(f[14], f[7]));
+    const float2 S3 = padd(make_float2(f[6], f[10]), make_float2(f[8], f[17]));
+    const float2 D3 = psub(make_float2(f[6], f[10]), make_float2(f[8], f[17]));
+    const float2 S4 = padd(make_float2(f[12], f[11]), make_float2(f[15], f[18]));
+    const float2 D4 = psub(make_float2(f[12], f[11]), make_float2(f[15], f[18]));
+    const T sx = S1.x, sy = S1.y, dx = D1.x, dy = D1.y, sz = S2.x, a5 = S2.y, dz = D2.x, b5 = D2.y;
+    const T a6 = S3.x, a10 = S3.y, b6 = D3.x, b10 = D3.y, a12 = S4.x, a11 = S4.y, b12 = D4.x, b11 = D4.y;
+#else
     const T sx = f[1] + f[3], dx = f[1] - f[3];
     const T sy = f[2] + f[4], dy = f[2] - f[4];
     const T sz = f[9] + f[14], dz = f[9] - f[14];
@@ -242,6 +287,7 @@ template <class T> __host__ __device__ __forceinline__ void collide_mrt_dev(T f[
     const T a10 = f[10] + f[17], b10 = f[10] - f[17];
     const T a12 = f[12] + f[15], b12 = f[12] - f[15];
     const T a11 = f[11] + f[18], b11 = f[11] - f[18];
+#endif
     const T a13 = f[13] + f[16], b13 = f[13] - f[16];
     const T axy = a5 + a6, axz = a10 + a12, ayz = a11 + a13;
     const T sdi = axy + axz + ayz;
@@ -267,8 +313,8 @@ template <class T> __host__ __device__ __forceinline__ void collide_mrt_dev(T f[
         const T tr = n1 * T(1.0 / 19.0);
         const T pxx = n1 * T(1.0 / 57.0) + n9 * T(1.0 / 3.0);
         const T pyy = T(0.5) * (tr - pxx + n11), pzz = T(0.5) * (tr - pxx - n11);
-        const T qn = lsqrt(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (n13 * n13 + n14 * n14 + n15 * n15));
-        omega = smag_omega(omega, cs, qn);
+        const T qn = dsqrt(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (n13 * n13 + n14 * n14 + n15 * n15));
+        omega = lrcp(T(0.5) * tau0 + T(0.5) * dsqrt(tau0 * tau0 + smag_k * qn));
     }
     const T c1 = T(1) - omega;
     /* post-collision stresses less their value at (1, U), over the row norms */
@@ -284,47 +330,55 @@ template <class T> __host__ __device__ __forceinline__ void collide_mrt_dev(T f[
     const T ox = jx * T(1.0 / 6.0), oy = jy * T(1.0 / 6.0), oz = jz * T(1.0 / 6.0);
     const T hx = jx * T(1.0 / 12.0), hy = jy * T(1.0 / 12.0), hz = jz * T(1.0 / 12.0);
     f[0] = A0;
+    const T ayz9 = Aa - t9, d9 = Ad + t9;
+    const T ex = Aa + T(2) * t9, ey = ayz9 + t11, ez = ayz9 - t11;
+    const T bxy = d9 + t11, bxz = d9 - t11, byz = Ad - T(2) * t9;
+    const T e5 = bxy + t13, e6 = bxy - t13, o5 = hx + hy, o6 = hy - hx;      /* xy: (5,7), (6,8) */
+    const T e10 = bxz + t15, e12 = bxz - t15, o10 = hx + hz, o12 = hz - hx;  /* xz: (10,17), (12,15) */
+    const T e11 = byz + t14, e13 = byz - t14, o11 = hy + hz, o13 = hz - hy;  /* yz: (11,18), (13,16) */
+#if LBM_F2_ON
     {
-        const T e = Aa + T(2) * t9;
-        f[1] = e + ox;
-        f[3] = e - ox;
+        const float2 E = make_float2(ex, ey), O = make_float2(ox, oy);
+        const float2 P = padd(E, O), M = psub(E, O);
+        f[1] = P.x, f[2] = P.y, f[3] = M.x, f[4] = M.y;
     }
-    const T ayz9 = Aa - t9;
+    f[9] = ez + oz;
+    f[14] = ez - oz;
     {
-        const T e = ayz9 + t11;
-        f[2] = e + oy;
-        f[4] = e - oy;
+        const float2 E = make_float2(e5, e6), O = make_float2(o5, o6);
+        const float2 P = padd(E, O), M = psub(E, O);
+        f[5] = P.x, f[6] = P.y, f[7] = M.x, f[8] = M.y;
     }
     {
-        const T e = ayz9 - t11;
-        f[9] = e + oz;
-        f[14] = e - oz;
+        const float2 E = make_float2(e10, e12), O = make_float2(o10, o12);
+        const float2 P = padd(E, O), M = psub(E, O);
+        f[10] = P.x, f[12] = P.y, f[17] = M.x, f[15] = M.y;
     }
-    const T d9 = Ad + t9;
-    {   /* xy: (5,7) c = (1,1,0), (6,8) c = (-1,1,0) */
-        const T b = d9 + t11;
-        const T e5 = b + t13, o5 = hx + hy, e6 = b - t13, o6 = hy - hx;
-        f[5] = e5 + o5;
-        f[7] = e5 - o5;
-        f[6] = e6 + o6;
-        f[8] = e6 - o6;
+    {
+        const float2 E = make_float2(e11, e13), O = make_float2(o11, o13);
+        const float2 P = padd(E, O), M = psub(E, O);
+        f[11] = P.x, f[13] = P.y, f[18] = M.x, f[16] = M.y;
     }
-    {   /* xz: (10,17) c = (1,0,1), (12,15) c = (-1,0,1) */
-        const T b = d9 - t11;
-        const T e10 = b + t15, o10 = hx + hz, e12 = b - t15, o12 = hz - hx;
-        f[10] = e10 + o10;
-        f[17] = e10 - o10;
-        f[12] = e12 + o12;
-        f[15] = e12 - o12;
-    }
-    {   /* yz: (11,18) c = (0,1,1), (13,16) c = (0,-1,1) */
-        const T b = Ad - T(2) * t9;
-        const T e11 = b + t14, o11 = hy + hz, e13 = b - t14, o13 = hz - hy;
-        f[11] = e11 + o11;
-        f[18] = e11 - o11;
-        f[13] = e13 + o13;
-        f[16] = e13 - o13;
-    }
+#else
+    f[1] = ex + ox;
+    f[3] = ex - ox;
+    f[2] = ey + oy;
+    f[4] = ey - oy;
+    f[9] = ez + oz;
+    f[14] = ez - oz;
+    f[5] = e5 + o5;
+    f[7] = e5 - o5;
+    f[6] = e6 + o6;
+    f[8] = e6 - o6;
+    f[10] = e10 + o10;
+    f[17] = e10 - o10;
+    f[12] = e12 + o12;
+    f[15] = e12 - o12;
+    f[11] = e11 + o11;
+    f[18] = e11 - o11;
+    f[13] = e13 + o13;
+    f[16] = e13 - o13;
+#endif
 }
 
 /* BGK with the incompressible equilibrium w (rho + 3 c.j + 4.5 (c.j)^2 - 1.5 j^2)

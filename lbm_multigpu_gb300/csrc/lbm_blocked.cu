@@ -1,8 +1,8 @@
 /*
  * lbm_blocked.cu -- the stream-collide kernels (sc_kernels.cuh) in the blocked
  * population layout (Level::blocked: the 19 populations of 32 x-consecutive
- * nodes stored together, population q at the fixed offset 32 q), for FP32,
- * FP16 and BF16 storage.  A separate translation unit, so that it compiles in
+ * nodes stored together, each opposite pair interleaved), for FP32, FP16 and
+ * BF16 storage.  A separate translation unit, so that it compiles in
  * parallel with the structure-of-arrays instances in lbm_kernels.cu.
  */
 #include "sc_kernels.cuh"

@@ -78,9 +78,9 @@ struct Config {
     /* extension keys (not in the reference record) */
     std::string geometry = "channel_square";
     std::string precision = "fp32";
-    /* "LAYOUT: soa | blocked | auto": population layout in HBM; auto keeps
-     * FP32 and FP64 in the reference's structure-of-arrays layout and stores
-     * FP16 / BF16 in blocks of 32 nodes */
+    /* "LAYOUT: soa | blocked | auto": population layout in HBM; auto stores
+     * FP32, FP16 and BF16 in blocks of 32 nodes and keeps FP64 (the accuracy
+     * twin) in the reference's structure-of-arrays layout */
     std::string pop_layout = "auto";
     float tau = 0;                  /* > 0: tau0 given directly instead of RE */
     float lid_u[3] = {0, 0, 0};
@@ -220,7 +220,7 @@ int parse_inputs(const char* text, Config& c) {
         else if (key == "GEOMETRY") c.geometry = val;
         else if (key == "PRECISION") c.precision = val;
         else if (key == "LAYOUT") {
-            ok = (val == "soa" || val == "blocked" || val == "pairs" || val == "auto");
+            ok = (val == "soa" || val == "blocked" || val == "auto");
             c.pop_layout = val;
         }
         else if (key == "TAU") F(c.tau);
@@ -1082,8 +1082,7 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
     if (model < 0) return fail(LBM_ERR_CONFIG, "MODEL '%s' is not one of MRT, MRT_DI3, BGK, MRT_CPU3D", c.model.c_str());
     const int storage = storage_id(c.precision);
     if (storage < 0) return fail(LBM_ERR_CONFIG, "PRECISION '%s' is not one of fp32, fp16, bf16, fp64", c.precision.c_str());
-    const int blocked = c.pop_layout == "blocked" ? 1 : c.pop_layout == "pairs" ? 2
-                        : (c.pop_layout == "auto" && (storage == STORE_F16 || storage == STORE_BF16)) ? 1 : 0;
+    const int blocked = c.pop_layout == "blocked" || (c.pop_layout == "auto" && storage != STORE_F64) ? 1 : 0;
     if (blocked && storage == STORE_F64) return fail(LBM_ERR_CONFIG, "LAYOUT blocked is for FP32, FP16 and BF16 storage");
     static const char* geoms[] = {"channel_square", "channel_circle", "channel", "cavity", "periodic", "dyninlet", "duct"};
     if (std::find(std::begin(geoms), std::end(geoms), c.geometry) == std::end(geoms))
@@ -1478,7 +1477,7 @@ int lbm_save_state(lbm_handle* h, const char* path) {
     return LBM_OK;
 }
 
-static const char* layout_name(int b) { return b == 0 ? "soa" : b == 1 ? "blocked" : b == 2 ? "pairs" : "unknown"; }
+static const char* layout_name(int b) { return b == 0 ? "soa" : b == 1 ? "blocked" : "unknown"; }
 
 static int read_checkpoint_record(std::istream& in, std::string& rec) {
     char magic[sizeof CKPT_MAGIC];
@@ -1513,7 +1512,7 @@ int lbm_restore_state(lbm_handle* h, const char* path) {
             hdr[4] != h->storage + 256 * L.blocked)
             return fail(LBM_ERR_CONFIG, "checkpoint: level %d is %dx%dx%d (pitch %d, storage %d, layout %s), the "
                         "handle's %dx%dx%d (storage %d, layout %s)", l, hdr[0], hdr[1], hdr[2], hdr[3], hdr[4] & 255,
-                        hdr[4] >= 256 ? "blocked" : "soa", L.nx, L.ny, L.nz, h->storage, L.blocked ? "blocked" : "soa");
+                        layout_name(hdr[4] >> 8), L.nx, L.ny, L.nz, h->storage, layout_name(L.blocked));
         std::vector<char> raw(size_t(L.qstride) * 19 * storage_bytes(h->storage));
         if (!in.read(raw.data(), std::streamsize(raw.size()))) return fail(LBM_ERR_PARSE, "checkpoint: truncated level");
         for (int b = 0; b < 2; ++b) CUDA_TRY(cudaMemcpy(s.f[b], raw.data(), raw.size(), cudaMemcpyHostToDevice));

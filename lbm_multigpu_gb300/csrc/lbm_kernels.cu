@@ -518,9 +518,11 @@ __global__ void k_interp_fc(const RefineParams r, const Level C, const Level F, 
 cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const void* fA, void* fB, const uint8_t* mask,
                                   float* stats, float* mom_export, cudaStream_t s, const uint32_t* links) {
     if (p.halfway && !links) return cudaErrorInvalidValue;
-    if (L.blocked == 1) return launch_sc_blocked(L, p, fA, fB, mask, stats, mom_export, s, links);
-    if (L.blocked == 2) return launch_sc_pairs(L, p, fA, fB, mask, stats, mom_export, s, links);
-    return launch_sc_layout<0>(L, p, fA, fB, mask, stats, mom_export, s, links);
+    StepParams q = p;
+    q.tau0 = 1.f / p.omega;
+    q.smag_k = 18.f * 1.41421356f * p.cs;
+    if (L.blocked) return launch_sc_blocked(L, q, fA, fB, mask, stats, mom_export, s, links);
+    return launch_sc_layout<0>(L, q, fA, fB, mask, stats, mom_export, s, links);
 }
 
 cudaError_t launch_stream_collide_mlp(const Level& L, const StepParams& p, const void* fA, void* fB,
@@ -528,8 +530,7 @@ cudaError_t launch_stream_collide_mlp(const Level& L, const StepParams& p, const
                                       int* err, cudaStream_t s) {
     if ((p.halfway && !links) || !blob || !err || p.has_lid || p.has_xbc || p.pull_clamp || p.exp_nx > 0)
         return cudaErrorInvalidValue;
-    if (L.blocked == 1) return launch_sc_mlp_blocked(L, p, fA, fB, mask, stats, links, blob, err, s);
-    if (L.blocked == 2) return launch_sc_mlp_pairs(L, p, fA, fB, mask, stats, links, blob, err, s);
+    if (L.blocked) return launch_sc_mlp_blocked(L, p, fA, fB, mask, stats, links, blob, err, s);
     return launch_sc_mlp_layout<0>(L, p, fA, fB, mask, stats, links, blob, err, s);
 }
 

@@ -50,30 +50,28 @@ enum Storage : int { STORE_F32 = 0, STORE_F16 = 1, STORE_BF16 = 2, STORE_F64 = 3
 /* One grid level in HBM.  Nodes are numbered c = z plane + y pitch + x with
  * a padded x pitch (a multiple of 32).  Populations are stored either
  *   0, structure-of-arrays: f[q][z][y][x], q-planes qstride elements apart
- *     (the reference's layout, LR7:210-216), or in blocks of the 32 nodes
- *     x = 32 b .. 32 b + 31 of a row, each block 19 x 32 elements holding
- *     their 19 populations together:
- *   1, rows: population q of lane l at 32 q + l;
- *   2, pairs: population 0 at l, then the nine opposite pairs (q, opp(q))
- *     interleaved, pair k at 32 + 64 k + 2 l (+1 for the second), so that a
- *     node stores a pair with one wide store.
- * In the blocked layouts the offset of a population from a node's block
- * position is a compile-time constant. */
+ *     (the reference's layout, LR7:210-216), or
+ *   1, blocked: the 32 nodes x = 32 b .. 32 b + 31 of a row keep their 19
+ *     populations together in 19 x 32 elements, population 0 of lane l at
+ *     l, then the nine opposite pairs (q, opp(q)) interleaved, pair k at
+ *     32 + 64 k + 2 l (+1 for the second member), so that a node stores a
+ *     pair with one wide store and the offset of a population from the
+ *     node's block position is a compile-time constant. */
 struct Level {
     int nx, ny, nz;
     int pitch;            /* elements per row, a multiple of 32 */
     long long plane;      /* pitch * ny */
     long long qstride;    /* plane * nz */
     int storage;          /* Storage */
-    int blocked;          /* 0: structure-of-arrays, 1: blocks of rows, 2: blocks of pairs */
+    int blocked;          /* 0: structure-of-arrays, 1: blocked */
     float off[19];        /* FP16/BF16 store f - off[q] (equilibrium at the reference velocity) */
     float u_ref;          /* that reference velocity (along x) */
 };
 
-/* elements of one 32-node block of the blocked layouts */
+/* elements of one 32-node block of the blocked layout */
 constexpr unsigned BLOCK_ELEMS = 19u * 32u;
 
-/* the pairs of the pair layout: (q, opp(q)) for the first members
+/* the pairs of the blocked layout: (q, opp(q)) for the first members
  * 1, 2, 9, 5, 6, 10, 12, 11, 13 */
 __host__ __device__ constexpr int pair_first(int k) {
     return k == 0 ? 1 : k == 1 ? 2 : k == 2 ? 9 : k == 3 ? 5 : k == 4 ? 6 : k == 5 ? 10 : k == 6 ? 12 : k == 7 ? 11 : 13;
@@ -90,10 +88,9 @@ __host__ __device__ constexpr unsigned pair_qoff(int q) {
     return q == 0 ? 0u : 32u + 64u * unsigned(pair_of(q)) + unsigned(pair_slot(q));
 }
 
-/* element offset of population q of node c in any layout */
+/* element offset of population q of node c in either layout */
 __host__ __device__ __forceinline__ unsigned pidx(const Level& L, int q, unsigned c) {
-    if (L.blocked == 1) return (c >> 5) * BLOCK_ELEMS + (unsigned(q) << 5) + (c & 31u);
-    if (L.blocked == 2) return (c >> 5) * BLOCK_ELEMS + pair_qoff(q) + (q == 0 ? 1u : 2u) * (c & 31u);
+    if (L.blocked) return (c >> 5) * BLOCK_ELEMS + pair_qoff(q) + (q == 0 ? 1u : 2u) * (c & 31u);
     return unsigned(q) * unsigned(L.qstride) + c;
 }
 
@@ -101,6 +98,9 @@ struct StepParams {
     int model;
     int les;
     float omega, cs, dpdy;
+    /* derived by launch_stream_collide: 1 / omega and 18 sqrt(2) cs, the
+     * constants of the Smagorinsky relaxation (LR7:683-685) */
+    float tau0, smag_k;
     /* dynamic inlet (DI3): when dpdy_dev is set the body force is read from
      * the device (the P-control updates it there); nodes with y > dyn_y1 get
      * no body force (DI3:1358) */

@@ -1,9 +1,9 @@
 /*
  * sc_kernels.cuh -- the stream-collide kernels, templated on the storage
  * format S and on the population layout LAY (Level::blocked: structure of
- * arrays, or blocks of 32 nodes as rows or pairs).  lbm_kernels.cu
- * instantiates the structure-of-arrays kernels, lbm_blocked.cu and
- * lbm_pairs.cu the blocked ones, so that the sets compile in parallel.
+ * arrays, or blocks of 32 nodes).  lbm_kernels.cu instantiates the
+ * structure-of-arrays kernels and lbm_blocked.cu the blocked ones, so that
+ * the two sets compile in parallel.
  *
  * k_stream_collide is the hot kernel: one thread per lattice node, a warp
  * spans 32 consecutive x of one row, so every population load and store of a
@@ -82,89 +82,87 @@ template <> struct Fmt<__nv_bfloat16> {
     static __device__ __forceinline__ void st(__nv_bfloat16* p, float v, float off) { str(p, v - off); }
 };
 
-/* Element offsets of the pulled populations, split into a z term, a y term,
- * an x term and a population term so that a pull is the sum of four table
- * entries (Level describes the layouts):
- *   0 structure-of-arrays  q qstride + z plane + y pitch + x
- *   1 blocks of rows       32 q + 19 (z plane + y pitch) + (x / 32) 608 + x % 32
- *   2 blocks of pairs      pair_qoff(q) + 19 (z plane + y pitch) + (x / 32) 608
- *                          + (q ? 2 : 1) (x % 32)
- * In the blocked layouts the population term is a compile-time constant, so
- * the 19 pulls and the 19 stores of a node need no per-population address
- * arithmetic beyond an immediate offset.  xt is the x term of population 0,
- * xtp that of the others. */
-template <int LAY> struct Lay;
-template <> struct Lay<0> {
-    static __device__ __forceinline__ unsigned zt(const Level& L, unsigned z) { return z * unsigned(L.plane); }
-    static __device__ __forceinline__ unsigned yt(const Level& L, unsigned y) { return y * unsigned(L.pitch); }
-    static __device__ __forceinline__ unsigned xt(unsigned x) { return x; }
-    static __device__ __forceinline__ unsigned xtp(unsigned x) { return x; }
-    static __device__ __forceinline__ unsigned qt(const Level& L, int q) { return unsigned(q) * unsigned(L.qstride); }
-};
-template <> struct Lay<1> {
-    static __device__ __forceinline__ unsigned zt(const Level& L, unsigned z) { return z * unsigned(L.plane) * 19u; }
-    static __device__ __forceinline__ unsigned yt(const Level& L, unsigned y) { return y * unsigned(L.pitch) * 19u; }
-    static __device__ __forceinline__ unsigned xt(unsigned x) { return (x >> 5) * BLOCK_ELEMS + (x & 31u); }
-    static __device__ __forceinline__ unsigned xtp(unsigned x) { return xt(x); }
-    static __device__ __forceinline__ unsigned qt(const Level&, int q) { return unsigned(q) << 5; }
-};
-template <> struct Lay<2> {
-    static __device__ __forceinline__ unsigned zt(const Level& L, unsigned z) { return z * unsigned(L.plane) * 19u; }
-    static __device__ __forceinline__ unsigned yt(const Level& L, unsigned y) { return y * unsigned(L.pitch) * 19u; }
-    static __device__ __forceinline__ unsigned xt(unsigned x) { return (x >> 5) * BLOCK_ELEMS + (x & 31u); }
-    static __device__ __forceinline__ unsigned xtp(unsigned x) { return (x >> 5) * BLOCK_ELEMS + 2u * (x & 31u); }
-    static __device__ __forceinline__ unsigned qt(const Level&, int q) { return pair_qoff(q); }
-};
-
-/* the element offsets of one node: its own (population 0 and the others) and
- * the z, y and x terms of its pull sources (index 1 - c_q) */
-template <int LAY> struct NodeIdx {
-    unsigned zb[3], yb[3], xs[3], xq[3];
-    unsigned self0, selfp;
+/* Per-node addressing of the populations in the two layouts (Level):
+ *   0 structure-of-arrays: q qstride + z plane + y pitch + x, each pull the
+ *     sum of a population, a z, a y and an x term;
+ *   1 blocked: a node's populations sit at compile-time offsets from its
+ *     block position, pair_qoff(q) + 2 (x % 32) (population 0 at x % 32),
+ *     and a neighbour's at a signed offset of a few elements in x and of
+ *     19 pitch / 19 plane in y / z.  The pull of population q is then one
+ *     base pointer plus the sum of at most three per-thread offsets plus an
+ *     immediate, and the stores of a node one base pointer plus immediates.
+ * pull(f, q): the population q arriving from x - c_q; own(f, q): this
+ * node's population q; at(f, q, cn): population q of node cn (the
+ * neighbours of the inlet / outlet rebuilds). */
+template <int LAY> struct NodeIdx;
+template <> struct NodeIdx<0> {
+    unsigned zb[3], yb[3], xs[3], qs, self;
     __device__ __forceinline__ NodeIdx(const Level& L, unsigned xm, unsigned x, unsigned xp, unsigned ym, unsigned y,
                                        unsigned yp, unsigned zm, unsigned z, unsigned zp) {
-        using A = Lay<LAY>;
-        zb[0] = A::zt(L, zm), zb[1] = A::zt(L, z), zb[2] = A::zt(L, zp);
-        yb[0] = A::yt(L, ym), yb[1] = A::yt(L, y), yb[2] = A::yt(L, yp);
-        xs[0] = A::xt(xm), xs[1] = A::xt(x), xs[2] = A::xt(xp);
-        xq[0] = A::xtp(xm), xq[1] = A::xtp(x), xq[2] = A::xtp(xp);
-        self0 = zb[1] + yb[1] + xs[1];
-        selfp = zb[1] + yb[1] + xq[1];
+        const unsigned plane = unsigned(L.plane), pitch = unsigned(L.pitch);
+        zb[0] = zm * plane, zb[1] = z * plane, zb[2] = zp * plane;
+        yb[0] = ym * pitch, yb[1] = y * pitch, yb[2] = yp * pitch;
+        xs[0] = xm, xs[1] = x, xs[2] = xp;
+        qs = unsigned(L.qstride);
+        self = zb[1] + yb[1] + x;
     }
-    /* population q pulled from x - c_q */
-    __device__ __forceinline__ unsigned pull(const Level& L, int q) const {
-        return Lay<LAY>::qt(L, q) + zb[1 - cz(q)] + yb[1 - cy(q)] + (q == 0 ? xs : xq)[1 - cx(q)];
+    template <class P> __device__ __forceinline__ P* pull(P* f, int q) const {
+        return f + (unsigned(q) * qs + zb[1 - cz(q)] + yb[1 - cy(q)] + xs[1 - cx(q)]);
     }
-    /* population q of this node */
-    __device__ __forceinline__ unsigned own(const Level& L, int q) const {
-        return Lay<LAY>::qt(L, q) + (q == 0 ? self0 : selfp);
+    template <class P> __device__ __forceinline__ P* own(P* f, int q) const { return f + (unsigned(q) * qs + self); }
+    template <class P> __device__ __forceinline__ P* at(P* f, int q, unsigned cn) const {
+        return f + (unsigned(q) * qs + cn);
     }
-    /* population q of the node in the same row / plane at x term index dx,
-     * y term index dy (the neighbours of the inlet / outlet rebuilds) */
-    __device__ __forceinline__ unsigned at(const Level& L, int q, int dx, int dy) const {
-        return Lay<LAY>::qt(L, q) + zb[1] + yb[dy] + (q == 0 ? xs : xq)[dx];
+};
+template <> struct NodeIdx<1> {
+    unsigned base, lane;
+    int dx[3], dy[3], dz[3]; /* element offsets to the x-1 / x / x+1 (y, z) neighbours' pair slots */
+    __device__ __forceinline__ NodeIdx(const Level& L, unsigned xm, unsigned x, unsigned xp, unsigned ym, unsigned y,
+                                       unsigned yp, unsigned zm, unsigned z, unsigned zp) {
+        const int ry = int(L.pitch) * 19, rz = int(L.plane) * 19;
+        lane = x & 31u;
+        const unsigned xq = (x >> 5) * BLOCK_ELEMS + 2u * lane;
+        base = z * unsigned(rz) + y * unsigned(ry) + xq;
+        dx[0] = int((xm >> 5) * BLOCK_ELEMS + 2u * (xm & 31u)) - int(xq);
+        dx[1] = 0;
+        dx[2] = int((xp >> 5) * BLOCK_ELEMS + 2u * (xp & 31u)) - int(xq);
+        dy[0] = (int(ym) - int(y)) * ry, dy[1] = 0, dy[2] = (int(yp) - int(y)) * ry;
+        dz[0] = (int(zm) - int(z)) * rz, dz[1] = 0, dz[2] = (int(zp) - int(z)) * rz;
+    }
+    /* the neighbour part is summed in 32 bits (the element index stays below
+     * 2^31) and widened once; the population's constant offset is added to
+     * the 64-bit pointer, where it becomes the load's immediate */
+    template <class P> __device__ __forceinline__ P* pull(P* f, int q) const {
+        if (q == 0) return f + (base - lane);
+        return (f + (base + unsigned(dz[1 - cz(q)] + dy[1 - cy(q)] + dx[1 - cx(q)]))) + pair_qoff(q);
+    }
+    template <class P> __device__ __forceinline__ P* own(P* f, int q) const {
+        return q == 0 ? f + (base - lane) : (f + base) + pair_qoff(q);
+    }
+    template <class P> __device__ __forceinline__ P* at(P* f, int q, unsigned cn) const {
+        return f + ((cn >> 5) * BLOCK_ELEMS + pair_qoff(q) + (q == 0 ? 1u : 2u) * (cn & 31u));
     }
 };
 
 /* the 19 values g of this node into buffer f: raw stored values (RAW) or
- * populations with the format's offsets removed; the pair layout writes each
- * opposite pair with one store */
+ * populations with the format's offsets removed; the blocked layout writes
+ * each opposite pair with one store */
 template <class S, int LAY, bool RAW>
 __device__ __forceinline__ void store19(const Level& L, S* __restrict__ f, const NodeIdx<LAY>& n,
                                         const typename Fmt<S>::T g[19]) {
     using F = Fmt<S>;
-    if constexpr (LAY == 2) {
-        F::str(f + n.own(L, 0), RAW ? g[0] : g[0] - L.off[0]);
+    if constexpr (LAY == 1) {
+        F::str(n.own(f, 0), RAW ? g[0] : g[0] - L.off[0]);
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
             const int q1 = pair_first(k), q2 = opp(q1);
-            F::st2(f + n.own(L, q1), RAW ? g[q1] : g[q1] - L.off[q1], RAW ? g[q2] : g[q2] - L.off[q2]);
+            F::st2(n.own(f, q1), RAW ? g[q1] : g[q1] - L.off[q1], RAW ? g[q2] : g[q2] - L.off[q2]);
         }
     } else {
 #pragma unroll
         for (int q = 0; q < 19; ++q) {
-            if (RAW) F::str(f + n.own(L, q), g[q]);
-            else F::st(f + n.own(L, q), g[q], L.off[q]);
+            if (RAW) F::str(n.own(f, q), g[q]);
+            else F::st(n.own(f, q), g[q], L.off[q]);
         }
     }
 }
@@ -183,6 +181,10 @@ constexpr int FEAT_DEVMRT = 16;
 #define LBM_SC_ZN 1
 #endif
 constexpr int SC_ZN = LBM_SC_ZN;
+/* with two nodes per thread: load both before updating either */
+#ifndef LBM_SC_PIPE
+#define LBM_SC_PIPE 0
+#endif
 /* a straight-line path for warps whose nodes are all plain fluid */
 #ifndef LBM_SC_FAST
 #define LBM_SC_FAST 0
@@ -192,9 +194,12 @@ constexpr int SC_ZN = LBM_SC_ZN;
 #ifndef LBM_SC_DEV
 #define LBM_SC_DEV 1
 #endif
-/* resident blocks per SM the register allocation must allow (0: no bound) */
+/* resident blocks per SM the register allocation must allow (0: no bound)
+ * for the FP16 / BF16 deviation kernels without lid or alternate
+ * boundaries: 10 blocks of 128 threads, 48 registers, no spills (measured
+ * 3 % faster than 9 blocks at 55 registers on the 512 x 128 x 128 channel) */
 #ifndef LBM_SC_MINB
-#define LBM_SC_MINB 0
+#define LBM_SC_MINB 10
 #endif
 
 /* the collision, statistics, store and moment export of a non-solid node;
@@ -208,7 +213,7 @@ __device__ __forceinline__ void sc_collide_store(const Level& L, const StepParam
     constexpr bool DEV = LBM_SC_DEV && sizeof(S) == 2;
     const unsigned qs = unsigned(L.qstride);
     if constexpr (DEV && DEVMRT) {
-        collide_mrt_dev<T>(f, T(p.omega), p.les != 0, T(p.cs), T(L.u_ref));
+        collide_mrt_dev<T>(f, T(p.omega), p.les != 0, T(p.tau0), T(p.smag_k), T(L.u_ref));
     } else {
         T dp = T(p.dpdy_dev ? *p.dpdy_dev : p.dpdy);
         if (y > p.dyn_y1) dp = T(0);
@@ -270,30 +275,21 @@ __device__ __forceinline__ void sc_export(const Level& L, const StepParams& p, f
     }
 }
 
-/* the node update of one node (x, y, z) inside the level.
- * FP16 / BF16 storage (DEV): the node works on the stored deviations
- * h = f - off and LR7's MRT collides them in that form (collide_mrt_dev),
- * so no population is offset on its way in or out; boundary
- * rebuilds, the lid, the alternate boundaries, the other collision models,
- * the statistics and the moment export see populations f = h + off. */
-template <class S, int FEAT, int LAY>
-__device__ __forceinline__ void sc_node(const Level& L, const StepParams& p, const S* __restrict__ fA,
-                                        S* __restrict__ fB, const uint8_t* __restrict__ mask,
-                                        float* __restrict__ stats, float* __restrict__ mom_export,
-                                        const uint32_t* __restrict__ links, const int x, const int y, const int z) {
-    using F = Fmt<S>;
-    using T = typename F::T;
-    constexpr bool DEV = LBM_SC_DEV && sizeof(S) == 2;
+/* one node of the step: its addressing, mask byte and coordinates */
+template <int LAY> struct ScNode {
+    NodeIdx<LAY> n;
+    unsigned c;
+    int mbyte, type, x, y, z;
+};
+
+template <int FEAT, int LAY>
+__device__ __forceinline__ ScNode<LAY> sc_setup(const Level& L, const uint8_t* __restrict__ mask, const int x,
+                                                const int y, const int z) {
     /* 32-bit element offsets: a level holds fewer than 2^31 elements per
      * buffer (checked at allocation) */
     const unsigned plane = unsigned(L.plane), pitch = unsigned(L.pitch);
     const unsigned c = z * plane + y * pitch + x;
     const int mbyte = mask[c];
-    const int type = mbyte & TYPE_MASK;
-    /* under half-way bounce-back nothing pulls from a solid node, which still
-     * runs the full-way branch below: an early return here would make the
-     * population loads of every warp wait for the mask byte */
-    constexpr bool HALFWAY = (FEAT & FEAT_HALFWAY) != 0;
     /* periodic neighbours; only boundary nodes, whose pulled values the
      * reference discards or bounces, ever wrap in x or y */
     constexpr bool cl = (FEAT & FEAT_CLAMP) != 0;
@@ -303,13 +299,47 @@ __device__ __forceinline__ void sc_node(const Level& L, const StepParams& p, con
     const unsigned yp = (y == L.ny - 1) ? (cl ? y : 0) : y + 1;
     const unsigned zm = (z == 0) ? (cl ? 0 : L.nz - 1) : z - 1;
     const unsigned zp = (z == L.nz - 1) ? (cl ? z : 0) : z + 1;
-    const NodeIdx<LAY> n(L, xm, unsigned(x), xp, ym, unsigned(y), yp, zm, unsigned(z), zp);
+    return ScNode<LAY>{NodeIdx<LAY>(L, xm, unsigned(x), xp, ym, unsigned(y), yp, zm, unsigned(z), zp), c, mbyte,
+                       mbyte & TYPE_MASK, x, y, z};
+}
 
-    /* f: populations, or for DEV their stored deviations */
-    T f[19];
+/* the 19 pulls of a node: populations, or for DEV their stored deviations */
+template <class S>
+__device__ __forceinline__ constexpr bool sc_dev() { return LBM_SC_DEV && sizeof(S) == 2; }
+template <class S, int LAY>
+__device__ __forceinline__ void sc_load(const Level& L, const S* __restrict__ fA, const ScNode<LAY>& nd,
+                                        typename Fmt<S>::T f[19]) {
+    using F = Fmt<S>;
+    using T = typename F::T;
 #pragma unroll
-    for (int q = 0; q < 19; ++q) f[q] = DEV ? T(F::ldr(fA + n.pull(L, q))) : F::ld(fA + n.pull(L, q), L.off[q]);
+    for (int q = 0; q < 19; ++q)
+        f[q] = sc_dev<S>() ? T(F::ldr(nd.n.pull(fA, q))) : F::ld(nd.n.pull(fA, q), L.off[q]);
+}
 
+/* the rest of the node update once its pulls are in f.
+ * FP16 / BF16 storage (DEV): the node works on the stored deviations
+ * h = f - off and LR7's MRT collides them in that form (collide_mrt_dev),
+ * so no population is offset on its way in or out; boundary rebuilds, the
+ * lid, the alternate boundaries, the other collision models, the
+ * statistics and the moment export see populations f = h + off. */
+template <class S, int FEAT, int LAY>
+__device__ __forceinline__ void sc_finish(const Level& L, const StepParams& p, const S* __restrict__ fA,
+                                          S* __restrict__ fB, float* __restrict__ stats,
+                                          float* __restrict__ mom_export, const uint32_t* __restrict__ links,
+                                          const ScNode<LAY>& nd, typename Fmt<S>::T f[19]) {
+    using F = Fmt<S>;
+    using T = typename F::T;
+    constexpr bool DEV = sc_dev<S>();
+    constexpr bool HALFWAY = (FEAT & FEAT_HALFWAY) != 0;
+    const NodeIdx<LAY>& n = nd.n;
+    const unsigned c = nd.c, pitch = unsigned(L.pitch);
+    const int mbyte = nd.mbyte, type = nd.type, x = nd.x, y = nd.y, z = nd.z;
+    /* the neighbours of the inlet / outlet rebuilds (wrapped as the pulls) */
+    constexpr bool cl = (FEAT & FEAT_CLAMP) != 0;
+    const unsigned xm = (x == 0) ? (cl ? 0 : L.nx - 1) : x - 1;
+    const unsigned xp = (x == L.nx - 1) ? (cl ? x : 0) : x + 1;
+    const unsigned ym = (y == 0) ? (cl ? 0 : L.ny - 1) : y - 1;
+    const unsigned yp = (y == L.ny - 1) ? (cl ? y : 0) : y + 1;
 #if LBM_SC_FAST
     const bool plain = type == FLUID && !(HALFWAY && (mbyte & NEAR_SOLID));
     if (__all_sync(__activemask(), plain)) {
@@ -326,8 +356,8 @@ __device__ __forceinline__ void sc_node(const Level& L, const StepParams& p, con
 #pragma unroll
         for (int q = 1; q < 19; ++q)
             if (lk & (1u << q))
-                f[q] = DEV ? F::ldr(fA + n.own(L, opp(q))) + (L.off[opp(q)] - L.off[q])
-                           : F::ld(fA + n.own(L, opp(q)), L.off[opp(q)]);
+                f[q] = DEV ? F::ldr(n.own(fA, opp(q))) + (L.off[opp(q)] - L.off[q])
+                           : F::ld(n.own(fA, opp(q)), L.off[opp(q)]);
     }
 
     if (type == WALL || type == BODY) {
@@ -342,15 +372,10 @@ __device__ __forceinline__ void sc_node(const Level& L, const StepParams& p, con
     } else {
         if (type >= WEST_INLET && type <= NORTH_OUTLET) {
             /* rebuild from the neighbour's stored post-collision state */
-            unsigned nb0, nbp;
-            if (type == WEST_INLET) nb0 = n.xs[2], nbp = n.xq[2];
-            else if (type == EAST_OUTLET) nb0 = n.xs[0], nbp = n.xq[0];
-            else nb0 = n.xs[1], nbp = n.xq[1];
-            const unsigned row = n.zb[1] + (type == SOUTH_INLET ? n.yb[2] : type == NORTH_OUTLET ? n.yb[0] : n.yb[1]);
-            nb0 += row;
-            nbp += row;
+            const unsigned cn = type == WEST_INLET ? c - x + xp : type == EAST_OUTLET ? c - x + xm
+                              : type == SOUTH_INLET ? c + (yp - y) * pitch : c + (ym - y) * pitch;
 #pragma unroll
-            for (int q = 0; q < 19; ++q) f[q] = F::ld(fA + Lay<LAY>::qt(L, q) + (q == 0 ? nb0 : nbp), L.off[q]);
+            for (int q = 0; q < 19; ++q) f[q] = F::ld(n.at(fA, q, cn), L.off[q]);
             T uin = T(p.u_in);
             if (p.noise_amp != 0.f) {
                 const uint32_t cell = uint32_t((z * L.ny + y) * L.nx + x);
@@ -382,8 +407,25 @@ __device__ __forceinline__ void sc_node(const Level& L, const StepParams& p, con
     if (p.exp_nx > 0) sc_export<S>(L, p, mom_export, f, x, y, z);
 }
 
+
+/* the node update of one node (x, y, z) inside the level */
 template <class S, int FEAT, int LAY>
-__global__ void __launch_bounds__(SC_BX* SC_BY, LBM_SC_MINB) k_stream_collide(const Level L, const StepParams p,
+__device__ __forceinline__ void sc_node(const Level& L, const StepParams& p, const S* __restrict__ fA,
+                                        S* __restrict__ fB, const uint8_t* __restrict__ mask,
+                                        float* __restrict__ stats, float* __restrict__ mom_export,
+                                        const uint32_t* __restrict__ links, const int x, const int y, const int z) {
+    const ScNode<LAY> nd = sc_setup<FEAT, LAY>(L, mask, x, y, z);
+    typename Fmt<S>::T f[19];
+    sc_load<S, LAY>(L, fA, nd, f);
+    sc_finish<S, FEAT, LAY>(L, p, fA, fB, stats, mom_export, links, nd, f);
+}
+
+template <int FEAT> __host__ __device__ constexpr int sc_min_blocks() {
+    return (FEAT & FEAT_DEVMRT) && !(FEAT & (FEAT_LID | FEAT_XBC)) ? LBM_SC_MINB : 0;
+}
+
+template <class S, int FEAT, int LAY>
+__global__ void __launch_bounds__(SC_BX* SC_BY, sc_min_blocks<FEAT>()) k_stream_collide(const Level L, const StepParams p,
                                                                   const S* __restrict__ fA, S* __restrict__ fB,
                                                                   const uint8_t* __restrict__ mask,
                                                                   float* __restrict__ stats,
@@ -394,6 +436,18 @@ __global__ void __launch_bounds__(SC_BX* SC_BY, LBM_SC_MINB) k_stream_collide(co
     if (x >= L.nx || y >= L.ny) return;
     if constexpr (SC_ZN == 1) {
         sc_node<S, FEAT, LAY>(L, p, fA, fB, mask, stats, mom_export, links, x, y, int(blockIdx.z));
+    } else if constexpr (SC_ZN == 2 && LBM_SC_PIPE) {
+        /* two nodes of a z column: the pulls of both in flight before either
+         * is updated (the second is the first again past the last plane, and
+         * is then not updated) */
+        const int z0 = blockIdx.z * 2, z1 = min(z0 + 1, L.nz - 1);
+        const ScNode<LAY> a = sc_setup<FEAT, LAY>(L, mask, x, y, z0);
+        const ScNode<LAY> b = sc_setup<FEAT, LAY>(L, mask, x, y, z1);
+        typename Fmt<S>::T fa[19], fb[19];
+        sc_load<S, LAY>(L, fA, a, fa);
+        sc_load<S, LAY>(L, fA, b, fb);
+        sc_finish<S, FEAT, LAY>(L, p, fA, fB, stats, mom_export, links, a, fa);
+        if (z1 != z0) sc_finish<S, FEAT, LAY>(L, p, fA, fB, stats, mom_export, links, b, fb);
     } else {
         const int z0 = blockIdx.z * SC_ZN, z1 = min(z0 + SC_ZN, L.nz);
 #pragma unroll 1
@@ -446,18 +500,18 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, 6) k_stream_collide_mlp(const L
             const int mbyte = mask[c];
             type = mbyte & TYPE_MASK;
 #pragma unroll
-            for (int q = 0; q < 19; ++q) f[q] = F::ld(fA + n.pull(L, q), L.off[q]);
+            for (int q = 0; q < 19; ++q) f[q] = F::ld(n.pull(fA, q), L.off[q]);
             if (HALFWAY && (mbyte & NEAR_SOLID)) {
                 const uint32_t lk = links[c];
 #pragma unroll
                 for (int q = 1; q < 19; ++q)
-                    if (lk & (1u << q)) f[q] = F::ld(fA + n.own(L, opp(q)), L.off[opp(q)]);
+                    if (lk & (1u << q)) f[q] = F::ld(n.own(fA, opp(q)), L.off[opp(q)]);
             }
             if (type >= WEST_INLET && type <= NORTH_OUTLET) {
-                const int dx = type == WEST_INLET ? 2 : type == EAST_OUTLET ? 0 : 1;
-                const int dy = type == SOUTH_INLET ? 2 : type == NORTH_OUTLET ? 0 : 1;
+                const unsigned cn = type == WEST_INLET ? c - x + xp : type == EAST_OUTLET ? c - x + xm
+                                  : type == SOUTH_INLET ? c + (yp - y) * pitch : c + (ym - y) * pitch;
 #pragma unroll
-                for (int q = 0; q < 19; ++q) f[q] = F::ld(fA + n.at(L, q, dx, dy), L.off[q]);
+                for (int q = 0; q < 19; ++q) f[q] = F::ld(n.at(fA, q, cn), L.off[q]);
                 float uin = p.u_in;
                 if (p.noise_amp != 0.f) {
                     const uint32_t cell = uint32_t((z * L.ny + y) * L.nx + x);
@@ -663,10 +717,5 @@ cudaError_t launch_sc_blocked(const Level& L, const StepParams& p, const void* f
 cudaError_t launch_sc_mlp_blocked(const Level& L, const StepParams& p, const void* fA, void* fB,
                                   const uint8_t* mask, float* stats, const uint32_t* links, const void* blob, int* err,
                                   cudaStream_t s);
-cudaError_t launch_sc_pairs(const Level& L, const StepParams& p, const void* fA, void* fB, const uint8_t* mask,
-                            float* stats, float* mom_export, cudaStream_t s, const uint32_t* links);
-cudaError_t launch_sc_mlp_pairs(const Level& L, const StepParams& p, const void* fA, void* fB,
-                                const uint8_t* mask, float* stats, const uint32_t* links, const void* blob, int* err,
-                                cudaStream_t s);
 
 }  // namespace lbm

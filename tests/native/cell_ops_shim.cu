@@ -33,10 +33,12 @@ void cell_invert_scaled(const float* mom, float sf, float* f, int n) {
     for (int i = 0; i < n; ++i) invert_scaled<float>(mom + 9L * i, sf, f + 19L * i);
 }
 void cell_collide_mrt_dev_d(int les, double omega, double cs, double u, double* h, int n) {
-    for (int i = 0; i < n; ++i) collide_mrt_dev<double>(h + 19L * i, omega, les != 0, cs, u);
+    const double k = 18.0 * 1.4142135623730951 * cs;
+    for (int i = 0; i < n; ++i) collide_mrt_dev<double>(h + 19L * i, omega, les != 0, 1.0 / omega, k, u);
 }
 void cell_collide_mrt_dev(int les, float omega, float cs, float u, float* h, int n) {
-    for (int i = 0; i < n; ++i) collide_mrt_dev<float>(h + 19L * i, omega, les != 0, cs, u);
+    const float k = 18.f * 1.41421356f * cs;
+    for (int i = 0; i < n; ++i) collide_mrt_dev<float>(h + 19L * i, omega, les != 0, 1.f / omega, k, u);
 }
 float cell_philox_uniform(uint32_t seed, uint32_t cell, uint32_t step) { return philox_uniform(seed, cell, step); }
 void cell_alt_boundary(int type, float* f, int n, const int* yz, int ny, int nz, float u, int t) {
