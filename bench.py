@@ -124,8 +124,9 @@ def dist_setup():
 
 
 def time_precision(precision: str, steps: int, warmup: int, world: int, dist, with_clocks: bool, gpu: int,
-                   bounceback: str = "halfway", sgs: str = "smagorinsky"):
-    """resident-in-HBM run of `steps` steps after `warmup`; returns (ms, clocks)"""
+                   bounceback: str = "halfway", sgs: str = "smagorinsky", keep_fields: bool = False):
+    """resident-in-HBM run of `steps` steps after `warmup`; returns (ms, kernel ms, clocks, audit, launches,
+    the final rho, u, v, w fields when keep_fields)"""
     import lbm_multigpu_gb300 as lbm
 
     s = lbm.Solver(inputs_text(precision, warmup + steps + 10, bounceback, sgs))
@@ -144,10 +145,35 @@ def time_precision(precision: str, steps: int, warmup: int, world: int, dist, wi
     launches = s.launch_count() - n0
     if dist:
         dist.barrier()
-    kernel_ms = s.time_stream_collide(20)
+    fields = s.fields() if keep_fields else None  # the state after warmup + steps steps
     audit = s.audit()
+    kernel_ms = s.time_stream_collide(20)
     s.close()
-    return ms, kernel_ms, clocks, audit, launches
+    return ms, kernel_ms, clocks, audit, launches, fields
+
+
+def fp64_twin_fields(nsteps: int):
+    """the FP64-storage twin of the same kernels after nsteps steps (the
+    accuracy reference of the reduced-precision stores), and the fluid mask"""
+    import lbm_multigpu_gb300 as lbm
+
+    with lbm.Solver(inputs_text("fp64", nsteps + 10)) as s:
+        s.step(nsteps)
+        return s.fields(), s.mask()
+
+
+def field_errors(fields, ref, mask) -> dict:
+    """max and RMS density and velocity error of fields against ref over the
+    fluid nodes, and the relative L2 velocity error"""
+    import numpy as np
+
+    fl = (mask != 1) & (mask != 2)
+    rho, u = fields[0][fl].astype(np.float64), np.stack([f[fl] for f in fields[1:]]).astype(np.float64)
+    rr, ur = ref[0][fl].astype(np.float64), np.stack([f[fl] for f in ref[1:]]).astype(np.float64)
+    dr, du = rho - rr, np.linalg.norm(u - ur, axis=0)
+    return dict(rho_err_max=float(np.abs(dr).max()), rho_err_rms=float(np.sqrt(np.mean(dr ** 2))),
+                u_err_max=float(du.max()), u_err_rms=float(np.sqrt(np.mean(du ** 2))),
+                u_rel_l2=float(np.linalg.norm(u - ur) / np.linalg.norm(ur)))
 
 
 def worst_over_ranks(ms: float, dist) -> float:
@@ -291,6 +317,22 @@ def reference_arm(args, world, rank):
     print(json.dumps(line))
 
 
+C3_PATCH = dict(lr_dims=(96, 64, 64), lr_origin=(48.25, 47.25, 16.25), cf_time="linear")
+
+
+def c3_inputs(tmax: int, lr_dims=C3_PATCH["lr_dims"], lr_origin=C3_PATCH["lr_origin"],
+              cf_time=C3_PATCH["cf_time"]) -> str:
+    """the two-level refinement record: coarse 256x128x64 MRT-LES channel,
+    circular cylinder of diameter 12 coarse cells at (64.5, 63.5), ratio-2
+    patch (by default the configured 96x64x64 fine cells bounded in z from
+    coarse z 16.25, linear temporal interpolation), tau0 = 0.52, 1 % noise"""
+    import lbm_multigpu_gb300 as lbm
+
+    return lbm.make_inputs(256, 128, 64, obst1=(64.5, 63.5, 0.0), r1=6.0, re=90.0, umax=0.05, tmax=tmax, les=1,
+                           cs=0.01, geometry="channel_circle", refinement=1, lr_dims=lr_dims, lr_factor=0.5,
+                           lr_origin=lr_origin, inlet_noise=0.01, cf_time=cf_time)
+
+
 def workload_c3(steps: int, warmup: int) -> dict:
     """two-level refinement as the configuration names it: coarse 256x128x64
     MRT-LES channel, circular cylinder of diameter 12 coarse cells, a ratio-2
@@ -303,10 +345,7 @@ def workload_c3(steps: int, warmup: int) -> dict:
     import lbm_multigpu_gb300 as lbm
 
     def run(lr_dims, lr_origin, cf_time):
-        text = lbm.make_inputs(256, 128, 64, obst1=(64.5, 63.5, 0.0), r1=6.0, re=90.0, umax=0.05,
-                               tmax=steps + warmup + 10, les=1, cs=0.01, geometry="channel_circle", refinement=1,
-                               lr_dims=lr_dims, lr_factor=0.5, lr_origin=lr_origin, inlet_noise=0.01,
-                               cf_time=cf_time)
+        text = c3_inputs(steps + warmup + 10, lr_dims, lr_origin, cf_time)
         with lbm.Solver(text) as s:
             s.step(warmup)
             s.synchronize()
@@ -322,7 +361,7 @@ def workload_c3(steps: int, warmup: int) -> dict:
                                    interface_and_force=ms / steps - kc - 2 * kf),
                     gpu_launches=launches, audit_mass=float(audit[0]))
 
-    main = run((96, 64, 64), (48.25, 47.25, 16.25), "linear")
+    main = run(C3_PATCH["lr_dims"], C3_PATCH["lr_origin"], C3_PATCH["cf_time"])
     ref = run((96, 64, 128), (48.25, 47.25, -0.75), "none")
     return dict(workload="C3 two-level refinement: coarse 256x128x64 + fine 96x64x64 (ratio 2, bounded in z from "
                          "coarse z 16.25), linear temporal interpolation, MRT-LES, circular cylinder D=12, tau0=0.52 "
@@ -333,43 +372,51 @@ def workload_c3(steps: int, warmup: int) -> dict:
                                                 "interpolation (LR7's layout and schedule)"))
 
 
-def workload_c4(steps: int) -> dict:
+def workload_c4(steps: int, every: int = 250) -> dict:
     """precision: the channel geometry scaled to 768x256x256 (square cylinder
     side 24 at x=192, tau0=0.52) with populations stored as FP16 / BF16
-    (offset f - feq(1, u_in)), FP32 collide, beside FP32 and an FP64-storage
-    twin of the same kernels: max / RMS density and velocity error of each
-    against FP64, and MLUPS"""
+    (deviations from the MRT equilibrium at (1, u_in)), FP32 collide, beside
+    FP32 and an FP64-storage twin of the same kernels, advanced side by side:
+    max / RMS density and velocity error of each against FP64 every `every`
+    steps (the error-vs-step trace), and MLUPS from the summed step times"""
     import numpy as np
 
     import lbm_multigpu_gb300 as lbm
 
     nx, ny, nz = 768, 256, 256
-    out, ref, mask = {}, None, None
-    for prec in ("fp64", "fp32", "fp16", "bf16"):
-        text = lbm.make_inputs(nx, ny, nz, obst1=(192.5, 127.5, 0.0), r1=12.0, re=180.0, umax=0.05,
-                               tmax=steps + 10, les=1, cs=0.01, geometry="channel_square", precision=prec,
-                               bounceback="halfway")
-        with lbm.Solver(text) as s:
-            ms = s.step_timed(steps)
-            rho, u, v, w = s.fields()
-            if mask is None:
-                mask = s.mask()
-        fl = (mask != 1) & (mask != 2)
-        r = dict(mlups=nx * ny * nz * steps / (ms * 1e3), ms_per_step=ms / steps)
-        vel = np.stack([u[fl], v[fl], w[fl]]).astype(np.float64)
-        rh = rho[fl].astype(np.float64)
-        if ref is None:
-            ref = (rh, vel)
-        else:
-            dr, dv = rh - ref[0], np.linalg.norm(vel - ref[1], axis=0)
-            r.update(rho_err_max=float(np.abs(dr).max()), rho_err_rms=float(np.sqrt(np.mean(dr ** 2))),
-                     u_err_max=float(dv.max()), u_err_rms=float(np.sqrt(np.mean(dv ** 2))),
-                     u_rel_l2=float(np.linalg.norm(vel - ref[1]) / np.linalg.norm(ref[1])))
-        out[prec] = r
+    precs = ("fp64", "fp32", "fp16", "bf16")
+    solvers = {}
+    for prec in precs:
+        solvers[prec] = lbm.Solver(lbm.make_inputs(nx, ny, nz, obst1=(192.5, 127.5, 0.0), r1=12.0, re=180.0,
+                                                   umax=0.05, tmax=steps + 10, les=1, cs=0.01,
+                                                   geometry="channel_square", precision=prec, bounceback="halfway"))
+    mask = solvers["fp64"].mask()
+    ms = {prec: 0.0 for prec in precs}
+    trace = {prec: [] for prec in precs[1:]}
+    done = 0
+    while done < steps:
+        k = min(every, steps - done)
+        for prec in precs:
+            ms[prec] += solvers[prec].step_timed(k)
+        done += k
+        ref = solvers["fp64"].fields()
+        for prec in precs[1:]:
+            e = field_errors(solvers[prec].fields(), ref, mask)
+            trace[prec].append(dict(step=done, **e))
+    for s_ in solvers.values():
+        s_.close()
+    out = {}
+    for prec in precs:
+        out[prec] = dict(mlups=nx * ny * nz * steps / (ms[prec] * 1e3), ms_per_step=ms[prec] / steps)
+        if prec != "fp64":
+            out[prec].update({k: v for k, v in trace[prec][-1].items() if k != "step"})
+            out[prec]["trace"] = [dict(step=t["step"], u_rel_l2=t["u_rel_l2"], u_err_rms=t["u_err_rms"],
+                                       rho_err_rms=t["rho_err_rms"]) for t in trace[prec]]
     for prec in ("fp16", "bf16"):
         out[prec]["mlups_vs_fp32"] = out[prec]["mlups"] / out["fp32"]["mlups"]
     return dict(workload="C4 precision: 768x256x256 channel, square cylinder side 24, MRT-LES, half-way "
-                         "bounce-back; errors over fluid nodes against the FP64-storage twin",
+                         "bounce-back; errors over fluid nodes against the FP64-storage twin, traced every "
+                         f"{every} steps",
                 steps=steps, results=out)
 
 
@@ -469,20 +516,27 @@ def main():
 
     # FP32 Smagorinsky (the reference point), then the FP16 / BF16 stores
     main_prec = "fp32" if args.precision == "all" else args.precision
-    ms32, kms32, clocks, audit, launches = time_precision(main_prec, args.steps, args.warmup, world, dist, True, local)
-    res = {}
+    ms32, kms32, clocks, audit, launches, f32 = time_precision(main_prec, args.steps, args.warmup, world, dist, True,
+                                                               local, keep_fields=True)
+    res, fields = {}, {main_prec: f32}
     for prec in (("fp16", "bf16") if args.precision == "all" else ()):
-        ms, kms, _, _, _ = time_precision(prec, args.steps, args.warmup, world, dist, False, local)
+        ms, kms, _, _, _, fields[prec] = time_precision(prec, args.steps, args.warmup, world, dist, False, local,
+                                                       keep_fields=True)
         res[prec] = (ms, kms)
     full = sgsr = None
     if args.precision == "all" and SGS_WEIGHTS.exists():
         # the learned closure in place of Smagorinsky (tensor-core MLP per tile)
-        mss, kmss, _, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, sgs="mlp")
+        mss, kmss, _, _, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, sgs="mlp")
         sgsr = (mss, kmss)
     if args.precision == "all":
         # the reference's own wall treatment (full-way, on-node bounce-back)
-        msf, kmsf, _, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, "fullway")
+        msf, kmsf, _, _, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, "fullway")
         full = (msf, kmsf)
+    # every storage precision against the FP64 twin of the same steps
+    acc = {}
+    if rank == 0:
+        ref, mask = fp64_twin_fields(args.warmup + args.steps)
+        acc = {prec: field_errors(f, ref, mask) for prec, f in fields.items()}
 
     def worst(ms):
         return worst_over_ranks(ms, dist)
@@ -522,6 +576,7 @@ def main():
                                       h2d_bytes_per_step=e2e["h2d"], d2h_bytes_per_step=e2e["d2h"],
                                       steps=min(args.steps, 2000)),
         gpu_launches=launches * world,
+        accuracy_vs_fp64=dict(acc.get(main_prec, {}), steps=args.warmup + args.steps),
         clocks=clocks,
         audit=dict(mass=float(audit[0]), momentum=[float(a) for a in audit[1:]]),
     )
@@ -529,7 +584,8 @@ def main():
         v = world * CELLS * args.steps / (ms * 1e-3) / 1e6
         gbs = CELLS * BYTES_PER_CELL[prec] / (kms * 1e-3) / 1e9
         line[f"{prec}_store"] = dict(value=v, ratio_vs_fp32=v / mlups, ms_per_step=ms / args.steps,
-                                     kernel_gbs=gbs, frac=gbs / pk["hbm_gbs"])
+                                     kernel_ms=kms, kernel_gbs=gbs, frac=gbs / pk["hbm_gbs"],
+                                     accuracy_vs_fp64=dict(acc.get(prec, {}), steps=args.warmup + args.steps))
     if full:
         v = world * CELLS * args.steps / (worst(full[0]) * 1e-3) / 1e6
         gbs = CELLS * BYTES_PER_CELL["fp32"] / (full[1] * 1e-3) / 1e9

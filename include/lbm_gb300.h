@@ -207,7 +207,9 @@ size_t lbm_body_force_scratch_doubles(void);
  * the process exits.  It never allocates.  The first call on a device looks
  * up that array's address (make the first call before capturing work into a
  * stream).  All calls share the array: calls that overlap on the GPU (other
- * streams, other threads) race and must be serialised by the caller.  Domains
+ * streams, other threads) race and must be serialised by the caller.  The
+ * looked-up address is kept for the life of the process, so a device that
+ * has been reset (cudaDeviceReset) must not be used with this call again.  Domains
  * whose 19 populations need 2^31 or more elements are rejected (LBM_ERR_ARG),
  * as by lbm_body_force_f32. */
 int lbm_body_force_f32_noalloc(const float* fA, const uint8_t* mask, int nx, int ny, int nz, int pitch,

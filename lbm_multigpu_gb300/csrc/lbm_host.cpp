@@ -576,8 +576,13 @@ struct lbm_handle {
      * each): lbm_step captures batches of steps into one CUDA graph, updated
      * in place from batch to batch (uniform runs too: it removes the gaps
      * between their launches) */
-    cudaGraphExec_t gexec = nullptr;
+    cudaGraphExec_t gexec[17] = {}; /* by batch length (GRAPH_STEPS = 16) */
     long long launches = 0;         /* kernels this handle has launched */
+    /* FP32 staging of the populations of a level for lbm_get/set_populations
+     * (the stored layout or precision is not the caller's), allocated on
+     * first use and kept */
+    float* stage = nullptr;
+    size_t stage_n = 0;
     /* learned subgrid closure: device weight blob and its error flag */
     unsigned char* mlp_blob = nullptr;
     int* mlp_err = nullptr;
@@ -948,17 +953,18 @@ int run_graph(lbm_handle* h, int k) {
         return rc != LBM_OK ? rc : fail(LBM_ERR_CUDA, "step capture: %s", cudaGetErrorString(ec));
     }
     cudaError_t e = cudaSuccess;
-    if (h->gexec) {
+    cudaGraphExec_t& gx = h->gexec[k];
+    if (gx) {
         cudaGraphExecUpdateResultInfo info{};
-        if (cudaGraphExecUpdate(h->gexec, g, &info) != cudaSuccess) {
+        if (cudaGraphExecUpdate(gx, g, &info) != cudaSuccess) {
             cudaGetLastError();
-            cudaGraphExecDestroy(h->gexec);
-            h->gexec = nullptr;
+            cudaGraphExecDestroy(gx);
+            gx = nullptr;
         }
     }
-    if (!h->gexec) e = cudaGraphInstantiate(&h->gexec, g, 0);
+    if (!gx) e = cudaGraphInstantiate(&gx, g, 0);
     cudaGraphDestroy(g);
-    if (e == cudaSuccess) e = cudaGraphLaunch(h->gexec, h->stream);
+    if (e == cudaSuccess) e = cudaGraphLaunch(gx, h->stream);
     if (e != cudaSuccess) {
         restore();
         return fail(LBM_ERR_CUDA, "step graph: %s", cudaGetErrorString(e));
@@ -1224,7 +1230,9 @@ int lbm_destroy(lbm_handle* h) {
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->ev_cf_fork) cudaEventDestroy(h->ev_cf_fork);
     if (h->ev_cf_join) cudaEventDestroy(h->ev_cf_join);
-    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    for (cudaGraphExec_t& g : h->gexec)
+        if (g) cudaGraphExecDestroy(g);
+    cudaFree(h->stage);
     if (h->side) cudaStreamDestroy(h->side);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -1303,6 +1311,20 @@ int lbm_init_equilibrium(lbm_handle* h) {
     return do_init(h);
 }
 
+/* the handle's FP32 staging buffer, at least n floats */
+static int staging(lbm_handle* h, size_t n, float** d) {
+    if (h->stage_n < n) {
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        cudaFree(h->stage);
+        h->stage = nullptr;
+        h->stage_n = 0;
+        CUDA_TRY(cudaMalloc((void**)&h->stage, n * sizeof(float)));
+        h->stage_n = n;
+    }
+    *d = h->stage;
+    return LBM_OK;
+}
+
 int lbm_get_populations(lbm_handle* h, int level, float* f) {
     if (int rc = check_level(h, level)) return rc;
     if (!f) return fail(LBM_ERR_ARG, "f is null");
@@ -1316,11 +1338,10 @@ int lbm_get_populations(lbm_handle* h, int level, float* f) {
         return LBM_OK;
     }
     float* d = nullptr;
-    CUDA_TRY(cudaMallocAsync((void**)&d, n * sizeof(float), h->stream));
+    if (int rc = staging(h, n, &d)) return rc;
     cudaError_t e = launch_pack(s.L, s.f[s.cur], d, h->stream);
     ++h->launches;
     if (e == cudaSuccess) e = cudaMemcpyAsync(f, d, n * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
-    cudaFreeAsync(d, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "get_populations: %s", cudaGetErrorString(e));
     return LBM_OK;
@@ -1341,10 +1362,9 @@ int lbm_set_populations(lbm_handle* h, int level, const float* f) {
         return LBM_OK;
     }
     float* d = nullptr;
-    CUDA_TRY(cudaMallocAsync((void**)&d, n * sizeof(float), h->stream));
+    if (int rc = staging(h, n, &d)) return rc;
     cudaError_t e = cudaMemcpyAsync(d, f, n * sizeof(float), cudaMemcpyHostToDevice, h->stream);
     for (int i = 0; i < 2 && e == cudaSuccess; ++i, ++h->launches) e = launch_unpack(s.L, d, s.f[i], h->stream);
-    cudaFreeAsync(d, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "set_populations: %s", cudaGetErrorString(e));
     return LBM_OK;
@@ -1353,8 +1373,13 @@ int lbm_set_populations(lbm_handle* h, int level, const float* f) {
 int lbm_step(lbm_handle* h, int nsteps) {
     if (!h) return fail(LBM_ERR_ARG, "null handle");
     if (nsteps < 0) return fail(LBM_ERR_ARG, "nsteps %d < 0", nsteps);
+    /* the first step is launched directly and the batches grow 2, 4, 8, 16,
+     * so that the host captures each batch while the GPU runs the one
+     * before (one executable graph per batch length, updated in place) */
+    int kb = 1;
     for (int i = 0; i < nsteps;) {
-        const int k = std::min(GRAPH_STEPS, nsteps - i);
+        const int k = std::min(kb, nsteps - i);
+        kb = std::min(2 * kb, GRAPH_STEPS);
         int rc;
         if (k >= 2 && graph_ok(h, k)) {
             rc = run_graph(h, k);
@@ -1852,17 +1877,9 @@ int lbm_format_forces(const char* inputs_text, const double* fxyz, int n, char* 
 /* ---- kernel-level API ---- */
 
 static int kernel_level(Level& L, int nx, int ny, int nz, int pitch) {
-    if (nx < 1 || ny < 1 || nz < 1 || pitch < nx || pitch % 32) return fail(LBM_ERR_ARG, "bad dimensions or pitch");
-    L = Level{};
-    L.nx = nx;
-    L.ny = ny;
-    L.nz = nz;
-    L.pitch = pitch;
-    L.plane = (long long)pitch * ny;
-    L.qstride = L.plane * nz;
-    L.storage = STORE_F32;
-    set_offsets(L, 0.f, MRT);
-    if (L.qstride * 19 >= (1LL << 31)) return fail(LBM_ERR_ARG, "level too large: 19 populations must index below 2^31");
+    const int rc = f32_kernel_level(L, nx, ny, nz, pitch);
+    if (rc == 1) return fail(LBM_ERR_ARG, "bad dimensions or pitch");
+    if (rc == 2) return fail(LBM_ERR_ARG, "level too large: 19 populations must index below 2^31");
     return LBM_OK;
 }
 

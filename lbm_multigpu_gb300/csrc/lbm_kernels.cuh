@@ -71,6 +71,25 @@ struct Level {
 /* elements of one 32-node block of the blocked layout */
 constexpr unsigned BLOCK_ELEMS = 19u * 32u;
 
+/* The FP32 structure-of-arrays level of the kernel-level API (caller-owned
+ * buffers in the reference's layout, no storage offsets).  Returns 1 for bad
+ * dimensions or pitch, 2 when 19 populations would not index below 2^31,
+ * else 0 with L filled in. */
+inline int f32_kernel_level(Level& L, int nx, int ny, int nz, int pitch) {
+    if (nx < 1 || ny < 1 || nz < 1 || pitch < nx || pitch % 32) return 1;
+    if ((long long)pitch * ny * nz * 19 >= (1LL << 31)) return 2;
+    L = Level{};
+    L.nx = nx;
+    L.ny = ny;
+    L.nz = nz;
+    L.pitch = pitch;
+    L.plane = (long long)pitch * ny;
+    L.qstride = L.plane * nz;
+    L.storage = STORE_F32;
+    L.blocked = 0;
+    return 0;
+}
+
 /* the pairs of the blocked layout: (q, opp(q)) for the first members
  * 1, 2, 9, 5, 6, 10, 12, 11, 13 */
 __host__ __device__ constexpr int pair_first(int k) {

@@ -34,7 +34,10 @@ double* g_scratch_addr[MAX_DEVICES] = {nullptr};
  * code the array's name only stands in for the symbol: a kernel given it
  * would fault, or on a system where the GPU can reach host memory silently
  * use the wrong memory.  So the address is looked up once per device, with
- * that device current, and reused. */
+ * that device current, and reused.  A cudaDeviceReset (or anything else that
+ * destroys the device's primary context) reloads the module and can move
+ * the array; the cached address is then stale, so this entry point must not
+ * be used on a device after it has been reset in the same process. */
 int scratch_on_current_device(double** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -56,9 +59,11 @@ int scratch_on_current_device(double** out) {
 extern "C" int lbm_body_force_f32_noalloc(const float* fA, const uint8_t* mask, int nx, int ny, int nz, int pitch,
                                           double* force_out, void* cuda_stream) {
     if (!fA || !mask || !force_out) return lbm::set_error(LBM_ERR_ARG, "null device pointer", cudaSuccess);
-    if (nx < 1 || ny < 1 || nz < 1 || pitch < nx || pitch % 32)
-        return lbm::set_error(LBM_ERR_ARG, "bad dimensions or pitch", cudaSuccess);
-    if ((long long)pitch * ny * nz * 19 >= (1LL << 31))
+    /* the same level as lbm_body_force_f32 builds */
+    lbm::Level L;
+    const int lc = lbm::f32_kernel_level(L, nx, ny, nz, pitch);
+    if (lc == 1) return lbm::set_error(LBM_ERR_ARG, "bad dimensions or pitch", cudaSuccess);
+    if (lc == 2)
         return lbm::set_error(LBM_ERR_ARG, "level too large: 19 populations must index below 2^31", cudaSuccess);
     /* the reduction needs force_scan_partials()*3 doubles whatever the domain
      * size (the scan kernel strides over rows with a fixed grid) */
@@ -67,14 +72,6 @@ extern "C" int lbm_body_force_f32_noalloc(const float* fA, const uint8_t* mask, 
                               cudaSuccess);
     double* scratch = nullptr;
     if (int rc = scratch_on_current_device(&scratch)) return rc;
-    lbm::Level L{};
-    L.nx = nx;
-    L.ny = ny;
-    L.nz = nz;
-    L.pitch = pitch;
-    L.plane = (long long)pitch * ny;
-    L.qstride = L.plane * nz;
-    L.storage = lbm::STORE_F32;
     /* every launch writes all partials before its final sum reads them, so
      * nothing in the shared array needs clearing between calls */
     cudaError_t e = lbm::launch_force_scan(L, fA, mask, scratch, force_out, (cudaStream_t)cuda_stream);

@@ -4,8 +4,8 @@ TEST INFRASTRUCTURE ONLY.  Nothing here is part of the product path.
 
 * ``build_oracle()`` compiles this directory's CPU restatement
   (lbm_oracle.cpp, sgs_oracle.cpp) into ``oracle/_build/liblbm_oracle.so``.
-* ``stage()`` reads the reference sources from ``$LBM_REFERENCE``
-  (default /root/reference, present only in the development container) and
+* ``stage()`` reads the reference sources from ``$LBM_REFERENCE`` (the
+  reference checkout; unset, nothing is staged) and
   writes copies of the code paths the tests need into ``oracle/_ref/``, which is
   git-ignored and travels to the GPU machine with the working tree:
     - ``lr7_body.inc``: LRTurbTest/LRMultiGPU7.cu from ImageFcnLR up to main()
@@ -35,7 +35,9 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 REF_DIR = HERE / "_ref"
 BUILD_DIR = HERE / "_build"
-REF_ROOT = Path(os.environ.get("LBM_REFERENCE", "/root/reference"))
+# the reference checkout to stage from: $LBM_REFERENCE (unset: nothing is
+# staged, and the copies already in _ref/, if any, are used)
+REF_ROOT = Path(os.environ["LBM_REFERENCE"]) if os.environ.get("LBM_REFERENCE") else None
 
 CXX = os.environ.get("CXX", "g++")
 # identical FP32 arithmetic on x86 and aarch64 hosts: no contraction into FMA
@@ -66,6 +68,11 @@ LR7_CONFIGS = {
     "chan_les_1k": dict(XDIM=64, YDIM=24, ZDIM=6, TMAX=1000, STARTF=0, OBSTR1="4.f", OBSTX1="20.5f",
                         OBSTY1="11.5f", RE="60.f", UMAX="0.05f", SmagLES=1, CS="0.01f", REFINEMENT=0,
                         VELAV=0, START_VELAV=100000, START_VELFLUC=250000),
+    # the geometry of the 512x128x128 channel benchmark (square body of side 16
+    # at x = 128): only its ImageFcn is evaluated (the mask fixture)
+    "c2_geom": dict(XDIM=512, YDIM=128, ZDIM=128, TMAX=4, STARTF=0, OBSTR1="8.f", OBSTX1="128.5f",
+                    OBSTY1="63.5f", RE="120.f", UMAX="0.05f", SmagLES=1, CS="0.01f", REFINEMENT=0,
+                    VELAV=0, START_VELAV=100000, START_VELFLUC=250000),
     # tiny channel for the output-writer fixtures (statistics switch on at t = 5 and 12)
     "tiny": dict(XDIM=64, YDIM=8, ZDIM=4, TMAX=20, STARTF=0, OBSTR1="2.f", OBSTX1="20.5f", OBSTY1="3.5f",
                  RE="40.f", UMAX="0.05f", SmagLES=1, CS="0.01f", REFINEMENT=0, VELAV=1, START_VELAV=5,
@@ -122,8 +129,10 @@ def _parse_defines(text: str, stop_pat: str) -> dict:
     return out
 
 
-def stage(ref_root: Path = REF_ROOT) -> bool:
+def stage(ref_root: Path | None = REF_ROOT) -> bool:
     """Copy the needed reference code paths into oracle/_ref.  False if absent."""
+    if ref_root is None:
+        return False
     lr7 = ref_root / "LRTurbTest" / "LRMultiGPU7.cu"
     di3 = ref_root / "MRTtest" / "DynInlet3.cu"
     cpu = ref_root / "CPU_3D" / "CPU_3D.cpp"

@@ -243,7 +243,20 @@ def alt_bc():
     np.savez_compressed(HERE / "alt_bc.npz", **out)
 
 
-PARTS = dict(cells=lambda: cells(), runs=lambda: runs(), writer=lambda: writer(),
+def masks():
+    """the reference's ImageFcn (LR7:88-127) on the 512x128x128 channel
+    benchmark's geometry (square body of side 16 at x = 128.5, y = 63.5),
+    with the run record the reference writes for it"""
+    cfg = ref_recipe.LR7_CONFIGS["c2_geom"]
+    L = lib("lr7_c2_geom.so")
+    X, Y, Z = cfg["XDIM"], cfg["YDIM"], cfg["ZDIM"]
+    img = np.zeros((Z, Y, X), np.int32)
+    L.ref_image(ptr(img))
+    np.savez_compressed(HERE / "masks.npz", c2_image=img.astype(np.int16))
+    (HERE / "masks.json").write_text(json.dumps(dict(c2=dict(inputs=write_inputs_text(L))), indent=1))
+
+
+PARTS = dict(cells=lambda: cells(), runs=lambda: runs(), writer=lambda: writer(), masks=lambda: masks(),
              cpu3d_cavity=lambda: cpu3d_cavity(), alt_bc=lambda: alt_bc(),
              runs_1k=lambda: runs((("chan_les_1k", 1000),), "runs_1k"),
              cpu3d_cavity_1k=lambda: cpu3d_cavity("cav24_1k", 1000, "cpu3d_cavity24_1k.npz"))

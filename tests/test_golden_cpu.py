@@ -5,11 +5,14 @@ and the node masks against the reference's ImageFcn / ImageFcnLR, bit-exact.
 from __future__ import annotations
 
 import ctypes
+from pathlib import Path
 
 import numpy as np
 import pytest
 
 from oracle_bindings import REF_CODE, OracleRun, Refine, moments, ptr, rel_l2
+
+ROOT = Path(__file__).resolve().parents[1]
 
 F = ctypes.c_float
 # FP32 per-cell tolerance: populations are O(0.05..0.33), the reference
@@ -218,3 +221,51 @@ def test_lid_regularisation_vs_reference(golden, orc, cellops):
         g = f0.copy()
         getattr(lib, fn)(ptr(g), n, 0, F(0.0), F(0.04), F(0.0), 1)
         np.testing.assert_allclose(g, want, atol=ATOL_CELL, rtol=0, err_msg=fn)
+
+
+def test_c2_benchmark_mask_vs_imagefcn(product):
+    """the mask of the 512x128x128 channel benchmark, from the record bench.py
+    runs, equals the reference's ImageFcn (LR7:88-127) on that geometry node
+    for node (tests/golden/masks.npz, made by make_golden.py)"""
+    import json
+
+    import bench
+
+    img = np.load(ROOT / "tests" / "golden" / "masks.npz")["c2_image"]
+    m = product.inputs_mask(bench.inputs_text("fp32", 10), 0).reshape(img.shape)
+    np.testing.assert_array_equal(_mask_codes(m), img)
+    text = json.loads((ROOT / "tests" / "golden" / "masks.json").read_text())["c2"]["inputs"]
+    np.testing.assert_array_equal(_mask_codes(product.inputs_mask(text, 0).reshape(img.shape)), img)
+    assert (img == 10).sum() == 16 * 16 * 128
+
+
+def test_c3_circle_masks_vs_cylinder_rule(product):
+    """the coarse and fine masks of the two-level refinement benchmark: the
+    cylinder rule of CPU_3D's ImageFcn, (x - X)^2 + (y - Y)^2 < R^2 in FP32
+    (CPU_3D/CPU_3D.cpp:41-42), on coarse nodes and on the fine nodes at
+    LR location + i LR factor (ImageFcnLR's coordinates, LR7:68-86), with the
+    channel's walls, inlet and outlet on the coarse level (LR7:88-127)"""
+    import bench
+
+    text = bench.c3_inputs(10)
+    f32 = np.float32
+    X, Y, R = f32(64.5), f32(63.5), f32(6.0)
+
+    def circle(xc, yc):
+        dx, dy = xc - X, yc - Y
+        return (dx * dx + dy * dy) < R * R
+
+    nx, ny, nz = 256, 128, 64
+    m = product.inputs_mask(text, 0).reshape(nz, ny, nx)
+    y, x = np.meshgrid(np.arange(ny, dtype=f32), np.arange(nx, dtype=f32), indexing="ij")
+    want = np.where(circle(x, y), 2, 0).astype(np.uint8)
+    want[:, 0], want[:, -1] = 3, 4
+    want[0, :], want[-1, :] = 1, 1
+    np.testing.assert_array_equal(m, np.broadcast_to(want, m.shape))
+    fx, fy, fz = bench.C3_PATCH["lr_dims"]
+    x0, y0, _ = (f32(v) for v in bench.C3_PATCH["lr_origin"])
+    fm = product.inputs_mask(text, 1).reshape(fz, fy, fx)
+    yy, xx = np.meshgrid(np.arange(fy, dtype=f32), np.arange(fx, dtype=f32), indexing="ij")
+    fwant = np.where(circle(x0 + xx * f32(0.5), y0 + yy * f32(0.5)), 2, 0).astype(np.uint8)
+    np.testing.assert_array_equal(fm, np.broadcast_to(fwant, fm.shape))
+    assert (fwant == 2).sum() > 400  # the cylinder lies in the patch

@@ -179,8 +179,9 @@ def test_z_bounded_patch_vs_oracle(product, cf_time):
 @pytest.mark.parametrize("cf_time", ["none", "linear"])
 def test_refinement_step_graphs_are_bit_exact(product, cf_time):
     """lbm_step captures refinement steps in batches into CUDA graphs; one
-    call of n steps (batches of 16, 16 and 8 replayed from graphs) equals n
-    calls of one step (launched directly) bit for bit on both levels, with
+    call of n steps (one direct step, then batches of 16, 16 and 7 replayed
+    from graphs) equals n calls of one step (launched directly) bit for bit
+    on both levels, with
     running statistics and inlet noise on (both take the step index baked
     into each captured launch), with and without linear temporal
     interpolation"""
@@ -864,3 +865,55 @@ def test_checkpoint_layout_must_match(product, tmp_path):
     with lbm.Solver(_chan_inputs(lbm, 10, precision="fp16", layout="soa")) as s:
         with pytest.raises(lbm.LbmError, match="layout"):
             s.restore_state(path)
+
+
+def test_c2_benchmark_channel_vs_oracle(product):
+    """the channel exactly as bench.py runs it (its own record: 512x128x128,
+    MRT + Smagorinsky CS = 0.01, tau0 = 0.52, square body of side 16 at
+    x = 128 with half-way bounce-back, 1 % seeded inlet noise, zero-gradient
+    outlet, periodic z) against the oracle at full size after 60 steps:
+    velocity relative L2 and density within 1e-5, drag within 1e-4"""
+    import bench
+
+    lbm = product
+    steps = 60
+    with lbm.Solver(bench.inputs_text("fp32", steps)) as s:
+        s.step(steps)
+        f, mask, om, F = s.populations(), s.mask(), s.params()["omega"], s.forces()
+    o = OracleRun(bench.NX, bench.NY, bench.NZ, mask, om, model=0, les=1, cs=0.01, u_in=0.05, init_u=0.05,
+                  noise_amp=0.01, seed=12345, halfway=1)
+    o.step(steps)
+    err, drho = _compare(f, o.fa, mask)
+    assert err < RTOL and drho < 1e-5, (err, drho)
+    Fo = np.array(o.forces)[: len(F)]
+    assert rel_l2(F[:, 0], Fo[:, 0]) < FTOL
+    assert np.abs(F[:, 1] - Fo[:, 1]).max() < FTOL * np.abs(Fo[:, 0]).max()
+    # the flow developed past the body: the wake differs from the inlet state
+    _, j = moments(f)
+    assert np.abs(j[0][:, 40:90, 140:200] - 0.05).max() > 1e-3
+
+
+def test_c3_configured_patch_vs_oracle(product):
+    """the two-level refinement as bench.py runs it: coarse 256x128x64
+    channel with a circular cylinder of diameter 12, the configured 96x64x64
+    fine patch bounded in z, linear temporal interpolation, 1 % noise;
+    10 coarse steps (20 fine) against the oracle on both levels"""
+    import bench
+
+    lbm = product
+    steps = 10
+    with lbm.Solver(bench.c3_inputs(steps)) as s:
+        s.step(steps)
+        fc, ff, mc, mf, pr = s.populations(0), s.populations(1), s.mask(0), s.mask(1), s.params()
+    fx, fy, fz = bench.C3_PATCH["lr_dims"]
+    x0, y0, z0 = bench.C3_PATCH["lr_origin"]
+    r = Refine(cnx=256, cny=128, cnz=64, fnx=fx, fny=fy, fnz=fz, lrx0=x0, lry0=y0, lrz0=z0, lrfactor=0.5,
+               lrlevel=2, order=2, cs=0.01, omega_c=pr["omega"], omega_f=pr["omega_lr"], quirk_fc_top_zflip=1,
+               zbounded=1, cz0=int(z0))
+    o = OracleRun(256, 128, 64, mc, pr["omega"], les=1, cs=0.01, noise_amp=0.01, seed=12345,
+                  refine=dict(r=r, mask=mf, omega_f=pr["omega_lr"]), cf_time=True)
+    o.step(steps)
+    assert _compare(fc, o.fa, mc)[0] < RTOL
+    _, jf = moments(ff)
+    _, jo = moments(o.ffa)
+    assert rel_l2(jf[:, mf != 2], jo[:, mf != 2]) < RTOL

@@ -6,7 +6,8 @@ afford cudaMalloc, a plugin host that forbids allocation) use this variant of
 lbm_body_force_f32: it keeps its partial sums in a fixed array of the
 library's device memory instead of a caller-provided scratch buffer.  This
 test calls it through the C ABI twice in a row, on two different population
-states, and checks each result against the scratch-buffer entry point.  The
+states, and checks each result against the scratch-buffer entry point, then
+against the handle's own drag/lift and its accumulation into force_out.  The
 file is named to be collected last.
 """
 from __future__ import annotations
@@ -54,6 +55,42 @@ def test_noalloc_force_matches_scratch_version_twice(product):
         w, g = want.cpu().numpy(), got.cpu().numpy()
         assert np.abs(w[0]) > 0.1
         np.testing.assert_allclose(g, w, rtol=1e-12, atol=1e-12)
+
+
+def test_noalloc_force_matches_handle_and_accumulates(product):
+    """the allocation-free reduction against the handle's own drag/lift of
+    the same populations (its force history entry for the next step), and
+    its documented accumulation: two calls on a non-default stream into a
+    force_out that starts non-zero add twice the force"""
+    torch = pytest.importorskip("torch")
+    lbm = product
+    lib = lbm.library()
+    text = lbm.make_inputs(NX, NY, NZ, obst1=(20.5, 11.5, 0.0), r1=4.0, re=60.0, umax=0.05, tmax=20, les=1,
+                           cs=0.01, geometry="channel_square")
+    k = 6
+    with lbm.Solver(text) as s:
+        mask = s.mask()
+        s.step(k)
+        f = s.populations()
+        s.step(1)
+        F_handle = s.forces()[k]
+    dev = torch.device("cuda", torch.cuda.current_device())
+    m = torch.full((NZ, NY, PITCH), lbm.NODE["WALL"], dtype=torch.uint8, device=dev)
+    m[..., :NX] = torch.from_numpy(mask).to(dev)
+    fa = torch.zeros((19, NZ, NY, PITCH), dtype=torch.float32, device=dev)
+    fa[..., :NX] = torch.from_numpy(f).to(dev)
+    start = torch.tensor([1.5, -2.0, 0.25], dtype=torch.float64, device=dev)
+    got = start.clone()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    P = ctypes.c_void_p
+    for _ in range(2):
+        assert lib.lbm_body_force_f32_noalloc(P(fa.data_ptr()), P(m.data_ptr()), NX, NY, NZ, PITCH,
+                                              P(got.data_ptr()), P(side.cuda_stream)) == 0, lib.lbm_last_error()
+    side.synchronize()
+    once = (got - start).cpu().numpy() / 2
+    assert abs(F_handle[0]) > 0.1
+    np.testing.assert_allclose(once, F_handle, rtol=1e-12, atol=1e-12)
 
 
 def test_noalloc_rejects_oversized_domains(product):
