@@ -240,10 +240,16 @@ int lbm_mlp_predict(const float* d_params, const float* d_X, int n, float* d_nu,
 int lbm_mlp_train(const float* d_X, const float* d_T, int n, int batch, int steps, float lr, uint32_t seed,
                   float* params, float* loss_hist, void* stream);
 /* nu_t of n samples through the tensor-core path the collide kernels use:
- * BF16 weights and activations, FP32 accumulation (tcgen05.mma, all three
- * layers), b2 folded into W2 against the constant unit; params in host
- * memory, samples and output on the device;
- * synchronous on stream */
+ * BF16 weights and activations, FP32 accumulation (tcgen05.mma for the two
+ * hidden layers, the output layer in FP32), b2 folded into W2 against the
+ * constant unit; params in host memory, samples and output on the device;
+ * synchronous on stream.
+ * Every kernel of this library that uses tensor memory (this call,
+ * lbm_tc_selftest, steps of a handle with the learned closure, ensemble steps
+ * with it) runs on one internal stream per device, ordered after the
+ * caller's stream and before its later work, so such kernels never run side
+ * by side: two of them sharing an SM could ask for more than its 512 tensor-
+ * memory columns.  Calls from several threads are serialised by a lock. */
 int lbm_mlp_predict_tc(const float* params, const float* d_X, int n, float* d_nu, void* stream);
 /* the weight blob the tensor-core inference stages in shared memory, from
  * a parameter vector (host memory, lbm_mlp_blob_bytes() bytes):

@@ -264,8 +264,18 @@ __device__ __forceinline__ float2 psub(float2 a, float2 b) {
  * meq10 = meq12 = meq16,17,18 = 0.
  * tau0 = 1 / omega and smag_k = 18 sqrt(2) CS are the Smagorinsky constants
  * (LR7:683-685), worked out once per launch. */
-template <class T>
-__host__ __device__ __forceinline__ void collide_mrt_dev(T f[19], T omega, bool les, T tau0, T smag_k, T U) {
+/* the moments of collide_mrt_dev that the populations give: density and
+ * momentum deviations, j^2 - U^2, the stress equilibria and the
+ * non-equilibrium stress moments n1, n9, n11, n13, n14, n15 */
+template <class T> struct MrtDev {
+    T rho, jx, jy, jz, q2, U2, m9eq, m11eq, jxy, jyz, jxz, n1, n9, n11, n13, n14, n15;
+};
+
+/* The projected collision is linear in the deviation from any equilibrium of
+ * the model at rest, so it also takes full populations with U = 0 (the
+ * rest equilibrium, alpha_q rho, then cancels exactly): collide_mrt_dev(f,
+ * ..., 0) is collide_mrt<MRT> up to rounding. */
+template <class T> __host__ __device__ __forceinline__ MrtDev<T> mrt_dev_moments(const T f[19], T U) {
 #if LBM_F2_ON
     /* even and odd parts of the opposite pairs, two pairs per instruction */
     const float2 S1 = padd(make_float2(f[1], f[2]), make_float2(f[3], f[4]));
@@ -291,8 +301,10 @@ __host__ __device__ __forceinline__ void collide_mrt_dev(T f[19], T omega, bool 
     const T a13 = f[13] + f[16], b13 = f[13] - f[16];
     const T axy = a5 + a6, axz = a10 + a12, ayz = a11 + a13;
     const T sdi = axy + axz + ayz;
-    const T rho = f[0] + (sx + sy + sz) + sdi;                 /* rho - 1 */
-    const T jx = dx + (b5 - b6) + (b10 - b12);                 /* jx - U */
+    /* on deviations: rho - 1 and jx - U; on full populations (U = 0, the
+     * model's equilibrium at rest then being the offset) rho and jx */
+    const T rho = f[0] + (sx + sy + sz) + sdi;
+    const T jx = dx + (b5 - b6) + (b10 - b12);
     const T jy = dy + (b5 + b6) + (b11 - b13);
     const T jz = dz + (b10 + b12) + (b11 + b13);
     const T Jx = jx + U;                                       /* the momentum */
@@ -303,19 +315,53 @@ __host__ __device__ __forceinline__ void collide_mrt_dev(T f[19], T omega, bool 
     const T jxy = Jx * jy, jyz = jy * jz, jxz = Jx * jz;
     /* stress non-equilibrium moments (the linear parts of the deviations
      * plus those of the equilibrium at (1, U): 2 U^2 for m9, 0 else) */
+    MrtDev<T> m;
     const T n9 = (T(2) * sx - sy - sz + axy + axz - T(2) * ayz) + (T(2) * U2 - m9eq);
     const T n11 = (sy - sz + axy - axz) - m11eq;
     const T n13 = (a5 - a6) - jxy, n14 = (a11 - a13) - jyz, n15 = (a10 - a12) - jxz;
-    if (les) {
-        /* Pi_neq as collide_mrt forms it: n1 = 19 (sdi - f0 - j^2) with the
-         * equilibrium's 19 U^2 */
-        const T n1 = T(19) * ((sdi - f[0]) - q2);
-        const T tr = n1 * T(1.0 / 19.0);
-        const T pxx = n1 * T(1.0 / 57.0) + n9 * T(1.0 / 3.0);
-        const T pyy = T(0.5) * (tr - pxx + n11), pzz = T(0.5) * (tr - pxx - n11);
-        const T qn = dsqrt(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (n13 * n13 + n14 * n14 + n15 * n15));
-        omega = lrcp(T(0.5) * tau0 + T(0.5) * dsqrt(tau0 * tau0 + smag_k * qn));
-    }
+    /* n1 = 19 (sdi - f0 - j^2) with the equilibrium's 19 U^2 */
+    m.n1 = T(19) * ((sdi - f[0]) - q2);
+    m.rho = rho, m.jx = jx, m.jy = jy, m.jz = jz, m.q2 = q2, m.U2 = U2, m.m9eq = m9eq, m.m11eq = m11eq;
+    m.jxy = jxy, m.jyz = jyz, m.jxz = jxz, m.n9 = n9, m.n11 = n11, m.n13 = n13, m.n14 = n14, m.n15 = n15;
+    return m;
+}
+
+/* the non-equilibrium stress Pi_neq (xx, yy, zz, xy, xz, yz) from the
+ * moments, as collide_mrt forms it for the Smagorinsky model: Pi_xx =
+ * n1/57 + n9/3, Pi_yy + Pi_zz = n1/19 - Pi_xx, Pi_yy - Pi_zz = n11 */
+template <class T> __host__ __device__ __forceinline__ void mrt_dev_pi(const MrtDev<T>& m, T p[6]) {
+    const T tr = m.n1 * T(1.0 / 19.0);
+    p[0] = m.n1 * T(1.0 / 57.0) + m.n9 * T(1.0 / 3.0);
+    p[1] = T(0.5) * (tr - p[0] + m.n11);
+    p[2] = T(0.5) * (tr - p[0] - m.n11);
+    p[3] = m.n13;
+    p[4] = m.n15;
+    p[5] = m.n14;
+}
+
+/* the Smagorinsky relaxation rate from the moments (LR7:683-685) */
+template <class T> __host__ __device__ __forceinline__ T mrt_dev_les_omega(const MrtDev<T>& m, T tau0, T smag_k) {
+    T p[6];
+    mrt_dev_pi(m, p);
+    const T qn = dsqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2] + T(2) * (p[3] * p[3] + p[4] * p[4] + p[5] * p[5]));
+    return lrcp(T(0.5) * tau0 + T(0.5) * dsqrt(tau0 * tau0 + smag_k * qn));
+}
+
+/* the products of the moments again from rho, j and the stresses, for a
+ * caller that kept only those (fewer registers across a long wait) */
+template <class T> __host__ __device__ __forceinline__ void mrt_dev_complete(MrtDev<T>& m, T U) {
+    const T Jx = m.jx + U;
+    const T jxx = Jx * Jx, jyy = m.jy * m.jy, jzz = m.jz * m.jz;
+    m.U2 = U * U;
+    m.q2 = (jxx - m.U2) + (jyy + jzz);
+    m.m9eq = T(2) * jxx - (jyy + jzz), m.m11eq = jyy - jzz;
+    m.jxy = Jx * m.jy, m.jyz = m.jy * m.jz, m.jxz = Jx * m.jz;
+}
+
+/* the post-collision deviations at the stress relaxation rate omega */
+template <class T> __host__ __device__ __forceinline__ void mrt_dev_relax(T f[19], const MrtDev<T>& m, T omega) {
+    const T rho = m.rho, jx = m.jx, jy = m.jy, jz = m.jz, q2 = m.q2, U2 = m.U2, m9eq = m.m9eq, m11eq = m.m11eq;
+    const T jxy = m.jxy, jyz = m.jyz, jxz = m.jxz, n9 = m.n9, n11 = m.n11, n13 = m.n13, n14 = m.n14, n15 = m.n15;
     const T c1 = T(1) - omega;
     /* post-collision stresses less their value at (1, U), over the row norms */
     const T t9 = ((m9eq - T(2) * U2) + c1 * n9) * T(1.0 / 36.0);
@@ -379,6 +425,13 @@ __host__ __device__ __forceinline__ void collide_mrt_dev(T f[19], T omega, bool 
     f[13] = e13 + o13;
     f[16] = e13 - o13;
 #endif
+}
+
+template <class T>
+__host__ __device__ __forceinline__ void collide_mrt_dev(T f[19], T omega, bool les, T tau0, T smag_k, T U) {
+    const MrtDev<T> m = mrt_dev_moments(f, U);
+    if (les) omega = mrt_dev_les_omega(m, tau0, smag_k);
+    mrt_dev_relax(f, m, omega);
 }
 
 /* BGK with the incompressible equilibrium w (rho + 3 c.j + 4.5 (c.j)^2 - 1.5 j^2)

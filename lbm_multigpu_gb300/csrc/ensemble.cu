@@ -82,6 +82,7 @@ __global__ void __launch_bounds__(32 * TY) k_ens_step(const Table T, const float
             for (int k = 0; k < 6; ++k) p6[k] *= s;
             sgs::features_fast(p6, M.tau0, M.omega, xf); /* omega = 1 / tau0 */
             const float nu = sgs::infer_nu<ROWS>(smem, xf, err);
+            if (nu < 0.f) break; /* a tensor-core wait ran out (block-uniform) */
             omega = 1.f / (M.tau0 + 3.f * nu);
         }
         collide_mrt<MRT>(f, omega, SGS == SGS_SMAG, cs, 0.f);
@@ -319,6 +320,13 @@ template <int TY, int SGS> static cudaError_t step_attr() {
 template <int TY, int SGS> static cudaError_t step_t(const ens::Table& T, const float* fA, float* fB,
                                                     const void* blob, float cs, int* err, int grid, cudaStream_t s) {
     if (cudaError_t e = step_attr<TY, SGS>()) return e;
+    if (SGS == ens::SGS_MLP) {
+        TmemLane lane(s);
+        if (lane.status() != cudaSuccess) return lane.status();
+        ens::k_ens_step<TY, SGS><<<grid, 32 * TY, step_smem<TY, SGS>(), lane.stream()>>>(
+            T, fA, fB, (const unsigned char*)blob, cs, err);
+        return cudaGetLastError();
+    }
     ens::k_ens_step<TY, SGS><<<grid, 32 * TY, step_smem<TY, SGS>(), s>>>(T, fA, fB, (const unsigned char*)blob, cs,
                                                                          err);
     return cudaGetLastError();

@@ -114,6 +114,7 @@ cudaError_t one_step(lbm_ensemble* e) {
 cudaError_t build_graph(lbm_ensemble* e) {
     drop_graph(e);
     cudaGraph_t g = nullptr;
+    if (cudaError_t r0 = lbm::TmemLane::prepare()) return r0;
     cudaError_t r = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
     if (r != cudaSuccess) return r;
     const int saved = e->cur;

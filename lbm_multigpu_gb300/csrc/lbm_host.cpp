@@ -571,7 +571,6 @@ struct lbm_handle {
      * stream: forked after the previous step, joined before the next */
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    cudaEvent_t ev_cf_fork = nullptr, ev_cf_join = nullptr; /* CF TIME linear: the last band fill beside InterpFC */
     /* refinement steps are launch-bound (a dozen small launches and events
      * each): lbm_step captures batches of steps into one CUDA graph, updated
      * in place from batch to batch (uniform runs too: it removes the gaps
@@ -587,6 +586,7 @@ struct lbm_handle {
     unsigned char* mlp_blob = nullptr;
     int* mlp_err = nullptr;
     bool mlp_ready = false;
+    bool mlp_warm = false;         /* a closure step ran directly: its launcher is set up */
     std::vector<float> mlp_params; /* host copy, for checkpoints */
     /* dynamic inlet: the body force on the device, the control history
      * (t, mean v, dpdy per control step) and whether the trip is in the mask */
@@ -844,9 +844,11 @@ int one_step(lbm_handle* h) {
         blend = h->have_mom;
         h->have_mom = true;
     }
-    if (c.sgs_mlp)
+    if (c.sgs_mlp) {
         CUDA_TRY(launch_stream_collide_mlp(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, C.links, h->mlp_blob,
                                            h->mlp_err, h->stream));
+        h->mlp_warm = true;
+    }
     else
         CUDA_TRY(launch_stream_collide(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, h->mom, h->stream,
                                        C.links));
@@ -885,23 +887,11 @@ int one_step(lbm_handle* h) {
             if (pf.force_on) CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
             Fn.cur = 1 - Fn.cur;
         }
-        if (c.cf_time) {
-            /* the band fill and the restriction touch disjoint fine nodes
-             * (band vs children of the interior with its 2-node margin) and
-             * the next coarse step exports into the other buffer: the fill
-             * runs on the second stream beside the restriction, joined
-             * before the step ends */
-            CUDA_TRY(cudaEventRecord(h->ev_cf_fork, h->stream));
-            CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_cf_fork, 0));
-            CUDA_TRY(launch_interp_cf(h->rp, Fn.L, h->mom, Fn.f[Fn.cur], Fn.mask, h->side));
-            CUDA_TRY(cudaEventRecord(h->ev_cf_join, h->side));
-            CUDA_TRY(launch_interp_fc(h->rp, C.L, Fn.L, Fn.f[Fn.cur], C.f[C.cur], C.mask, h->stream));
-            CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_cf_join, 0));
-        } else {
-            CUDA_TRY(launch_interp_cf(h->rp, Fn.L, h->mom, Fn.f[Fn.cur], Fn.mask, h->stream));
-            CUDA_TRY(launch_interp_fc(h->rp, C.L, Fn.L, Fn.f[Fn.cur], C.f[C.cur], C.mask, h->stream));
-        }
-        h->launches += 2;
+        /* the band fill at the end of the coarse step and the restriction
+         * touch disjoint nodes (band vs the coarse nodes over the interior
+         * with its 2-node margin): one launch */
+        CUDA_TRY(launch_interface(h->rp, C.L, Fn.L, h->mom, Fn.f[Fn.cur], Fn.mask, C.f[C.cur], C.mask, h->stream));
+        ++h->launches;
     }
     h->t = t + 1;
     return LBM_OK;
@@ -911,10 +901,11 @@ constexpr int GRAPH_STEPS = 16; /* steps per captured graph */
 
 /* k steps from h->t on can be captured: their steps call nothing that
  * synchronises (the trip leaving the mask does) or sets kernel attributes
- * on first use (the learned-closure launcher does) */
+ * and creates the tensor-memory lane on first use (the learned-closure
+ * launcher does, in the direct step before the first batch) */
 bool graph_ok(const lbm_handle* h, int k) {
     const Config& c = h->cfg;
-    if (c.sgs_mlp) return false;
+    if (c.sgs_mlp && !h->mlp_warm) return false;
     if (h->trip_in_mask && h->t + k - 1 >= c.trip_end) return false;
     return true;
 }
@@ -1150,9 +1141,7 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
         cudaDeviceGetStreamPriorityRange(&lo, &hi);
         if (cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, hi) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&h->ev_cf_fork, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&h->ev_cf_join, cudaEventDisableTiming) != cudaSuccess)
+            cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess)
             return bail(fail(LBM_ERR_CUDA, "cannot create the force stream"));
     }
     /* reference velocity of the FP16/BF16 offsets: the inlet velocity of a channel */
@@ -1228,8 +1217,6 @@ int lbm_destroy(lbm_handle* h) {
     cudaFree(h->dyn_hist);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
-    if (h->ev_cf_fork) cudaEventDestroy(h->ev_cf_fork);
-    if (h->ev_cf_join) cudaEventDestroy(h->ev_cf_join);
     for (cudaGraphExec_t& g : h->gexec)
         if (g) cudaGraphExecDestroy(g);
     cudaFree(h->stage);

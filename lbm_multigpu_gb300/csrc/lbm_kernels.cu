@@ -6,6 +6,7 @@
  * the FP64 audit, DI3's inlet control and the refinement exchange.
  */
 #include <algorithm>
+#include <mutex>
 
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -338,16 +339,23 @@ __device__ __forceinline__ void second_order(const float mc[8][9], const float S
  * thread per band node; mom_c is [9][cnz][eny][enx] (coarse footprint).
  * With mom_prev (the previous coarse step's export) the corner moments are
  * first interpolated in time, (1 - theta) prev + theta cur. */
+/* band nodes of the coarse-to-fine fill */
+inline long long cf_nodes(const RefineParams& r) {
+    const int L = r.lrlevel;
+    return (long long)(r.fny * 2 * L + (r.fnx - 2 * L) * 2 * L) * r.fnz +
+           (r.zbounded ? 2LL * L * (r.fnx - 2 * L) * (r.fny - 2 * L) : 0LL);
+}
+
+/* the band node idx of the coarse-to-fine fill */
 template <class S>
-__global__ void k_interp_cf(const RefineParams r, const Level F, const float* __restrict__ mom_c,
-                            const float* __restrict__ mom_prev, float theta, S* __restrict__ f_f,
-                            const uint8_t* __restrict__ mask_f) {
+__device__ __forceinline__ void interp_cf_node(const RefineParams& r, const Level& F, const float* __restrict__ mom_c,
+                                               const float* __restrict__ mom_prev, float theta, S* __restrict__ f_f,
+                                               const uint8_t* __restrict__ mask_f, const long long idx) {
     const int L = r.lrlevel;
     const int nb_x = r.fny * 2 * L;                /* x-band nodes per plane */
     const int nb_y = (r.fnx - 2 * L) * 2 * L;      /* y-band nodes per plane (x-band excluded) */
     const int per_plane = nb_x + nb_y;
     const int inner = (r.fnx - 2 * L) * (r.fny - 2 * L);  /* z-band nodes per plane (bounded patch) */
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long nxy = (long long)per_plane * r.fnz;
     if (idx >= nxy + (r.zbounded ? 2LL * L * inner : 0LL)) return;
     int k, xf, yf;
@@ -437,16 +445,26 @@ __global__ void k_interp_cf(const RefineParams r, const Level F, const float* __
     for (int q = 0; q < 19; ++q) Fmt<S>::st(f_f + pidx(F, q, unsigned(cf)), g[q], F.off[q]);
 }
 
+template <class S>
+__global__ void k_interp_cf(const RefineParams r, const Level F, const float* __restrict__ mom_c,
+                            const float* __restrict__ mom_prev, float theta, S* __restrict__ f_f,
+                            const uint8_t* __restrict__ mask_f) {
+    interp_cf_node<S>(r, F, mom_c, mom_prev, theta, f_f, mask_f, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+/* the coarse nodes strictly inside the patch that the restriction replaces:
+ * x0 .. x0 + nxi - 1 and likewise in y and z */
+struct FcBox {
+    int x0, y0, z0, nxi, nyi, nzi;
+};
+
 /* InterpFC (LR7:2172-2348): coarse nodes strictly inside the patch (2-node
  * margin) are replaced by the restriction of their 8 fine children. */
 template <class S>
-__global__ void k_interp_fc(const RefineParams r, const Level C, const Level F, const S* __restrict__ f_f,
-                            S* __restrict__ f_c, const uint8_t* __restrict__ mask_c, int x0, int y0, int nxi, int nyi,
-                            int z0) {
-    const int xi = blockIdx.x * blockDim.x + threadIdx.x, yi = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = z0 + int(blockIdx.z);
-    if (xi >= nxi || yi >= nyi) return;
-    const int x = x0 + xi, y = y0 + yi;
+__device__ __forceinline__ void interp_fc_node(const RefineParams& r, const Level& C, const Level& F,
+                                               const S* __restrict__ f_f, S* __restrict__ f_c,
+                                               const uint8_t* __restrict__ mask_c, const int x, const int y,
+                                               const int z) {
     const long long cc = z * C.plane + (long long)y * C.pitch + x;
     const int t = mask_c[cc] & TYPE_MASK;
     if (t == WALL || t == BODY) return;
@@ -504,6 +522,37 @@ __global__ void k_interp_fc(const RefineParams r, const Level C, const Level F, 
     for (int q = 0; q < 19; ++q) Fmt<S>::st(f_c + pidx(C, q, unsigned(cc)), g[q], C.off[q]);
 }
 
+template <class S>
+__global__ void k_interp_fc(const RefineParams r, const Level C, const Level F, const S* __restrict__ f_f,
+                            S* __restrict__ f_c, const uint8_t* __restrict__ mask_c, const FcBox b) {
+    const int xi = blockIdx.x * blockDim.x + threadIdx.x, yi = blockIdx.y * blockDim.y + threadIdx.y;
+    if (xi >= b.nxi || yi >= b.nyi) return;
+    interp_fc_node<S>(r, C, F, f_f, f_c, mask_c, b.x0 + xi, b.y0 + yi, b.z0 + int(blockIdx.z));
+}
+
+/* the final band fill of a coarse step and the restriction in one launch:
+ * they touch disjoint nodes (the band, and the coarse nodes over the
+ * patch's interior with its 2-node margin), so the first cf_blocks blocks
+ * fill the band and the others restrict, one coarse node per thread */
+constexpr int IFACE_THREADS = 128;
+template <class S>
+__global__ void __launch_bounds__(IFACE_THREADS) k_interface(const RefineParams r, const Level C, const Level F,
+                                                             const float* __restrict__ mom_c, S* __restrict__ f_f,
+                                                             const uint8_t* __restrict__ mask_f, S* __restrict__ f_c,
+                                                             const uint8_t* __restrict__ mask_c, const FcBox b,
+                                                             int cf_blocks) {
+    if (int(blockIdx.x) < cf_blocks) {
+        interp_cf_node<S>(r, F, mom_c, nullptr, 1.f, f_f, mask_f,
+                          (long long)blockIdx.x * IFACE_THREADS + threadIdx.x);
+        return;
+    }
+    const long long i = (long long)(blockIdx.x - cf_blocks) * IFACE_THREADS + threadIdx.x;
+    const long long per_plane = (long long)b.nxi * b.nyi;
+    if (i >= per_plane * b.nzi) return;
+    const int zi = int(i / per_plane), rem = int(i - zi * per_plane);
+    interp_fc_node<S>(r, C, F, f_f, f_c, mask_c, b.x0 + rem % b.nxi, b.y0 + rem / b.nxi, b.z0 + zi);
+}
+
 /* ---- launchers ---- */
 
 #define LBM_DISPATCH(storage, KERNEL_CALL)                   \
@@ -514,6 +563,46 @@ __global__ void k_interp_fc(const RefineParams r, const Level C, const Level F, 
         case STORE_F64: { using S = double; KERNEL_CALL; } break;           \
         default: return cudaErrorInvalidValue;                \
     }
+
+/* ---- the tensor-memory lane: one stream and two events per device,
+ * created on first use and kept for the life of the process */
+namespace {
+constexpr int LANE_DEVICES = 64;
+std::mutex g_lane_mu[LANE_DEVICES];
+cudaStream_t g_lane[LANE_DEVICES] = {};
+cudaEvent_t g_lane_in[LANE_DEVICES] = {}, g_lane_out[LANE_DEVICES] = {};
+}  // namespace
+
+TmemLane::TmemLane(cudaStream_t caller) : caller_(caller) {
+    if ((err_ = cudaGetDevice(&dev_)) != cudaSuccess) return;
+    if (dev_ < 0 || dev_ >= LANE_DEVICES) {
+        err_ = cudaErrorInvalidDevice;
+        dev_ = -1;
+        return;
+    }
+    g_lane_mu[dev_].lock();
+    if (!g_lane[dev_]) {
+        if ((err_ = cudaStreamCreateWithFlags(&g_lane[dev_], cudaStreamNonBlocking)) != cudaSuccess ||
+            (err_ = cudaEventCreateWithFlags(&g_lane_in[dev_], cudaEventDisableTiming)) != cudaSuccess ||
+            (err_ = cudaEventCreateWithFlags(&g_lane_out[dev_], cudaEventDisableTiming)) != cudaSuccess)
+            return;
+    }
+    lane_ = g_lane[dev_];
+    done_ = g_lane_out[dev_];
+    if ((err_ = cudaEventRecord(g_lane_in[dev_], caller_)) == cudaSuccess)
+        err_ = cudaStreamWaitEvent(lane_, g_lane_in[dev_], 0);
+}
+
+cudaError_t TmemLane::prepare() {
+    TmemLane lane(nullptr);
+    return lane.status();
+}
+
+TmemLane::~TmemLane() {
+    if (dev_ < 0) return;
+    if (lane_ && cudaEventRecord(done_, lane_) == cudaSuccess) cudaStreamWaitEvent(caller_, done_, 0);
+    g_lane_mu[dev_].unlock();
+}
 
 cudaError_t launch_stream_collide(const Level& L, const StepParams& p, const void* fA, void* fB, const uint8_t* mask,
                                   float* stats, float* mom_export, cudaStream_t s, const uint32_t* links) {
@@ -530,8 +619,10 @@ cudaError_t launch_stream_collide_mlp(const Level& L, const StepParams& p, const
                                       int* err, cudaStream_t s) {
     if ((p.halfway && !links) || !blob || !err || p.has_lid || p.has_xbc || p.pull_clamp || p.exp_nx > 0)
         return cudaErrorInvalidValue;
-    if (L.blocked) return launch_sc_mlp_blocked(L, p, fA, fB, mask, stats, links, blob, err, s);
-    return launch_sc_mlp_layout<0>(L, p, fA, fB, mask, stats, links, blob, err, s);
+    TmemLane lane(s);
+    if (lane.status() != cudaSuccess) return lane.status();
+    if (L.blocked) return launch_sc_mlp_blocked(L, p, fA, fB, mask, stats, links, blob, err, lane.stream());
+    return launch_sc_mlp_layout<0>(L, p, fA, fB, mask, stats, links, blob, err, lane.stream());
 }
 
 cudaError_t launch_dyn_control(const Level& L, const void* f, int y1, float umax, float kp, float dpdy0_abs,
@@ -648,9 +739,7 @@ cudaError_t launch_audit(const Level& L, const void* f, const uint8_t* mask, dou
 
 cudaError_t launch_interp_cf(const RefineParams& r, const Level& F, const float* mom_c, void* f_f,
                              const uint8_t* mask_f, cudaStream_t s, const float* mom_prev, float theta) {
-    const int L = r.lrlevel;
-    const long long n = (long long)(r.fny * 2 * L + (r.fnx - 2 * L) * 2 * L) * r.fnz +
-                        (r.zbounded ? 2LL * L * (r.fnx - 2 * L) * (r.fny - 2 * L) : 0LL);
+    const long long n = cf_nodes(r);
     const int threads = 128;
     const unsigned blocks = unsigned((n + threads - 1) / threads);
     LBM_DISPATCH(F.storage,
@@ -658,9 +747,10 @@ cudaError_t launch_interp_cf(const RefineParams& r, const Level& F, const float*
     return cudaGetLastError();
 }
 
-cudaError_t launch_interp_fc(const RefineParams& r, const Level& C, const Level& F, const void* f_f, void* f_c,
-                             const uint8_t* mask_c, cudaStream_t s) {
-    /* coarse x with x > lrx0 + 1 and x < lrx0 + fnx*lrfactor - 2 (same for y) */
+/* the coarse nodes the restriction replaces: x with x > lrx0 + 1 and
+ * x < lrx0 + fnx lrfactor - 2, the same in y, and in z every plane of a
+ * full-depth patch or, for a bounded one, as in x and y */
+static FcBox fc_box(const RefineParams& r, const Level& C) {
     int x0 = 0, x1 = -1, y0 = 0, y1 = -1;
     for (int x = 0; x < C.nx; ++x)
         if (x > r.lrx0 + 1 && x < r.lrx0 + r.fnx * r.lrfactor - 2) {
@@ -672,7 +762,6 @@ cudaError_t launch_interp_fc(const RefineParams& r, const Level& C, const Level&
             if (y1 < y0) y0 = y;
             y1 = y;
         }
-    /* z: every plane of a full-depth patch; a bounded one as x and y */
     int z0 = 0, z1 = C.nz - 1;
     if (r.zbounded) {
         z1 = -1;
@@ -682,11 +771,29 @@ cudaError_t launch_interp_fc(const RefineParams& r, const Level& C, const Level&
                 z1 = z;
             }
     }
-    const int nxi = x1 - x0 + 1, nyi = y1 - y0 + 1, nzi = z1 - z0 + 1;
-    if (nxi <= 0 || nyi <= 0 || nzi <= 0) return cudaSuccess;
-    const dim3 block(32, 4), grid((nxi + 31) / 32, (nyi + 3) / 4, nzi);
-    LBM_DISPATCH(C.storage, (k_interp_fc<S><<<grid, block, 0, s>>>(r, C, F, (const S*)f_f, (S*)f_c, mask_c, x0, y0,
-                                                                    nxi, nyi, z0)));
+    FcBox b{x0, y0, z0, x1 - x0 + 1, y1 - y0 + 1, z1 - z0 + 1};
+    if (b.nxi <= 0 || b.nyi <= 0 || b.nzi <= 0) b.nxi = b.nyi = b.nzi = 0;
+    return b;
+}
+
+cudaError_t launch_interp_fc(const RefineParams& r, const Level& C, const Level& F, const void* f_f, void* f_c,
+                             const uint8_t* mask_c, cudaStream_t s) {
+    const FcBox b = fc_box(r, C);
+    if (b.nxi == 0) return cudaSuccess;
+    const dim3 block(32, 4), grid((b.nxi + 31) / 32, (b.nyi + 3) / 4, b.nzi);
+    LBM_DISPATCH(C.storage, (k_interp_fc<S><<<grid, block, 0, s>>>(r, C, F, (const S*)f_f, (S*)f_c, mask_c, b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_interface(const RefineParams& r, const Level& C, const Level& F, const float* mom_c, void* f_f,
+                             const uint8_t* mask_f, void* f_c, const uint8_t* mask_c, cudaStream_t s) {
+    if (C.storage != F.storage) return cudaErrorInvalidValue;
+    const FcBox b = fc_box(r, C);
+    const int cf_blocks = int((cf_nodes(r) + IFACE_THREADS - 1) / IFACE_THREADS);
+    const long long nfc = (long long)b.nxi * b.nyi * b.nzi;
+    const unsigned blocks = unsigned(cf_blocks + (nfc + IFACE_THREADS - 1) / IFACE_THREADS);
+    LBM_DISPATCH(C.storage, (k_interface<S><<<blocks, IFACE_THREADS, 0, s>>>(r, C, F, mom_c, (S*)f_f, mask_f, (S*)f_c,
+                                                                             mask_c, b, cf_blocks)));
     return cudaGetLastError();
 }
 

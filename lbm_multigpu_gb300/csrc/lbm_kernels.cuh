@@ -178,6 +178,33 @@ cudaError_t launch_force_scan(const Level& L, const void* fA, const uint8_t* mas
                               cudaStream_t s);
 int force_scan_partials();
 
+/* The tensor-memory lane of the current device.  Every kernel of this
+ * library that allocates tensor memory (TMEM) is launched on one stream per
+ * device, ordered after the caller's stream and before the caller's later
+ * work by events, so that no two of them run at the same time on a device.
+ * Each such kernel sizes its shared memory so that its own resident blocks
+ * never ask an SM for more than its 512 TMEM columns; two different ones
+ * side by side could, and tcgen05.alloc would then wait for columns.  The
+ * lane is held (a host mutex) from construction to destruction. */
+class TmemLane {
+public:
+    explicit TmemLane(cudaStream_t caller);
+    ~TmemLane();
+    TmemLane(const TmemLane&) = delete;
+    TmemLane& operator=(const TmemLane&) = delete;
+    cudaStream_t stream() const { return lane_; }
+    cudaError_t status() const { return err_; }
+    /* creates the current device's lane, before any stream capture that
+     * will use it */
+    static cudaError_t prepare();
+
+private:
+    cudaStream_t caller_ = nullptr, lane_ = nullptr;
+    cudaEvent_t done_ = nullptr;
+    int dev_ = -1;
+    cudaError_t err_ = cudaSuccess;
+};
+
 /* record an error for lbm_last_error(); returns code (lbm_host.cpp) */
 int set_error(int code, const char* what, cudaError_t e);
 /* axis: direction of the initial velocity u0 (0 x, 1 y, 2 z) */
@@ -219,6 +246,10 @@ cudaError_t launch_interp_cf(const RefineParams& r, const Level& F, const float*
                              float theta = 1.f);
 cudaError_t launch_interp_fc(const RefineParams& r, const Level& C, const Level& F, const void* f_f, void* f_c,
                              const uint8_t* mask_c, cudaStream_t s);
+/* the final band fill of a coarse step (from mom_c alone) and the
+ * restriction in one launch (they touch disjoint nodes) */
+cudaError_t launch_interface(const RefineParams& r, const Level& C, const Level& F, const float* mom_c, void* f_f,
+                             const uint8_t* mask_f, void* f_c, const uint8_t* mask_c, cudaStream_t s);
 
 /* learned subgrid closure (sgs_mlp.cu) */
 int mlp_grad_blocks(int n);

@@ -464,8 +464,16 @@ __global__ void __launch_bounds__(SC_BX* SC_BY, sc_min_blocks<FEAT>()) k_stream_
  * that each block stages the weights and allocates its TMEM once per launch.
  * MRT collision (LR7:583-711) at tau_eff = tau0 + 3 nu_t; FP32 arithmetic. */
 constexpr int MLP_BY = 4; /* tile 32 x 4: one M = 128 MMA per layer */
+/* resident blocks per SM the closure kernel is compiled for */
+#ifndef LBM_MLP_MINB
+#define LBM_MLP_MINB 7
+#endif
+/* issue the next tile's pulls before this tile's tensor-core round trips */
+#ifndef LBM_MLP_PREFETCH
+#define LBM_MLP_PREFETCH 0
+#endif
 template <class S, bool HALFWAY, int LAY>
-__global__ void __launch_bounds__(SC_BX* MLP_BY, 6) k_stream_collide_mlp(const Level L, const StepParams p,
+__global__ void __launch_bounds__(SC_BX* MLP_BY, LBM_MLP_MINB) k_stream_collide_mlp(const Level L, const StepParams p,
                                                                       const S* __restrict__ fA, S* __restrict__ fB,
                                                                       const uint8_t* __restrict__ mask,
                                                                       float* __restrict__ stats,
@@ -484,23 +492,53 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, 6) k_stream_collide_mlp(const L
     const int tiles_x = L.pitch / SC_BX, tiles_y = (L.ny + MLP_BY - 1) / MLP_BY;
     const int ntiles = tiles_x * tiles_y * L.nz;
     const float tau0 = 1.f / p.omega, inv_t0 = p.omega;
+    /* the node of this thread in tile g */
+    auto node_of = [&](int g, int& x, int& y, int& z) {
+        z = g / (tiles_x * tiles_y);
+        const int r = g - z * tiles_x * tiles_y;
+        x = (r % tiles_x) * SC_BX + int(threadIdx.x);
+        y = (r / tiles_x) * MLP_BY + int(threadIdx.y);
+    };
+    auto node_idx = [&](int x, int y, int z) {
+        const unsigned xm = (x == 0) ? L.nx - 1 : x - 1, xp = (x == L.nx - 1) ? 0 : x + 1;
+        const unsigned ym = (y == 0) ? L.ny - 1 : y - 1, yp = (y == L.ny - 1) ? 0 : y + 1;
+        const unsigned zm = (z == 0) ? L.nz - 1 : z - 1, zp = (z == L.nz - 1) ? 0 : z + 1;
+        return NodeIdx<LAY>(L, xm, unsigned(x), xp, ym, unsigned(y), yp, zm, unsigned(z), zp);
+    };
+    /* the 19 pulls of tile g, issued one tile ahead: they are in flight
+     * while the current tile runs its three tensor-core round trips */
+    float fn[19];
+    auto prefetch = [&](int g) {
+        int x, y, z;
+        node_of(g, x, y, z);
+        if (x < L.nx && y < L.ny) {
+            const NodeIdx<LAY> nn = node_idx(x, y, z);
+#pragma unroll
+            for (int q = 0; q < 19; ++q) fn[q] = F::ld(nn.pull(fA, q), L.off[q]);
+        }
+    };
+    if (LBM_MLP_PREFETCH && int(blockIdx.x) < ntiles) prefetch(blockIdx.x);
     for (int g = blockIdx.x; g < ntiles; g += gridDim.x) {
-        const int z = g / (tiles_x * tiles_y), r = g - z * tiles_x * tiles_y;
-        const int x = (r % tiles_x) * SC_BX + int(threadIdx.x), y = (r / tiles_x) * MLP_BY + int(threadIdx.y);
+        int x, y, z;
+        node_of(g, x, y, z);
         const bool live = x < L.nx && y < L.ny;
         float f[19];
         int type = FLUID;
         unsigned c = 0;
         const unsigned xm = (x == 0) ? L.nx - 1 : x - 1, xp = (x == L.nx - 1) ? 0 : x + 1;
         const unsigned ym = (y == 0) ? L.ny - 1 : y - 1, yp = (y == L.ny - 1) ? 0 : y + 1;
-        const unsigned zm = (z == 0) ? L.nz - 1 : z - 1, zp = (z == L.nz - 1) ? 0 : z + 1;
-        const NodeIdx<LAY> n(L, xm, unsigned(x), xp, ym, unsigned(y), yp, zm, unsigned(z), zp);
+        const NodeIdx<LAY> n = node_idx(x, y, z);
         if (live) {
             c = unsigned(z) * plane + unsigned(y) * pitch + unsigned(x);
             const int mbyte = mask[c];
             type = mbyte & TYPE_MASK;
+            if (LBM_MLP_PREFETCH) {
 #pragma unroll
-            for (int q = 0; q < 19; ++q) f[q] = F::ld(n.pull(fA, q), L.off[q]);
+                for (int q = 0; q < 19; ++q) f[q] = fn[q];
+            } else {
+#pragma unroll
+                for (int q = 0; q < 19; ++q) f[q] = F::ld(n.pull(fA, q), L.off[q]);
+            }
             if (HALFWAY && (mbyte & NEAR_SOLID)) {
                 const uint32_t lk = links[c];
 #pragma unroll
@@ -524,23 +562,38 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, 6) k_stream_collide_mlp(const L
 #pragma unroll
             for (int q = 0; q < 19; ++q) f[q] = wq(q);
         }
-        /* the closure for the whole tile */
-        float rho, p6[6], xf[sgs::NIN];
-        pi_neq<float>(f, rho, p6);
-        const float sc = -1.5f / rho;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) p6[k] *= sc;
-        sgs::features_fast(p6, tau0, inv_t0, xf);
-        const float nu = sgs::infer_nu<ROWS>(sm, xf, err);
-        if (!live) continue;
-        if (type == WALL || type == BODY) {
+        /* bounce-back nodes are done before the closure, so that only the
+         * moments stay live across its tensor-core round trips */
+        const bool solid = live && (type == WALL || type == BODY);
+        if (solid) {
             float gb[19];
 #pragma unroll
             for (int q = 0; q < 19; ++q) gb[q] = f[opp(q)];
             store19<S, LAY, false>(L, fB, n, gb);
-            continue;
         }
-        collide_mrt<MRT>(f, 1.f / (tau0 + 3.f * nu), false, 0.f, 0.f);
+        /* the closure for the whole tile; the collision's moments give
+         * Pi_neq (the projected MRT collision on full populations) */
+        const MrtDev<float> mo = mrt_dev_moments<float>(f, 0.f);
+        float p6[6], xf[sgs::NIN];
+        mrt_dev_pi(mo, p6);
+        const float sc = -1.5f / mo.rho;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) p6[k] *= sc;
+        sgs::features_fast(p6, tau0, inv_t0, xf);
+        if (LBM_MLP_PREFETCH && g + int(gridDim.x) < ntiles) prefetch(g + int(gridDim.x));
+        /* across the tensor-core round trips only rho, j and the five
+         * stresses stay live; the products are formed again afterwards */
+        float keep[9] = {mo.rho, mo.jx, mo.jy, mo.jz, mo.n9, mo.n11, mo.n13, mo.n14, mo.n15};
+        const float nu = sgs::infer_nu<ROWS>(sm, xf, err);
+        if (nu < 0.f) break; /* a tensor-core wait ran out (block-uniform) */
+        if (!live || solid) continue;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) asm volatile("" : "+f"(keep[k]));
+        MrtDev<float> mr;
+        mr.rho = keep[0], mr.jx = keep[1], mr.jy = keep[2], mr.jz = keep[3], mr.n9 = keep[4], mr.n11 = keep[5];
+        mr.n13 = keep[6], mr.n14 = keep[7], mr.n15 = keep[8], mr.n1 = 0.f;
+        mrt_dev_complete(mr, 0.f);
+        mrt_dev_relax(f, mr, 1.f / (tau0 + 3.f * nu));
         if (p.stats_on && p.t >= p.start_av) {
             float u = 0, v = 0;
 #pragma unroll

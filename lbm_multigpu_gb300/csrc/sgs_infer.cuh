@@ -1,16 +1,18 @@
 /* Tensor-core inference of the learned subgrid closure, for use inside a
  * kernel whose block of ROWS threads (ROWS = 128 or 256) each holds one
- * node's 16 features.  One call evaluates the MLP for the whole block, all
- * three layers on the tensor core:
+ * node's 16 features.  One call evaluates the MLP for the whole block, the
+ * two hidden layers on the tensor core:
  *
  *   features -> bf16 -> shared memory (A operand, core-matrix layout)
  *   layer 1:  tcgen05.mma  Z1[ROWS][64] = X[ROWS][16] W1^T       (TMEM, FP32)
  *   tcgen05.ld -> ReLU + bf16 pack (one cvt per pair) -> shared memory
  *   layer 2:  tcgen05.mma  Z2[ROWS][64] = H1[ROWS][64] W2^T, 4 K-steps
  *             (b2 rides in column HC against the constant unit h1[HC] = 1)
- *   tcgen05.ld -> ReLU + bf16 pack -> shared memory (over H1)
- *   layer 3:  tcgen05.mma  Y[ROWS][16] = H2[ROWS][64] W3^T (row 0 of W3 = w3)
- *   tcgen05.ld of column 0 -> + b3 -> softplus -> nu_t
+ *   tcgen05.ld -> y = b3 + w3 . ReLU(z2) in FP32 on the CUDA cores
+ *             (LBM_INFER_L3CC; else ReLU + bf16 pack -> shared memory and
+ *             layer 3 as tcgen05.mma Y[ROWS][16] = H2[ROWS][64] W3^T with
+ *             row 0 of W3 = w3, column 0 read back)
+ *   -> softplus -> nu_t
  *
  * Thread t of the block owns row t: MMA h = t / 128 covers rows 128 h ..
  * 128 h + 127 in TMEM lanes 0..127 of columns 64 h .. 64 h + 63, and warp w
@@ -48,16 +50,30 @@ template <int ROWS> struct InferSmem;
  * can serve (512 columns) fit on one SM */
 template <int ROWS> inline size_t infer_dyn_smem();
 
+/* the output layer (64 -> 1) on the CUDA cores from the layer-2
+ * accumulators in registers (one tensor-core round trip fewer), or as an
+ * N = 16 MMA */
+#ifndef LBM_INFER_L3CC
+#define LBM_INFER_L3CC 1
+#endif
+
 template <int ROWS> struct InferSmem {
     alignas(1024) unsigned char w1[W1_BYTES];
     alignas(1024) unsigned char w2[W2_BYTES];
+#if !LBM_INFER_L3CC
     alignas(1024) unsigned char w3[W3_BYTES];
-    alignas(1024) unsigned char a1[ROWS * NIN * 2];
-    alignas(1024) unsigned char a2[ROWS * NH * 2]; /* h1, then h2 */
+#endif
+    /* the layer-1 A operand (features, ROWS x 16 bf16) at the start, then
+     * h1, then h2 (h1 is written only after the layer-1 MMA has read x) */
+    alignas(1024) unsigned char a2[ROWS * NH * 2];
+    alignas(16) float w3f[NH];
     float b3;
     alignas(8) uint64_t mbar;
     uint32_t tmem;
     uint32_t phase;
+    /* a completion wait ran out: no further MMA is issued by this block,
+     * and failed_parity is the completion still outstanding */
+    uint32_t failed, failed_parity;
 };
 
 /* TMEM columns a block holds: 64 per 128 rows */
@@ -96,12 +112,21 @@ template <int ROWS> __device__ __forceinline__ void infer_setup(InferSmem<ROWS>&
     for (int i = t; i < int(W1_BYTES / 16); i += ROWS) reinterpret_cast<uint4*>(s.w1)[i] = src[i];
     for (int i = t; i < int(W2_BYTES / 16); i += ROWS)
         reinterpret_cast<uint4*>(s.w2)[i] = src[BLOB_W2 / 16 + i];
+#if !LBM_INFER_L3CC
     for (int i = t; i < int(W3_BYTES / 16); i += ROWS)
         reinterpret_cast<uint4*>(s.w3)[i] = src[BLOB_W3 / 16 + i];
+#endif
+    /* w3 = row 0 of the blob's output-layer B operand, as FP32 */
+    if (t < NH) {
+        const __nv_bfloat16 w = *reinterpret_cast<const __nv_bfloat16*>(blob + BLOB_W3 + tc::core_off(0, t, W2_LBO,
+                                                                                                      W2_SBO));
+        s.w3f[t] = __bfloat162float(w);
+    }
     if (t == 0) {
         s.b3 = *reinterpret_cast<const float*>(blob + BLOB_B3);
         tc::mbar_init(&s.mbar, 1);
         s.phase = 0;
+        s.failed = 0;
     }
     if (t < 32) tc::tmem_alloc(&s.tmem, tmem_cols<ROWS>());
     tc::fence_async_smem();
@@ -110,9 +135,15 @@ template <int ROWS> __device__ __forceinline__ void infer_setup(InferSmem<ROWS>&
     tc::fence_after_sync();
 }
 
+/* After a wait that ran out, the MMA it waited for may still be running:
+ * one thread waits for it once more (bounded) before the columns are freed */
 template <int ROWS> __device__ __forceinline__ void infer_teardown(InferSmem<ROWS>& s) {
     tc::fence_before_sync();
     __syncthreads();
+    if (s.failed && row_index() == 0) tc::mbar_wait(&s.mbar, s.failed_parity, 1u << 20);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
     if (row_index() < 32) tc::tmem_dealloc(s.tmem, tmem_cols<ROWS>());
 }
 
@@ -139,6 +170,10 @@ template <int ROWS> __device__ __forceinline__ bool infer_mma_wait(InferSmem<ROW
     const bool w = tc::mbar_wait(&s.mbar, parity, 1u << 20);
     const bool ok = __all_sync(0xffffffffu, w);
     tc::fence_after_sync();
+    if (!ok && (threadIdx.x & 31) == 0) {
+        s.failed = 1;
+        s.failed_parity = parity;
+    }
     return ok;
 }
 
@@ -156,6 +191,7 @@ __device__ __forceinline__ void infer_publish() {
  * A-operand rows of a2.  The loads run even after a failed wait (they are
  * valid TMEM reads); the caller then discards the row's result */
 template <int ROWS> __device__ __forceinline__ void infer_epilogue(InferSmem<ROWS>& s, uint32_t ta, int t) {
+    const uint32_t a2 = tc::smem_u32(s.a2);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         uint32_t r[16];
@@ -165,9 +201,9 @@ template <int ROWS> __device__ __forceinline__ void infer_epilogue(InferSmem<ROW
 #pragma unroll
         for (int hh = 0; hh < 2; ++hh) {
             const uint32_t* v = r + 8 * hh;
-            *reinterpret_cast<uint4*>(s.a2 + tc::core_off(t, 16 * c + 8 * hh, W2_LBO, W2_SBO)) =
-                make_uint4(relu_bf16x2(v[0], v[1]), relu_bf16x2(v[2], v[3]), relu_bf16x2(v[4], v[5]),
-                           relu_bf16x2(v[6], v[7]));
+            tc::sts128(a2 + tc::core_off(t, 16 * c + 8 * hh, W2_LBO, W2_SBO),
+                       make_uint4(relu_bf16x2(v[0], v[1]), relu_bf16x2(v[2], v[3]), relu_bf16x2(v[4], v[5]),
+                                  relu_bf16x2(v[6], v[7])));
         }
     }
 }
@@ -183,24 +219,29 @@ __device__ __forceinline__ void infer_mma_k64(uint32_t tmem, uint32_t a, const u
                          tc::sdesc(tc::smem_u32(b) + kc * 2 * W2_LBO, W2_LBO, W2_SBO), id, kc > 0);
 }
 
-/* nu_t of this thread's row; x[16] are its features (FP32, x[15] = 1) */
+/* nu_t of this thread's row; x[16] are its features (FP32, x[15] = 1).
+ * Returns -1 (block-uniform) once a completion wait of this block has run
+ * out: the caller then leaves its loop and tears down */
 template <int ROWS> __device__ __forceinline__ float infer_nu(InferSmem<ROWS>& s, const float x[NIN], int* err) {
     static_assert(ROWS == 128 || ROWS == 256, "one or two M=128 MMAs per block");
     const int t = row_index(), warp = t >> 5;
-    /* A of layer 1 */
-    *reinterpret_cast<uint4*>(s.a1 + tc::core_off(t, 0, W1_LBO, W1_SBO)) =
-        make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]), pack_bf16(x[6], x[7]));
-    *reinterpret_cast<uint4*>(s.a1 + tc::core_off(t, 8, W1_LBO, W1_SBO)) = make_uint4(
-        pack_bf16(x[8], x[9]), pack_bf16(x[10], x[11]), pack_bf16(x[12], x[13]), pack_bf16(x[14], x[15]));
+    /* A of layer 1 (at the start of a2) */
+    const uint32_t a1 = tc::smem_u32(s.a2);
+    tc::sts128(a1 + tc::core_off(t, 0, W1_LBO, W1_SBO),
+               make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]), pack_bf16(x[6], x[7])));
+    tc::sts128(a1 + tc::core_off(t, 8, W1_LBO, W1_SBO), make_uint4(pack_bf16(x[8], x[9]), pack_bf16(x[10], x[11]),
+                                                                   pack_bf16(x[12], x[13]), pack_bf16(x[14], x[15])));
     infer_publish();
-    /* three completions per call: parities ph, ph ^ 1, ph; the barrier above
-     * orders this read after the previous call's update */
+    if (s.failed) return -1.f;
+    /* the completions of a call have parities ph, ph ^ 1 (and ph again with
+     * the output layer on the tensor core); the barrier above orders this
+     * read after the previous call's update */
     const uint32_t ph = s.phase;
     const uint32_t id = tc::idesc_bf16_f32(128, NH);
     if (t == 0) {
 #pragma unroll
         for (int h = 0; h < ROWS / 128; ++h)
-            tc::mma_bf16(s.tmem + 64 * h, tc::sdesc(tc::smem_u32(s.a1) + h * 16 * W1_SBO, W1_LBO, W1_SBO),
+            tc::mma_bf16(s.tmem + 64 * h, tc::sdesc(a1 + h * 16 * W1_SBO, W1_LBO, W1_SBO),
                          tc::sdesc(tc::smem_u32(s.w1), W1_LBO, W1_SBO), id, 0);
         tc::mma_commit(&s.mbar);
     }
@@ -209,15 +250,39 @@ template <int ROWS> __device__ __forceinline__ float infer_nu(InferSmem<ROWS>& s
     /* layer 1 epilogue: relu -> h1 */
     infer_epilogue<ROWS>(s, ta, t);
     infer_publish();
+    if (s.failed) return -1.f;
     if (t == 0) {
         infer_mma_k64<ROWS>(s.tmem, tc::smem_u32(s.a2), s.w2, id);
         tc::mma_commit(&s.mbar);
     }
     ok = infer_mma_wait(s, ph ^ 1u) && ok;
+#if LBM_INFER_L3CC
+    /* output layer: y = b3 + w3 . relu(z2) in FP32, from the layer-2
+     * accumulators (two completions per call: parities ph, ph ^ 1) */
+    float y = s.b3;
+    const uint32_t w3 = tc::smem_u32(s.w3f);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        uint32_t r[16];
+        tc::tmem_ld16(ta + 16 * c, r);
+        tc::tmem_wait_ld();
+        tc::tmem_fence_regs<16>(r);
+#pragma unroll
+        for (int j = 0; j < 16; j += 4) {
+            const float4 w = tc::lds128f(w3 + 4 * (16 * c + j));
+            y = fmaf(w.x, fmaxf(__uint_as_float(r[j]), 0.f), y);
+            y = fmaf(w.y, fmaxf(__uint_as_float(r[j + 1]), 0.f), y);
+            y = fmaf(w.z, fmaxf(__uint_as_float(r[j + 2]), 0.f), y);
+            y = fmaf(w.w, fmaxf(__uint_as_float(r[j + 3]), 0.f), y);
+        }
+    }
+    /* two completions per call leave the parity of the next one at ph */
+#else
     /* layer 2 epilogue: relu -> h2 over h1 (the layer-2 MMA has finished
      * reading it) */
     infer_epilogue<ROWS>(s, ta, t);
     infer_publish();
+    if (s.failed) return -1.f;
     if (t == 0) {
         infer_mma_k64<ROWS>(s.tmem, tc::smem_u32(s.a2), s.w3, tc::idesc_bf16_f32(128, N3));
         tc::mma_commit(&s.mbar);
@@ -229,6 +294,7 @@ template <int ROWS> __device__ __forceinline__ float infer_nu(InferSmem<ROWS>& s
     tc::tmem_fence_regs<1>(&r0);
     const float y = __uint_as_float(r0) + s.b3;
     if (t == 0) s.phase = ph ^ 1u; /* every thread read it before the second infer_publish */
+#endif
     if (!ok) {
         if ((t & 31) == 0) atomicExch(err, 2);
         return 0.f;

@@ -280,6 +280,7 @@ __global__ void __launch_bounds__(128) k_mlp_predict_tc(const unsigned char* __r
 #pragma unroll
         for (int k = 0; k < NIN; ++k) x[k] = i < n ? X[size_t(i) * NIN + k] : 0.f;
         const float v = infer_nu<128>(s, x, err);
+        if (v < 0.f) break; /* a tensor-core wait ran out (block-uniform) */
         if (i < n) nu[i] = v;
     }
     infer_teardown<128>(s);
@@ -333,13 +334,17 @@ cudaError_t launch_mlp_predict_tc(const void* blob, const float* X, int n, float
     if (attr == cudaErrorNotReady)
         attr = cudaFuncSetAttribute(sgs::k_mlp_predict_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (attr != cudaSuccess) return attr;
-    sgs::k_mlp_predict_tc<<<b, 128, smem, s>>>((const unsigned char*)blob, X, n, nu, err);
+    TmemLane lane(s);
+    if (lane.status() != cudaSuccess) return lane.status();
+    sgs::k_mlp_predict_tc<<<b, 128, smem, lane.stream()>>>((const unsigned char*)blob, X, n, nu, err);
     return cudaGetLastError();
 }
 
 cudaError_t launch_tc_selftest(const void* A, const void* B, int kc, float* D, int* err, cudaStream_t s) {
     if (kc < 1 || kc > 4) return cudaErrorInvalidValue;
-    sgs::k_tc_selftest<<<1, 128, 0, s>>>((const __nv_bfloat16*)A, (const __nv_bfloat16*)B, kc, D, err);
+    TmemLane lane(s);
+    if (lane.status() != cudaSuccess) return lane.status();
+    sgs::k_tc_selftest<<<1, 128, 0, lane.stream()>>>((const __nv_bfloat16*)A, (const __nv_bfloat16*)B, kc, D, err);
     return cudaGetLastError();
 }
 

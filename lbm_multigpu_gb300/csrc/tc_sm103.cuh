@@ -50,6 +50,19 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t
     return d;
 }
 
+/* 16 bytes to a shared-memory address (32-bit shared window) */
+__device__ __forceinline__ void sts128(uint32_t saddr, uint4 v) {
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(saddr), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
+                 : "memory");
+}
+
+/* 16 bytes from a shared-memory address as four floats */
+__device__ __forceinline__ float4 lds128f(uint32_t saddr) {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(saddr));
+    return v;
+}
+
 /* one warp allocates ncols (power of two >= 32) TMEM columns; the base
  * address lands in *slot (shared memory) */
 __device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {

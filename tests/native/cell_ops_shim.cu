@@ -40,6 +40,16 @@ void cell_collide_mrt_dev(int les, float omega, float cs, float u, float* h, int
     const float k = 18.f * 1.41421356f * cs;
     for (int i = 0; i < n; ++i) collide_mrt_dev<float>(h + 19L * i, omega, les != 0, 1.f / omega, k, u);
 }
+void cell_pi_neq_d(const double* f, double* rho, double* p6, int n) {
+    for (int i = 0; i < n; ++i) pi_neq<double>(f + 19L * i, rho[i], p6 + 6L * i);
+}
+void cell_mrt_dev_pi_d(const double* f, double* rho, double* p6, int n) {
+    for (int i = 0; i < n; ++i) {
+        const MrtDev<double> m = mrt_dev_moments<double>(f + 19L * i, 0.0);
+        rho[i] = m.rho;
+        mrt_dev_pi(m, p6 + 6L * i);
+    }
+}
 float cell_philox_uniform(uint32_t seed, uint32_t cell, uint32_t step) { return philox_uniform(seed, cell, step); }
 void cell_alt_boundary(int type, float* f, int n, const int* yz, int ny, int nz, float u, int t) {
     for (int i = 0; i < n; ++i) alt_boundary<float>(type, f + 19L * i, 0, yz[2 * i], yz[2 * i + 1], 0, ny, nz, u, t);

@@ -87,3 +87,28 @@ def test_model_equilibrium_is_a_fixed_point(cellops):
     assert np.abs(h).max() < 1e-16
     assert abs(off.sum() - 1) < 1e-14 and abs(float(np.dot(CX, off)) - u) < 1e-14
     assert off[0] < 0.2  # 4/21 at rest, not the weight 1/3
+
+
+@pytest.mark.parametrize("les", [0, 1])
+def test_projected_collision_on_full_populations(cellops, les):
+    """with U = 0 the projected collision takes full populations (the
+    closure kernel's FP32 path): it equals collide_mrt<MRT> in FP64"""
+    f, _ = _states(np.zeros(19), 300, 11 + les, 0.01)
+    g = f.copy()
+    om, cs = 1 / 0.52, 0.01
+    cellops.cell_collide_d(MRT, les, ctypes.c_double(om), ctypes.c_double(cs), ctypes.c_double(0.0), _ptr(f), len(f))
+    cellops.cell_collide_mrt_dev_d(les, ctypes.c_double(om), ctypes.c_double(cs), ctypes.c_double(0.0), _ptr(g), len(g))
+    np.testing.assert_allclose(g, f, rtol=0, atol=1e-11)
+
+
+def test_moment_stress_equals_pi_neq(cellops):
+    """Pi_neq taken from the collision's moments (the closure's features)
+    equals sum c c f - rho/3 I - j j of the populations (pi_neq)"""
+    f, _ = _states(np.zeros(19), 300, 5, 0.02)
+    n = len(f)
+    r1, r2 = np.zeros(n), np.zeros(n)
+    p1, p2 = np.zeros((n, 6)), np.zeros((n, 6))
+    cellops.cell_pi_neq_d(_ptr(f), _ptr(r1), _ptr(p1), n)
+    cellops.cell_mrt_dev_pi_d(_ptr(f), _ptr(r2), _ptr(p2), n)
+    np.testing.assert_allclose(r2, r1, rtol=1e-14)
+    np.testing.assert_allclose(p2, p1, rtol=0, atol=1e-13)

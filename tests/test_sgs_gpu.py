@@ -222,3 +222,28 @@ def test_channel_comparison_runs(product):
     for name in ("smagorinsky", "mlp"):
         assert isinstance(out[name], dict), name
         assert all(np.isfinite(v) and v > 0 for v in out[name].values()), out[name]
+
+
+def test_closure_step_graphs_are_bit_exact(product):
+    """with the learned closure lbm_step replays batches of steps from CUDA
+    graphs too (after one direct step): 40 steps in one call equal 40 single
+    steps bit for bit, populations and forces"""
+    lbm = product
+    lib = lbm.library()
+    P = _params(lib, 21) * 3
+    steps = 40
+    text = lbm.make_inputs(64, 24, 6, obst1=(20.5, 11.5, 0.0), r1=4.0, re=60.0, umax=0.05, tmax=steps, les=1,
+                           cs=0.01, geometry="channel_square", sgs="mlp", bounceback="halfway", inlet_noise=0.01)
+    out = []
+    for batched in (True, False):
+        with lbm.Solver(text) as s:
+            s.set_sgs_mlp(P)
+            if batched:
+                s.step(steps)
+            else:
+                for _ in range(steps):
+                    s.step(1)
+            s.synchronize()
+            out.append((s.populations(), s.forces(steps)))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
