@@ -52,11 +52,52 @@ void forward(const float* P, const float* x, Fwd& a) {
         a.y += double(P[OFF_W3 + j]) * a.h2[j];
     }
 }
+/* the GPU inference's rounding (orc_mlp_set_bf16): features, W1, W2 (with
+ * b2 added to its column HC, the constant hidden unit) and w3 rounded to
+ * bf16 (nearest even), the first hidden layer rounded to bf16 after the
+ * ReLU, the layers summed in FP64 and read as FP32, the output layer
+ * y = b3 + sum_j w3_j relu(z2_j) as a chain of FP32 fused multiply-adds in
+ * j order */
+bool g_bf16 = false;
+float bf16(float v) {
+    uint32_t u;
+    std::memcpy(&u, &v, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    u &= 0xFFFF0000u;
+    float r;
+    std::memcpy(&r, &u, 4);
+    return r;
+}
+
+double forward_bf16(const float* P, const float* x) {
+    double h1[NH];
+    for (int j = 0; j < NH; ++j) {
+        double z = 0;
+        for (int k = 0; k < NIN; ++k) z += double(bf16(P[OFF_W1 + j * NIN + k])) * double(bf16(x[k]));
+        h1[j] = double(bf16(float(z > 0 ? z : 0)));
+    }
+    h1[HC] = 1;
+    float y = P[OFF_B3];
+    for (int j = 0; j < NH; ++j) {
+        double z = 0;
+        for (int k = 0; k < NH; ++k) {
+            const float w = k == HC ? P[OFF_W2 + j * NH + k] + P[OFF_B2 + j] : P[OFF_W2 + j * NH + k];
+            z += double(bf16(w)) * h1[k];
+        }
+        const float z2 = float(z);
+        y = std::fma(bf16(P[OFF_W3 + j]), z2 > 0 ? z2 : 0.f, y);
+    }
+    return y;
+}
 }  // namespace
 
 extern "C" {
 
 int orc_mlp_nparam(void) { return NPARAM; }
+
+/* 1: the closure's forward follows the GPU inference's bf16 rounding
+ * (forward_bf16), 0: FP64 */
+void orc_mlp_set_bf16(int on) { g_bf16 = on != 0; }
 
 void orc_sgs_features(const double* p, double tau0, double* x) {
     double pp = 0;
@@ -82,6 +123,10 @@ void orc_sgs_features(const double* p, double tau0, double* x) {
 void orc_mlp_forward(const float* params, const float* X, int n, double* nu) {
     Fwd a;
     for (int i = 0; i < n; ++i) {
+        if (g_bf16) {
+            nu[i] = NU_SCALE * softplus(forward_bf16(params, X + size_t(i) * NIN));
+            continue;
+        }
         forward(params, X + size_t(i) * NIN, a);
         nu[i] = NU_SCALE * softplus(a.y);
     }
@@ -152,9 +197,15 @@ void orc_collide_mlp(const float* params, double tau0, double* f, int n, double*
         orc_sgs_features(p, tau0, x);
         float xf[16];
         for (int k = 0; k < 16; ++k) xf[k] = float(x[k]);
-        Fwd a;
-        forward(params, xf, a);
-        const double nu = NU_SCALE * softplus(a.y);
+        double y;
+        if (g_bf16) {
+            y = forward_bf16(params, xf);
+        } else {
+            Fwd a;
+            forward(params, xf, a);
+            y = a.y;
+        }
+        const double nu = NU_SCALE * softplus(y);
         if (nu_out) nu_out[i] = nu;
         orc_collide_d(0, 0, 1 / (tau0 + 3 * nu), 0, 0, g, 1);
     }

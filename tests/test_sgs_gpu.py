@@ -117,9 +117,12 @@ def test_training_reduces_loss(product):
 
 def test_tensor_core_inference_matches_oracle(product):
     """the inference path of the collide kernels: BF16 weights and
-    activations through tcgen05.mma for all three layers, FP32 accumulation,
-    ReLU with the bf16 pack; against the FP64 oracle forward.  Tolerance: 2% relative L2 over the
-    samples (BF16 keeps 8 mantissa bits)"""
+    activations through tcgen05.mma for the hidden layers, FP32
+    accumulation, ReLU with the bf16 pack, the output layer in FP32; against
+    the FP64 oracle forward within 0.6 % relative L2 over the samples (about
+    twice what the bf16 rounding alone gives, 0.27 % in the CPU emulation),
+    and against the oracle's emulation of the same rounding within 1e-6
+    (what is left is the FP32 summation order; 7e-8 measured)"""
     torch = pytest.importorskip("torch")
     lib = product.library()
     P = _params(lib, 13)
@@ -133,15 +136,25 @@ def test_tensor_core_inference_matches_oracle(product):
     want = np.zeros(len(X))
     oracle().orc_mlp_forward(ptr(P), ptr(X), len(X), ptr(want))
     assert (got >= 0).all()
-    assert np.linalg.norm(got - want) <= 2e-2 * np.linalg.norm(want), np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert np.linalg.norm(got - want) <= 6e-3 * np.linalg.norm(want), np.linalg.norm(got - want) / np.linalg.norm(want)
+    emu = np.zeros(len(X))
+    oracle().orc_mlp_set_bf16(1)
+    try:
+        oracle().orc_mlp_forward(ptr(P), ptr(X), len(X), ptr(emu))
+    finally:
+        oracle().orc_mlp_set_bf16(0)
+    assert np.linalg.norm(got - emu) <= 1e-6 * np.linalg.norm(want), np.linalg.norm(got - emu) / np.linalg.norm(want)
 
 
 @pytest.mark.parametrize("bounceback", ["halfway", "fullway"])
 def test_channel_with_learned_closure_vs_oracle(product, bounceback):
     """the channel stream-collide with the learned closure in place of
     Smagorinsky (tensor-core MLP per 32 x 4 tile, persistent blocks) against
-    the oracle's step with the same closure in FP64; the BF16 inference error
-    stays under 5% of the closure's own effect (its distance to Smagorinsky)"""
+    the oracle's step with the same closure: with the GPU inference's bf16
+    rounding emulated, within 1e-5 relative L2 on velocity (the FP32 gate of
+    the other parity tests; 2.4e-6 measured after 30 steps, against 6e-5 with
+    the closure in FP64); with the closure in FP64, within 5 % of the
+    closure's own effect (its distance to Smagorinsky)"""
     from oracle_bindings import OracleRun, moments, rel_l2
 
     lbm = product
@@ -168,6 +181,15 @@ def test_channel_with_learned_closure_vs_oracle(product, bounceback):
     effect = rel_l2(js, jo)
     assert effect > 1e-4
     assert rel_l2(j, jo) < 0.05 * effect, (rel_l2(j, jo), effect)
+    ob = OracleRun(NX_, NY_, NZ_, mask, om, model=0, les=0, init_kind=0, init_u=0.05,
+                   halfway=int(bounceback == "halfway"), mlp=P)
+    oracle().orc_mlp_set_bf16(1)
+    try:
+        ob.step(steps)
+    finally:
+        oracle().orc_mlp_set_bf16(0)
+    jb = moments(ob.fa)[1][:, fl]
+    assert rel_l2(j, jb) < 1e-5, (rel_l2(j, jb), rel_l2(j, jo))
 
 
 def test_closure_requires_weights(product):
