@@ -218,28 +218,32 @@ int lbm_body_force_f32_noalloc(const float* fA, const uint8_t* mask, int nx, int
 /* ------------------------------------------------------------------------
  * Learned subgrid closure.  No counterpart in the reference (its LES is the
  * constant-Cs Smagorinsky model, LR7:683-685): a per-node MLP
- * 16 -> 64 -> 64 -> 1 (ReLU, softplus output) gives the eddy viscosity from
- * the node's non-equilibrium stress.  Parameters are a float vector of
+ * 16 -> 64 -> 64 -> 1 (ReLU, softplus output) gives a local Smagorinsky
+ * coefficient o = 1e-4 softplus(y) from the node's non-equilibrium stress;
+ * the collision's eddy viscosity is nu_t = o * x12 / tau0 = o * 100 |S|
+ * (o = 1e-4 is Cs = 0.1).  Parameters are a float vector of
  * lbm_mlp_param_count() entries: W1[64][16] (column 15 = bias), W2[64][64],
  * b2[64], w3[64], b3.  Hidden unit 63 of the first layer is the constant 1
  * (row 63 of W1 takes no part).  Samples are X[n][16] features (x15 = 1) and
- * T[n] target eddy viscosities (lattice units).
+ * T[n] target coefficients.
  * ------------------------------------------------------------------------ */
 int lbm_mlp_param_count(void);
 /* He-uniform hidden weights, Glorot-uniform output weights, zero biases,
  * from a seed (host memory) */
 int lbm_mlp_init_params(uint32_t seed, float* params);
-/* gradient of the mean squared error of nu_t / 1e-4 over n samples, and the
+/* gradient of the mean squared error of o / 1e-4 over n samples, and the
  * loss; device pointers, synchronous on stream */
 int lbm_mlp_grad(const float* d_params, const float* d_X, const float* d_T, int n, float* d_grad, float* d_loss,
                  void* stream);
-/* nu_t of n samples (FP32 forward on CUDA cores); device pointers, async */
+/* the coefficient o of n samples (FP32 forward on CUDA cores); device
+ * pointers, async */
 int lbm_mlp_predict(const float* d_params, const float* d_X, int n, float* d_nu, void* stream);
 /* Adam (beta 0.9 / 0.999) over seeded shuffled mini-batches of device
  * samples; params (host) in and out, loss_hist[steps] (host, may be NULL) */
 int lbm_mlp_train(const float* d_X, const float* d_T, int n, int batch, int steps, float lr, uint32_t seed,
                   float* params, float* loss_hist, void* stream);
-/* nu_t of n samples through the tensor-core path the collide kernels use:
+/* the coefficient o of n samples through the tensor-core path the collide
+ * kernels use:
  * BF16 weights and activations, FP32 accumulation (tcgen05.mma for the two
  * hidden layers, the output layer in FP32), b2 folded into W2 against the
  * constant unit; params in host memory, samples and output on the device;

@@ -81,9 +81,9 @@ __global__ void __launch_bounds__(32 * TY) k_ens_step(const Table T, const float
 #pragma unroll
             for (int k = 0; k < 6; ++k) p6[k] *= s;
             sgs::features_fast(p6, M.tau0, M.omega, xf); /* omega = 1 / tau0 */
-            const float nu = sgs::infer_nu<ROWS>(smem, xf, err);
-            if (nu < 0.f) break; /* a tensor-core wait ran out (block-uniform) */
-            omega = 1.f / (M.tau0 + 3.f * nu);
+            const float o = sgs::infer_nu<ROWS>(smem, xf, err);
+            if (o < 0.f) break; /* a tensor-core wait ran out (block-uniform) */
+            omega = 1.f / (M.tau0 + 3.f * o * sgs::strain_gain(xf, M.omega));
         }
         collide_mrt<MRT>(f, omega, SGS == SGS_SMAG, cs, 0.f);
         if (live) {

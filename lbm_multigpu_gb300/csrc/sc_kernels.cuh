@@ -583,12 +583,14 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, LBM_MLP_MINB) k_stream_collide_
         if (LBM_MLP_PREFETCH && g + int(gridDim.x) < ntiles) prefetch(g + int(gridDim.x));
         /* across the tensor-core round trips only rho, j and the five
          * stresses stay live; the products are formed again afterwards */
-        float keep[9] = {mo.rho, mo.jx, mo.jy, mo.jz, mo.n9, mo.n11, mo.n13, mo.n14, mo.n15};
-        const float nu = sgs::infer_nu<ROWS>(sm, xf, err);
-        if (nu < 0.f) break; /* a tensor-core wait ran out (block-uniform) */
+        float keep[10] = {mo.rho, mo.jx, mo.jy, mo.jz, mo.n9, mo.n11, mo.n13, mo.n14, mo.n15,
+                          sgs::strain_gain(xf, inv_t0)};
+        const float o = sgs::infer_nu<ROWS>(sm, xf, err);
+        if (o < 0.f) break; /* a tensor-core wait ran out (block-uniform) */
         if (!live || solid) continue;
 #pragma unroll
-        for (int k = 0; k < 9; ++k) asm volatile("" : "+f"(keep[k]));
+        for (int k = 0; k < 10; ++k) asm volatile("" : "+f"(keep[k]));
+        const float nu = o * keep[9];
         MrtDev<float> mr;
         mr.rho = keep[0], mr.jx = keep[1], mr.jy = keep[2], mr.jz = keep[3], mr.n9 = keep[4], mr.n11 = keep[5];
         mr.n13 = keep[6], mr.n14 = keep[7], mr.n15 = keep[8], mr.n1 = 0.f;

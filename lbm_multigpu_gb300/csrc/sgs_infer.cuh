@@ -12,14 +12,14 @@
  *             (LBM_INFER_L3CC; else ReLU + bf16 pack -> shared memory and
  *             layer 3 as tcgen05.mma Y[ROWS][16] = H2[ROWS][64] W3^T with
  *             row 0 of W3 = w3, column 0 read back)
- *   -> softplus -> nu_t
+ *   -> softplus -> the coefficient o (nu_t = o * strain_gain in the caller)
  *
  * Thread t of the block owns row t: MMA h = t / 128 covers rows 128 h ..
  * 128 h + 127 in TMEM lanes 0..127 of columns 64 h .. 64 h + 63, and warp w
  * reads lanes 32 (w % 4) .. + 31, which are exactly its threads' rows.
  * One elected thread issues the MMAs; completion arrives on an mbarrier that
  * every warp polls with a bounded wait (on a timeout the warp reports an
- * error code and returns nu_t = 0 so that the caller's state stays finite).
+ * error code and returns o = 0 so that the caller's state stays finite).
  */
 #pragma once
 #include <cuda_bf16.h>

@@ -8,7 +8,8 @@
  * shared-memory GEMMs into per-thread registers.  Each block writes its
  * partial gradient; k_mlp_adam sums the partials in a fixed order (so runs
  * are reproducible) and applies one Adam step.  Loss: mean squared error of
- * nu_t / NU_SCALE.
+ * o / NU_SCALE, o the network's coefficient (the eddy viscosity is
+ * o * strain_gain in the collision).
  */
 #include <cstdint>
 #include <cuda_bf16.h>

@@ -7,9 +7,11 @@
  * the definitions the GPU code implements:
  *   MLP 16 -> 64 -> 64 -> 1, ReLU, softplus output, hidden unit 63 of
  *   the first layer the constant 1 (row 63 of W1 takes no part),
- *   nu_t = 1e-4 * softplus(y); loss = mean over samples of
- *   (softplus(y) - nu_target / 1e-4)^2;
- *   features of p_ij = -3/2 Pi_neq_ij / rho and tau0 (x0..x15, x15 = 1);
+ *   coefficient o = 1e-4 * softplus(y), eddy viscosity in the collision
+ *   nu_t = o * x12 / tau0 (o * 100 |S|); loss = mean over samples of
+ *   (softplus(y) - o_target / 1e-4)^2;
+ *   features of p_ij = -3/2 Pi_neq_ij / rho and tau0 (x0..x15: x0..x11 = 0,
+ *   x12 = |p|, x13 = tr(p^3) / |p|^3, x14 = (tau0 - 1/2) 100, x15 = 1);
  *   box filter of a fine velocity field onto the coarse grid and the
  *   least-squares eddy viscosity of the filtered subgrid stress, its
  *   contractions averaged over 3x3x3 coarse cells.
@@ -23,7 +25,7 @@ namespace {
 constexpr int NIN = 16, NH = 64, HC = NH - 1;
 constexpr int OFF_W1 = 0, OFF_W2 = OFF_W1 + NH * NIN, OFF_B2 = OFF_W2 + NH * NH, OFF_W3 = OFF_B2 + NH,
               OFF_B3 = OFF_W3 + NH, NPARAM = OFF_B3 + 1;
-constexpr double P_REF = 0.01, S_REF = 0.01, NU_SCALE = 1e-4;
+constexpr double P_REF = 0.01, NU_SCALE = 1e-4;
 double relu(double z, double* dg) {
     if (dg) *dg = z > 0 ? 1 : 0;
     return z > 0 ? z : 0;
@@ -109,10 +111,7 @@ void orc_sgs_features(const double* p, double tau0, double* x) {
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j)
             for (int k = 0; k < 3; ++k) tr3 += m[i][j] * m[j][k] * m[k][i];
-    for (int i = 0; i < 6; ++i) {
-        x[i] = p[i] / P_REF;
-        x[6 + i] = p[i] / tau0 / S_REF;
-    }
+    for (int i = 0; i < 12; ++i) x[i] = 0; /* reserved: the inputs are invariants of p only */
     x[12] = std::sqrt(2 * pp) / P_REF;
     x[13] = pp > 1e-30 ? tr3 / std::pow(pp, 1.5) : 0;
     x[14] = (tau0 - 0.5) * 100;
@@ -186,8 +185,9 @@ void orc_pi_neq(const double* f, double* rho, double* p) {
 }
 
 /* the learned closure in the collision: per node (AoS f[n][19]) Pi_neq ->
- * p = -3/2 Pi_neq / rho -> features -> MLP -> nu_t, then the LR7 MRT
- * collision (model 0, no Smagorinsky) at 1 / (tau0 + 3 nu_t); nu_out[n] */
+ * p = -3/2 Pi_neq / rho -> features -> MLP -> coefficient o, eddy viscosity
+ * nu_t = o * x12 / tau0 (o G |S|, G = 1 / P_REF), then the LR7 MRT collision
+ * (model 0, no Smagorinsky) at 1 / (tau0 + 3 nu_t); nu_out[n] = nu_t */
 void orc_collide_mlp(const float* params, double tau0, double* f, int n, double* nu_out) {
     for (int i = 0; i < n; ++i) {
         double* g = f + 19L * i;
@@ -205,7 +205,7 @@ void orc_collide_mlp(const float* params, double tau0, double* f, int n, double*
             forward(params, xf, a);
             y = a.y;
         }
-        const double nu = NU_SCALE * softplus(y);
+        const double nu = NU_SCALE * softplus(y) * x[12] / tau0;
         if (nu_out) nu_out[i] = nu;
         orc_collide_d(0, 0, 1 / (tau0 + 3 * nu), 0, 0, g, 1);
     }

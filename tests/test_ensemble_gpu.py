@@ -78,7 +78,7 @@ def test_ensemble_mlp_collision_matches_oracle(product):
     P = np.zeros(lib.lbm_mlp_param_count(), np.float32)
     lib.lbm_mlp_init_params(21, ptr(P))
     P *= 3
-    P[-1] = 40.0            # nu_t around 4e-3: a visible change of tau
+    P[-1] = 40.0            # o around 4e-3 (Cs^2 0.4): a visible change of tau in the stressed field
     sizes, tau0 = [16, 24], 0.51
     rng = np.random.default_rng(0)
     with lbm.Ensemble(sizes, tau0, sgs="mlp") as e:

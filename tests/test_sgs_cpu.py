@@ -100,8 +100,6 @@ def _features_np(p, tau0):
     m = np.array([[p[0], p[3], p[4]], [p[3], p[1], p[5]], [p[4], p[5], p[2]]])
     pp = float((m * m).sum())
     x = np.zeros(16)
-    x[:6] = np.asarray(p) / 0.01
-    x[6:12] = np.asarray(p) / tau0 / 0.01
     x[12] = np.sqrt(2 * pp) / 0.01
     x[13] = np.trace(m @ m @ m) / pp ** 1.5 if pp > 1e-30 else 0.0
     x[14] = (tau0 - 0.5) * 100
@@ -181,6 +179,62 @@ def test_host_samples_stay_clear_of_solids():
     fluid[:, 10:12, 10:12] = False       # one coarse column solid
     X2, _ = samples_from_velocity(u, fluid, 0.505, margin=2)
     assert len(X2) == 4 * (64 - 25)      # the 5 x 5 cells around it drop out (all inside the interior)
+
+
+def test_regularised_targets_vanish_where_the_strain_is_weak():
+    """reg > 0: nu = max(0, -<tau:S>) / (2 (<S:S> + reg mean<S:S>)) keeps the
+    plain fit where the strain is strong and goes to zero where it is weak"""
+    from lbm_multigpu_gb300.sgs_pipeline import samples_from_velocity
+
+    rng = np.random.default_rng(8)
+    u = (0.03 * rng.standard_normal((3, 12, 16, 20))).astype(np.float32)
+    u[:, :, :, :10] *= 1e-3                  # a quiet half: weak strain, noise-level stress
+    fl = np.ones(u.shape[1:], bool)
+    X0, T0 = samples_from_velocity(u, fl, 0.52, margin=0)
+    X1, T1 = samples_from_velocity(u, fl, 0.52, margin=0, reg=0.25)
+    assert X0.shape == X1.shape      # the features carry each fit's own nu: p = (tau0 + 3 nu) S
+    assert (T1 <= T0 + 1e-12).all()
+    s = X0[:, 12]
+    strong, weak = s > np.percentile(s, 75), s < np.percentile(s, 25)
+    pos = strong & (T0 > 0)
+    assert pos.sum() > 10 and np.median(T1[pos] / T0[pos]) > 0.5
+    assert T1[weak].sum() < 1e-2 * T0[weak].sum()
+
+
+def test_coefficient_targets_invert_the_strain_gain():
+    """the collision's eddy viscosity is o x12 / tau0: the coefficient
+    targets times that gain give back the eddy-viscosity targets (below the
+    cap), zero where x12 is zero, and the oracle collision applies the same
+    gain"""
+    from lbm_multigpu_gb300.sgs_pipeline import coefficient_targets
+
+    X, T = _samples(256)
+    X[:, 12] = np.abs(X[:, 12])
+    X[:5, 12] = 0
+    X[:, 14] = 2.0
+    o = coefficient_targets(X, T)
+    g = X[:, 12] / (X[:, 14] / 100 + 0.5)
+    ok = (g > 0) & (T / np.where(g > 0, g, 1) < 5e-3)
+    np.testing.assert_allclose(o[ok] * g[ok], T[ok], rtol=1e-6)
+    assert (o[:5] == 0).all() and (o <= 5e-3).all()
+    # oracle: nu_out = 1e-4 softplus(y) x12 / tau0 with x from the node's stress
+    rng = np.random.default_rng(9)
+    from oracle_bindings import W as WQ
+
+    f = np.tile(WQ, (4, 1)) * (1 + 0.01 * rng.standard_normal((4, 19)))
+    P = _params(5, 0.2)
+    nu = np.zeros(4)
+    orc = oracle()
+    g2 = f.copy()
+    orc.orc_collide_mlp(ptr(P), ctypes.c_double(0.52), ptr(g2), 4, ptr(nu))
+    for i in range(4):
+        rho, pi = ctypes.c_double(), np.zeros(6)
+        orc.orc_pi_neq(ptr(f[i]), ctypes.byref(rho), ptr(pi))
+        x = np.zeros(16)
+        orc.orc_sgs_features(ptr(pi * (-1.5 / rho.value)), ctypes.c_double(0.52), ptr(x))
+        y = np.zeros(1)
+        orc.orc_mlp_forward(ptr(P), ptr(x.astype(np.float32)), 1, ptr(y))
+        np.testing.assert_allclose(nu[i], y[0] * x[12] / 0.52, rtol=1e-6)
 
 
 def _bf16(a):

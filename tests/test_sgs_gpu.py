@@ -160,7 +160,7 @@ def test_channel_with_learned_closure_vs_oracle(product, bounceback):
     lbm = product
     lib = lbm.library()
     P = _params(lib, 21) * 3
-    P[-1] = 40.0            # nu_t near 4e-3: tau_eff well above tau0
+    P[-1] = 10.0            # o near 1e-3 (Cs^2 0.1): nu_t = o x12 / tau0 about a tenth of nu0
     NX_, NY_, NZ_, steps = 64, 24, 6, 30
     kw = dict(obst1=(20.5, 11.5, 0.0), r1=4.0, re=60.0, umax=0.05, tmax=steps, les=1, cs=0.01,
               geometry="channel_square", bounceback=bounceback)
@@ -224,26 +224,30 @@ def test_trained_closure_beats_smagorinsky_on_held_out_boxes(product):
 
 
 def test_channel_comparison_runs(product):
-    """channel_profiles on a small case: every model's statistics exist,
-    the filtered 2x profiles are finite with a wake (reversed or slowed
-    mean flow and fluctuations behind the cylinder), and each model's
-    errors are finite numbers.  Which closure wins is reported, not asserted
-    (the committed weights lose to Smagorinsky in the wake)."""
+    """the learned closure against Smagorinsky in the square-cylinder channel
+    at the benchmarked channel's tau0 = 0.52, on a small grid: coarse
+    256 x 64 x 32, square of side 8 (Re 60), 3000 + 6000 + 6000 steps, against
+    the filtered 2x run.  The reference profiles are finite with a slowed
+    wake; the committed closure is closer than Smagorinsky (Cs = 0.1) to the
+    filtered mean-u, u-rms and v-rms profiles, each by more than twice the
+    spread of a rounding-level perturbation of the run (the "spread" model).
+    The same holds on the benchmarked 512 x 128 x 128 grid
+    (data/sgs_channel_report.json)."""
     import numpy as np
 
     from lbm_multigpu_gb300 import sgs_pipeline
 
     P = np.fromfile(product.__path__[0] + "/data/sgs_mlp.bin", dtype="<f4")
-    out, prof = sgs_pipeline.channel_profiles(P, coarse=(96, 32, 8), side=4, spinup=600, mean_steps=400,
-                                              fluc_steps=400, stations=(1, 2, 4))
-    assert out["stations"] == [22, 26, 34]  # rear face at x = 18, side 4
+    out, prof = sgs_pipeline.channel_profiles(P, coarse=(256, 64, 32), side=8, spinup=3000, mean_steps=6000,
+                                              fluc_steps=6000, stations=(1, 2, 4, 8), tau_c=0.52, centre_x=64)
+    assert out["stations"] == [76, 84, 100, 132]  # rear face at x = 68, side 8
     truth = prof["truth"]
-    assert truth.shape == (3, 4, 32) and np.isfinite(truth).all()
-    assert truth[0, 0, 14:18].mean() < 0.7 * truth[0, 0, 3:7].mean()  # slowed behind the cylinder
+    assert truth.shape == (4, 4, 64) and np.isfinite(truth).all()
+    assert truth[0, 0, 28:36].mean() < 0.7 * truth[0, 0, 3:8].mean()  # slowed behind the cylinder
     assert (truth[:, 2, 1:-1] >= 0).all() and truth[:, 2].max() > 0
-    for name in ("smagorinsky", "mlp"):
-        assert isinstance(out[name], dict), name
-        assert all(np.isfinite(v) and v > 0 for v in out[name].values()), out[name]
+    mlp, smag, spread = out["mlp"], out["smagorinsky"], out["spread"]
+    for k in ("u_mean_rel_l2", "u_rms_rel_l2", "v_rms_rel_l2"):
+        assert mlp[k] + 2 * spread[k] < smag[k], (k, out)
 
 
 def test_closure_step_graphs_are_bit_exact(product):
