@@ -79,8 +79,9 @@ int lbm_format_forces(const char* inputs_text, const double* fxyz, int n, char* 
 /* ---- handle API: the reference program's main() (LR7:2575-3029) ---- */
 
 /* Parse a .inputs record (the text WriteInputs produces, LR7:2547-2573, plus
- * the DPDY line of MRTtest/DynInlet3.cu and the extension keys listed in
- * INTEGRATION.md), allocate both grid levels on the current CUDA device,
+ * the DPDY line of MRTtest/DynInlet3.cu and this library's extension keys:
+ * GEOMETRY, PRECISION, LAYOUT, TAU, BOUNCEBACK, SGS, CF TIME, ...),
+ * allocate both grid levels on the current CUDA device,
  * build the node masks from the configured geometry (ImageFcn / ImageFcnLR)
  * and initialise at equilibrium (initialize / initializeLR, LR7:1060-1125). */
 int lbm_create(const char* inputs_text, lbm_handle** out);

@@ -27,6 +27,8 @@ DECLS = {
         float *yp = 0, *vp = 0, *ur = 0, *vr = 0, *wr = 0, *uave = 0, *urms = 0, *vave = 0, *vrms = 0;""",
     "lbm_save_state": """
         lbm_handle* h = 0;""",
+    "float off[19]": """
+        const lbm_handle* h = 0;""",
     "lbm_handle": """
         const char* text = "";""",
 }
