@@ -21,7 +21,11 @@ OpenMP restatement of the channel step, about 10 s of it), and
 `cpu_reference_program` the reference's own CPU program (CPU_3D/CPU_3D.cpp,
 staged and built by oracle/ref_recipe.py; a lid cavity) at the same shape.
 `--impl reference` times the channel step on the host cores alone (the
-reference arm), with CPU_3D's figure beside it.
+reference arm), with CPU_3D's figure beside it.  The default line also
+carries the two-level refinement (`c3_refinement`) and the closure's
+training ensemble (`c5_ensemble`) on their own configurations; `--workload`
+prints one of those rows, the precision study (`c4`) or the closure
+deployment (`sgs`) alone.
 """
 from __future__ import annotations
 
@@ -628,6 +632,12 @@ def main():
                                    frac=gbs / pk["hbm_gbs"],
                                    tensor_tflops=CELLS * SGS_FLOP_PER_CELL / (sgsr[1] * 1e-3) / 1e12,
                                    kernel="k_stream_collide_mlp<fp32>", weights=str(SGS_WEIGHTS.relative_to(ROOT)))
+    if args.precision == "all":
+        # the other GPU rows of the scope, each on its own configuration
+        # (rank 0, after the timed region): two-level refinement as configured
+        # and the closure's training ensemble
+        line["c3_refinement"] = workload_c3(min(args.steps, 500), max(args.warmup, 3))
+        line["c5_ensemble"] = workload_ensemble(min(args.steps, 64), max(args.warmup, 3))
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
         prog = cpu_reference_program()
