@@ -1312,6 +1312,20 @@ static int staging(lbm_handle* h, size_t n, float** d) {
     return LBM_OK;
 }
 
+/* the device's address of a caller buffer it can reach directly: page-locked
+ * host memory mapped into the device's address space (cudaHostAlloc, or
+ * cudaHostRegister with mapping, on a unified-addressing system); null for
+ * pageable memory.  The layout kernels then read or write such a buffer over
+ * the host link themselves: one pass, no copy engine and no staging copy */
+static void* mapped_view(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int lbm_get_populations(lbm_handle* h, int level, float* f) {
     if (int rc = check_level(h, level)) return rc;
     if (!f) return fail(LBM_ERR_ARG, "f is null");
@@ -1324,11 +1338,17 @@ int lbm_get_populations(lbm_handle* h, int level, float* f) {
         if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "get_populations: %s", cudaGetErrorString(e));
         return LBM_OK;
     }
-    float* d = nullptr;
-    if (int rc = staging(h, n, &d)) return rc;
-    cudaError_t e = launch_pack(s.L, s.f[s.cur], d, h->stream);
-    ++h->launches;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(f, d, n * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+    cudaError_t e;
+    if (void* dv = mapped_view(f)) {
+        e = launch_pack(s.L, s.f[s.cur], static_cast<float*>(dv), h->stream);
+        ++h->launches;
+    } else {
+        float* d = nullptr;
+        if (int rc = staging(h, n, &d)) return rc;
+        e = launch_pack(s.L, s.f[s.cur], d, h->stream);
+        ++h->launches;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(f, d, n * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "get_populations: %s", cudaGetErrorString(e));
     return LBM_OK;
@@ -1348,10 +1368,21 @@ int lbm_set_populations(lbm_handle* h, int level, const float* f) {
         if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "set_populations: %s", cudaGetErrorString(e));
         return LBM_OK;
     }
-    float* d = nullptr;
-    if (int rc = staging(h, n, &d)) return rc;
-    cudaError_t e = cudaMemcpyAsync(d, f, n * sizeof(float), cudaMemcpyHostToDevice, h->stream);
-    for (int i = 0; i < 2 && e == cudaSuccess; ++i, ++h->launches) e = launch_unpack(s.L, d, s.f[i], h->stream);
+    cudaError_t e;
+    if (const void* dv = mapped_view(f)) {
+        /* one read of the host buffer into the current buffer, then a device
+         * copy into the other */
+        e = launch_unpack(s.L, static_cast<const float*>(dv), s.f[0], h->stream);
+        ++h->launches;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s.f[1], s.f[0], size_t(s.L.qstride) * 19 * storage_bytes(s.L.storage),
+                                cudaMemcpyDeviceToDevice, h->stream);
+    } else {
+        float* d = nullptr;
+        if (int rc = staging(h, n, &d)) return rc;
+        e = cudaMemcpyAsync(d, f, n * sizeof(float), cudaMemcpyHostToDevice, h->stream);
+        for (int i = 0; i < 2 && e == cudaSuccess; ++i, ++h->launches) e = launch_unpack(s.L, d, s.f[i], h->stream);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "set_populations: %s", cudaGetErrorString(e));
     return LBM_OK;
