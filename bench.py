@@ -51,14 +51,16 @@ WORKLOAD = ("D3Q19 MRT+Smagorinsky channel 512x128x128, square cylinder side 16 
 
 
 SGS_WEIGHTS = ROOT / "lbm_multigpu_gb300" / "data" / "sgs_mlp.bin"
+SGS_REFRESH = 16   # the refresh interval of the learned_sgs_every entry
 # MLP 15(+1)->64->64->1 per cell: 2 (16*64 + 64*64 + 64) multiply-adds
 SGS_FLOP_PER_CELL = 2 * (16 * 64 + 64 * 64 + 64)
 
 
-def inputs_text(precision: str, tmax: int, bounceback: str = "halfway", sgs: str = "smagorinsky") -> str:
+def inputs_text(precision: str, tmax: int, bounceback: str = "halfway", sgs: str = "smagorinsky",
+                sgs_every: int = 1) -> str:
     import lbm_multigpu_gb300 as lbm
 
-    ext = dict(sgs="mlp", sgs_weights=str(SGS_WEIGHTS)) if sgs == "mlp" else {}
+    ext = dict(sgs="mlp", sgs_weights=str(SGS_WEIGHTS), sgs_every=sgs_every) if sgs == "mlp" else {}
     return lbm.make_inputs(NX, NY, NZ, obst1=(128.5, 63.5, 0.0), r1=8.0, re=120.0, umax=0.05, tmax=tmax, les=1,
                            cs=0.01, model="MRT", geometry="channel_square", precision=precision, inlet_noise=0.01,
                            seed=12345, bounceback=bounceback, **ext)
@@ -131,12 +133,13 @@ def dist_setup():
 
 
 def time_precision(precision: str, steps: int, warmup: int, world: int, dist, with_clocks: bool, gpu: int,
-                   bounceback: str = "halfway", sgs: str = "smagorinsky", keep_fields: bool = False):
+                   bounceback: str = "halfway", sgs: str = "smagorinsky", keep_fields: bool = False,
+                   sgs_every: int = 1):
     """resident-in-HBM run of `steps` steps after `warmup`; returns (ms, kernel ms, clocks, audit, launches,
     the final rho, u, v, w fields when keep_fields)"""
     import lbm_multigpu_gb300 as lbm
 
-    s = lbm.Solver(inputs_text(precision, warmup + steps + 10, bounceback, sgs))
+    s = lbm.Solver(inputs_text(precision, warmup + steps + 10, bounceback, sgs, sgs_every))
     s.step(warmup)
     s.synchronize()
     if dist:
@@ -459,13 +462,15 @@ def workload_sgs_channel(steps: int, warmup: int) -> dict:
     import lbm_multigpu_gb300 as lbm
 
     res = {}
-    for sgs in ("smagorinsky", "mlp"):
-        with lbm.Solver(inputs_text("fp32", steps + warmup + 10, sgs=sgs)) as s:
+    for name, sgs, every in (("smagorinsky", "smagorinsky", 1), ("mlp", "mlp", 1),
+                             (f"mlp_every{SGS_REFRESH}", "mlp", SGS_REFRESH)):
+        with lbm.Solver(inputs_text("fp32", steps + warmup + 10, sgs=sgs, sgs_every=every)) as s:
             s.step(warmup)
             ms = s.step_timed(steps)
             k = s.time_stream_collide(20)
-        res[sgs] = dict(mlups=CELLS * steps / (ms * 1e3), ms_per_step=ms / steps, kernel_ms=k)
+        res[name] = dict(mlups=CELLS * steps / (ms * 1e3), ms_per_step=ms / steps, kernel_ms=k)
     res["cost"] = 1 - res["mlp"]["mlups"] / res["smagorinsky"]["mlups"]
+    res[f"cost_every{SGS_REFRESH}"] = 1 - res[f"mlp_every{SGS_REFRESH}"]["mlups"] / res["smagorinsky"]["mlups"]
     res["tensor_tflops"] = CELLS * SGS_FLOP_PER_CELL / (res["mlp"]["kernel_ms"] * 1e-3) / 1e12
     return dict(workload="C5 deployment: " + WORKLOAD.replace("MRT+Smagorinsky", "MRT + learned closure"),
                 steps=steps, results=res)
@@ -561,6 +566,11 @@ def main():
         # the learned closure in place of Smagorinsky (tensor-core MLP per tile)
         mss, kmss, _, _, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, sgs="mlp")
         sgsr = (mss, kmss)
+        # the same closure evaluated every SGS_REFRESH steps, its eddy
+        # viscosity reused per node in between
+        msr, _, _, _, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, sgs="mlp",
+                                            sgs_every=SGS_REFRESH)
+        sgsr = (mss, kmss, msr)
     if args.precision == "all":
         # the reference's own wall treatment (full-way, on-node bounce-back)
         msf, kmsf, _, _, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, "fullway")
@@ -632,6 +642,11 @@ def main():
                                    frac=gbs / pk["hbm_gbs"],
                                    tensor_tflops=CELLS * SGS_FLOP_PER_CELL / (sgsr[1] * 1e-3) / 1e12,
                                    kernel="k_stream_collide_mlp<fp32>", weights=str(SGS_WEIGHTS.relative_to(ROOT)))
+        vr = world * CELLS * args.steps / (worst(sgsr[2]) * 1e-3) / 1e6
+        line[f"learned_sgs_every{SGS_REFRESH}"] = dict(
+            value=vr, ratio_vs_smagorinsky=vr / mlups, cost=1 - vr / mlups, ms_per_step=worst(sgsr[2]) / args.steps,
+            note=f"SGS every: {SGS_REFRESH} -- the closure's kernel on the steps t % {SGS_REFRESH} == 0, its "
+                 "per-node eddy viscosity reused by the plain stream-collide in between")
     if args.precision == "all":
         # the other GPU rows of the scope, each on its own configuration
         # (rank 0, after the timed region): two-level refinement as configured

@@ -212,7 +212,7 @@ def make_inputs(nx: int, ny: int, nz: int, *, obst1=(0.0, 0.0, 0.0), r1=1.0, obs
              "lid_face": "LID face:", "inlet_noise": "Inlet noise:", "seed": "Seed:", "velav": "VELAV:",
              "init": "Init:", "init_velocity": "Init velocity:", "order": "ORDER:", "fc_top_zflip": "FC top zflip:",
              "edge_pull": "EDGE PULL:", "lid_bc": "LID BC:", "bounceback": "BOUNCEBACK:", "sgs": "SGS:",
-             "sgs_weights": "SGS weights:", "dyny1": "DYNY1:", "dyn_every": "DYN every:",
+             "sgs_weights": "SGS weights:", "sgs_every": "SGS every:", "dyny1": "DYNY1:", "dyn_every": "DYN every:",
              "dyn_start": "DYN start:", "trip_end": "TRIP end:", "kp": "KP:", "faces": "FACES:",
              "cf_time": "CF TIME:", "layout": "LAYOUT:"}
     for k, v in ext.items():

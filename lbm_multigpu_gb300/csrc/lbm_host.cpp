@@ -97,6 +97,8 @@ struct Config {
     int halfway = 0;                /* "BOUNCEBACK: halfway" or "fullway" (the reference) */
     int lid_quirk = 0;              /* "LID BC: cpu3d" reproduces CPU_3D's lid as written */
     int sgs_mlp = 0;                /* "SGS: mlp": the learned closure replaces Smagorinsky */
+    int sgs_every = 1;              /* "SGS every: k": the closure's eddy viscosity is evaluated on the
+                                     * steps t with t % k == 0 and reused from a per-node buffer between */
     /* dynamic inlet (DI3): body force below DYNY1 (DI3:1358), P-control of
      * the mean velocity of the plane DYNY1 every DYN every steps after DYN
      * start (DI3:3150-3170), trip bodies (Obst2) until TRIP end (DI3:72-90) */
@@ -250,6 +252,10 @@ int parse_inputs(const char* text, Config& c) {
             c.sgs_mlp = val == "mlp";
         }
         else if (key == "SGS weights") c.sgs_weights = val;
+        else if (key == "SGS every") {
+            I(c.sgs_every);
+            ok = ok && c.sgs_every >= 1;
+        }
         else if (key == "DYNY1") I(c.dyny1);
         else if (key == "DYN every") I(c.dyn_every);
         else if (key == "DYN start") I(c.dyn_start);
@@ -356,6 +362,7 @@ std::string value_of(const Config& c, const std::string& key, float omega, float
     else if (key == "BOUNCEBACK") o << (c.halfway ? "halfway" : "fullway");
     else if (key == "SGS") o << (c.sgs_mlp ? "mlp" : "smagorinsky");
     else if (key == "SGS weights") o << c.sgs_weights;
+    else if (key == "SGS every") o << c.sgs_every;
     else if (key == "DYNY1") o << c.dyny1;
     else if (key == "DYN every") o << c.dyn_every;
     else if (key == "DYN start") o << c.dyn_start;
@@ -422,6 +429,7 @@ std::string write_inputs(const Config& c, float omega, float omegaLR) {
     if (c.halfway) line("BOUNCEBACK: ", "BOUNCEBACK");
     if (c.sgs_mlp) line("SGS: ", "SGS");
     if (!c.sgs_weights.empty()) line("SGS weights: ", "SGS weights");
+    if (c.sgs_every != 1) line("SGS every: ", "SGS every");
     if (c.dyny1 != d.dyny1) line("DYNY1: ", "DYNY1");
     if (c.dyn_every != d.dyn_every) line("DYN every: ", "DYN every");
     if (c.dyn_start != d.dyn_start) line("DYN start: ", "DYN start");
@@ -538,6 +546,7 @@ struct LevelState {
     bool has_lid = false;           /* the mask has LID nodes */
     bool has_xbc = false;           /* the mask has alternate-boundary nodes */
     uint32_t* links = nullptr;      /* device, per node: bit q = pull source of q is solid */
+    float* nu = nullptr;            /* device, per node: the learned closure's last eddy viscosity */
 };
 
 }  // namespace
@@ -587,6 +596,7 @@ struct lbm_handle {
     int* mlp_err = nullptr;
     bool mlp_ready = false;
     bool mlp_warm = false;         /* a closure step ran directly: its launcher is set up */
+    bool nu_valid = false;         /* lv[0].nu holds the closure's eddy viscosity of the current state's past */
     std::vector<float> mlp_params; /* host copy, for checkpoints */
     /* dynamic inlet: the body force on the device, the control history
      * (t, mean v, dpdy per control step) and whether the trip is in the mask */
@@ -607,6 +617,7 @@ void free_level(LevelState& s) {
     cudaFree(s.fpart);
     cudaFree(s.done);
     cudaFree(s.links);
+    cudaFree(s.nu);
     s = LevelState();
 }
 
@@ -777,6 +788,7 @@ int do_init(lbm_handle* h) {
     if (h->dpdy_dev) CUDA_TRY(cudaMemcpyAsync(h->dpdy_dev, &c.dpdy, sizeof(float), cudaMemcpyHostToDevice, h->stream));
     h->dyn_n = 0;
     h->have_mom = false;
+    h->nu_valid = false;
     for (int l = 0; l < h->nlevels; ++l) {
         LevelState& s = h->lv[l];
         for (int i = 0; i < 2; ++i) CUDA_TRY(launch_init(s.L, s.mask, s.f[i], kind, u0, h->stream, axis));
@@ -845,9 +857,20 @@ int one_step(lbm_handle* h) {
         h->have_mom = true;
     }
     if (c.sgs_mlp) {
-        CUDA_TRY(launch_stream_collide_mlp(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, C.links, h->mlp_blob,
-                                           h->mlp_err, h->stream));
-        h->mlp_warm = true;
+        /* the closure's eddy viscosity on the steps t % k == 0 (and the first
+         * step after the state was set), kept per node for the steps between */
+        p.nu = C.nu;
+        if (!C.nu || !h->nu_valid || t % c.sgs_every == 0) {
+            CUDA_TRY(launch_stream_collide_mlp(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, C.links,
+                                               h->mlp_blob, h->mlp_err, h->stream));
+            h->mlp_warm = true;
+            h->nu_valid = C.nu != nullptr;
+        } else {
+            p.nu_reuse = 1;
+            p.les = 0;
+            CUDA_TRY(launch_stream_collide(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, h->mom, h->stream,
+                                           C.links));
+        }
     }
     else
         CUDA_TRY(launch_stream_collide(C.L, p, C.f[C.cur], C.f[1 - C.cur], C.mask, C.stats, h->mom, h->stream,
@@ -924,6 +947,7 @@ int run_graph(lbm_handle* h, int k) {
     /* the host-side step state the captured steps advance, put back when
      * the batch does not reach the GPU (its steps never ran) */
     const int t0 = h->t, cur0 = h->lv[0].cur, cur1 = h->lv[1].cur, dyn_n0 = h->dyn_n;
+    const bool nu_valid0 = h->nu_valid;
     float* const mom0 = h->mom;
     float* const mom_prev0 = h->mom_prev;
     const bool have_mom0 = h->have_mom;
@@ -931,6 +955,7 @@ int run_graph(lbm_handle* h, int k) {
     auto restore = [&] {
         h->t = t0, h->lv[0].cur = cur0, h->lv[1].cur = cur1, h->dyn_n = dyn_n0;
         h->mom = mom0, h->mom_prev = mom_prev0, h->have_mom = have_mom0, h->launches = launches0;
+        h->nu_valid = nu_valid0;
     };
     CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     int rc = LBM_OK;
@@ -1194,6 +1219,11 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
         cudaMalloc(&h->audit_out, 4 * sizeof(double)) != cudaSuccess)
         return bail(fail(LBM_ERR_NOMEM, "cannot allocate audit scratch"));
     if ((rc = ensure_force_cap(h, std::max(1, c.tmax - c.startf)))) return bail(rc);
+    if (c.sgs_mlp && c.sgs_every > 1) {
+        const size_t nb = size_t(h->lv[0].L.qstride) * sizeof(float);
+        if (cudaMalloc(&h->lv[0].nu, nb) != cudaSuccess || cudaMemset(h->lv[0].nu, 0, nb) != cudaSuccess)
+            return bail(fail(LBM_ERR_NOMEM, "cannot allocate the closure's eddy-viscosity buffer"));
+    }
     if (!sgs_params.empty() && (rc = lbm_set_sgs_mlp(h, sgs_params.data(), sgs::NPARAM))) return bail(rc);
     if ((rc = do_init(h))) return bail(rc);
     *out = h;
@@ -1358,6 +1388,7 @@ int lbm_set_populations(lbm_handle* h, int level, const float* f) {
     if (int rc = check_level(h, level)) return rc;
     if (!f) return fail(LBM_ERR_ARG, "f is null");
     LevelState& s = h->lv[level];
+    h->nu_valid = false; /* the closure is evaluated again on the next step */
     const size_t n = size_t(s.L.nx) * s.L.ny * s.L.nz * 19;
     if (s.L.storage == STORE_F32 && s.L.pitch == s.L.nx && !s.L.blocked) {
         /* FP32 without row padding: straight into both buffers */
@@ -1451,6 +1482,7 @@ int lbm_set_sgs_mlp(lbm_handle* h, const float* params, int n) {
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     h->mlp_params.assign(params, params + n);
     h->mlp_ready = true;
+    h->nu_valid = false;
     return LBM_OK;
 }
 
@@ -1615,6 +1647,7 @@ int lbm_restore_state(lbm_handle* h, const char* path) {
         h->trip_in_mask = t < h->cfg.trip_end;
     }
     h->t = t;
+    h->nu_valid = false;
     return LBM_OK;
 }
 

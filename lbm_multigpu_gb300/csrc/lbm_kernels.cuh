@@ -142,6 +142,11 @@ struct StepParams {
     uint32_t noise_seed;
     /* coarse-moment export for the coarse->fine interpolation */
     int exp_x0, exp_y0, exp_nx, exp_ny;
+    /* the learned closure refreshed every k steps: its stream-collide writes
+     * each node's eddy viscosity here (when non-null), and the steps between
+     * refreshes (nu_reuse) relax at tau0 + 3 nu[c] in the plain kernel */
+    float* nu;
+    int nu_reuse;
 };
 
 /* launch configuration of the stream-collide kernel: a warp per row, 4 rows

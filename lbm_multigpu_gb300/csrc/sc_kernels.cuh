@@ -174,6 +174,9 @@ constexpr int FEAT_HALFWAY = 1, FEAT_LID = 2, FEAT_CLAMP = 4, FEAT_XBC = 8;
 /* FP16 / BF16 with LR7's MRT and no body force: the deviation collision
  * only (other models convert to populations and back) */
 constexpr int FEAT_DEVMRT = 16;
+/* the relaxation time of each node from the learned closure's last refresh
+ * (StepParams::nu) instead of the LES setting */
+constexpr int FEAT_NUBUF = 32;
 
 /* nodes per thread along z in k_stream_collide (the x/y index work of a
  * thread is done once for all of them) */
@@ -204,7 +207,7 @@ constexpr int SC_ZN = LBM_SC_ZN;
 
 /* the collision, statistics, store and moment export of a non-solid node;
  * f holds populations, or for DEV their stored deviations */
-template <class S, int LAY, bool DEVMRT>
+template <class S, int LAY, bool DEVMRT, bool NUBUF>
 __device__ __forceinline__ void sc_collide_store(const Level& L, const StepParams& p, S* __restrict__ fB,
                                                  float* __restrict__ stats, float* __restrict__ mom_export,
                                                  const NodeIdx<LAY>& n, typename Fmt<S>::T f[19], unsigned c,
@@ -212,8 +215,12 @@ __device__ __forceinline__ void sc_collide_store(const Level& L, const StepParam
     using T = typename Fmt<S>::T;
     constexpr bool DEV = LBM_SC_DEV && sizeof(S) == 2;
     const unsigned qs = unsigned(L.qstride);
+    /* the learned closure's eddy viscosity of this node from its last
+     * refresh, or the configured relaxation */
+    const float om = NUBUF ? 1.f / (p.tau0 + 3.f * p.nu[c]) : p.omega;
+    const bool les = !NUBUF && p.les != 0;
     if constexpr (DEV && DEVMRT) {
-        collide_mrt_dev<T>(f, T(p.omega), p.les != 0, T(p.tau0), T(p.smag_k), T(L.u_ref));
+        collide_mrt_dev<T>(f, T(om), les, T(p.tau0), T(p.smag_k), T(L.u_ref));
     } else {
         T dp = T(p.dpdy_dev ? *p.dpdy_dev : p.dpdy);
         if (y > p.dyn_y1) dp = T(0);
@@ -221,7 +228,7 @@ __device__ __forceinline__ void sc_collide_store(const Level& L, const StepParam
 #pragma unroll
             for (int q = 0; q < 19; ++q) f[q] += L.off[q];
         }
-        collide<T>(p.model, f, T(p.omega), p.les != 0, T(p.cs), dp);
+        collide<T>(p.model, f, T(om), les, T(p.cs), dp);
         if (DEV) {
 #pragma unroll
             for (int q = 0; q < 19; ++q) f[q] -= L.off[q];
@@ -343,7 +350,8 @@ __device__ __forceinline__ void sc_finish(const Level& L, const StepParams& p, c
 #if LBM_SC_FAST
     const bool plain = type == FLUID && !(HALFWAY && (mbyte & NEAR_SOLID));
     if (__all_sync(__activemask(), plain)) {
-        sc_collide_store<S, LAY, (FEAT & FEAT_DEVMRT) != 0>(L, p, fB, stats, mom_export, n, f, c, x, y, z);
+        sc_collide_store<S, LAY, (FEAT & FEAT_DEVMRT) != 0, (FEAT & FEAT_NUBUF) != 0>(L, p, fB, stats, mom_export, n,
+                                                                                      f, c, x, y, z);
         if (p.exp_nx > 0) sc_export<S>(L, p, mom_export, f, x, y, z);
         return;
     }
@@ -402,7 +410,8 @@ __device__ __forceinline__ void sc_finish(const Level& L, const StepParams& p, c
                 for (int q = 0; q < 19; ++q) f[q] -= L.off[q];
             }
         }
-        sc_collide_store<S, LAY, (FEAT & FEAT_DEVMRT) != 0>(L, p, fB, stats, mom_export, n, f, c, x, y, z);
+        sc_collide_store<S, LAY, (FEAT & FEAT_DEVMRT) != 0, (FEAT & FEAT_NUBUF) != 0>(L, p, fB, stats, mom_export, n,
+                                                                                      f, c, x, y, z);
     }
     if (p.exp_nx > 0) sc_export<S>(L, p, mom_export, f, x, y, z);
 }
@@ -591,6 +600,7 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, LBM_MLP_MINB) k_stream_collide_
 #pragma unroll
         for (int k = 0; k < 10; ++k) asm volatile("" : "+f"(keep[k]));
         const float nu = o * keep[9];
+        if (p.nu) p.nu[c] = nu;
         MrtDev<float> mr;
         mr.rho = keep[0], mr.jx = keep[1], mr.jy = keep[2], mr.jz = keep[3], mr.n9 = keep[4], mr.n11 = keep[5];
         mr.n13 = keep[6], mr.n14 = keep[7], mr.n15 = keep[8], mr.n1 = 0.f;
@@ -642,7 +652,8 @@ inline cudaError_t launch_sc_layout(const Level& L, const StepParams& p, const v
     const bool reduced = L.storage == STORE_F16 || L.storage == STORE_BF16;
     const int feat = (p.halfway ? FEAT_HALFWAY : 0) | (p.has_lid ? FEAT_LID : 0) | (p.pull_clamp ? FEAT_CLAMP : 0) |
                      (p.has_xbc ? FEAT_XBC : 0) |
-                     (reduced && p.model == MRT && p.dpdy == 0.f && !p.dpdy_dev ? FEAT_DEVMRT : 0);
+                     (reduced && p.model == MRT && p.dpdy == 0.f && !p.dpdy_dev ? FEAT_DEVMRT : 0) |
+                     (p.nu_reuse ? FEAT_NUBUF : 0);
 #define LBM_SC_CALL(FT)                                                                                          \
     (k_stream_collide<S, FT, LAY><<<grid, block, 0, s>>>(L, p, (const S*)fA, (S*)fB, mask, stats, mom_export, \
                                                           links))
@@ -700,6 +711,12 @@ inline cudaError_t launch_sc_layout(const Level& L, const StepParams& p, const v
         case 29: LBM_SC_DEV(29); break;
         case 30: LBM_SC_DEV(30); break;
         case 31: LBM_SC_DEV(31); break;
+        /* the steps between refreshes of the learned closure (channels:
+         * no lid, no alternate boundaries, no clamped pulls) */
+        case 32: LBM_SC(32); break;
+        case 33: LBM_SC(33); break;
+        case 48: LBM_SC_DEV(48); break;
+        case 49: LBM_SC_DEV(49); break;
         default: return cudaErrorInvalidValue;
     }
 #undef LBM_SC

@@ -250,12 +250,13 @@ def samples_from_velocity(u: np.ndarray, fluid: np.ndarray, tau0: float, margin:
 
 
 def _channel_record(nx: int, ny: int, nz: int, centre: tuple[float, float], half: float, tau: float, sgs: str,
-                    tmax: int, seed: int, stats: tuple[int, int] | None = None) -> str:
+                    tmax: int, seed: int, stats: tuple[int, int] | None = None, sgs_every: int = 1) -> str:
     """the square-cylinder channel (MRT, half-way walls, inlet 0.05 with 1 %
-    seeded noise); stats = (start of the mean, start of the variance)"""
+    seeded noise); stats = (start of the mean, start of the variance);
+    sgs_every: the closure's refresh interval"""
     from . import make_inputs
 
-    kw = dict(sgs="mlp") if sgs == "mlp" else {}
+    kw = dict(sgs="mlp", sgs_every=sgs_every) if sgs == "mlp" else {}
     if stats:
         kw.update(velav=1, start_velav=stats[0], start_velfluc=stats[1])
     return make_inputs(nx, ny, nz, obst1=(centre[0], centre[1], 0.0), r1=half, umax=0.05, tmax=tmax,
@@ -276,14 +277,16 @@ def fine_tau(tau_c: float) -> float:
 
 
 def _channel_run(nx: int, ny: int, nz: int, centre: tuple[float, float], half: float, tau: float, sgs: str,
-                 params, spinup: int, mean_steps: int, fluc_steps: int, seed: int, chunk: int = 2000):
+                 params, spinup: int, mean_steps: int, fluc_steps: int, seed: int, chunk: int = 2000,
+                 sgs_every: int = 1):
     """one channel run with running statistics: the mean over
     [spinup, spinup + mean_steps), the variance about it over the next
     fluc_steps.  Returns the statistics, or None if the run blew up."""
     from . import Solver
 
     t_end = spinup + mean_steps + fluc_steps
-    text = _channel_record(nx, ny, nz, centre, half, tau, sgs, t_end, seed, (spinup, spinup + mean_steps))
+    text = _channel_record(nx, ny, nz, centre, half, tau, sgs, t_end, seed, (spinup, spinup + mean_steps),
+                           sgs_every)
     with Solver(text) as s:
         if sgs == "mlp":
             s.set_sgs_mlp(params)
@@ -367,14 +370,15 @@ def zero_closure(params) -> np.ndarray:
     return z
 
 
-def channel_errors(params, ref: dict, models=("none", "smagorinsky", "mlp")):
+def channel_errors(params, ref: dict, models=("none", "smagorinsky", "mlp"), sgs_every: int = 1):
     """the coarse runs of `models` (tau0 = ref["tau_c"]) against `ref`
     (channel_truth): relative L2 of the mean-u, u-rms and v-rms profiles
     (walls excluded), "unstable" for a run that blew up; and the profiles.
     Model "spread" is the closure kernel with zero eddy viscosity
     (zero_closure): its errors are measured against the "none" run (same
     physics, FP32 rounding apart), so they show how far the statistics of
-    this run length move from a rounding-level perturbation alone."""
+    this run length move from a rounding-level perturbation alone.
+    sgs_every: the closure's refresh interval (SGS every)."""
     from . import stats_profiles
 
     nx, ny, nz = ref["coarse"]
@@ -389,7 +393,8 @@ def channel_errors(params, ref: dict, models=("none", "smagorinsky", "mlp")):
     out, profiles = {}, {}
     for name in models:
         sgs, w = ("mlp", zero_closure(params)) if name == "spread" else (name, params)
-        st = _channel_run(nx, ny, nz, (cx, cy), half, tau_c, sgs, w, *ref["steps"], ref["seed"])
+        st = _channel_run(nx, ny, nz, (cx, cy), half, tau_c, sgs, w, *ref["steps"], ref["seed"],
+                          sgs_every=sgs_every if name == "mlp" else 1)
         if st is None:
             out[name] = "unstable"
             continue
@@ -417,7 +422,7 @@ def channel_errors(params, ref: dict, models=("none", "smagorinsky", "mlp")):
 def channel_profiles(params: np.ndarray, coarse=(192, 64, 32), side: int = 8, spinup: int = 4000,
                      mean_steps: int = 4000, fluc_steps: int = 4000, stations=(1, 2, 4, 8), seed: int = 12345,
                      models=("none", "smagorinsky", "mlp", "spread"), tau_c: float = TAU_C,
-                     centre_x: int | None = None):
+                     centre_x: int | None = None, sgs_every: int = 1):
     """a-posteriori comparison in the square-cylinder channel family: a
     square cylinder in a channel (coarse grid `coarse`, tau0 = tau_c, i.e.
     Re = 3 * 0.05 * side / (tau_c - 1/2)) run with no model, Smagorinsky and
@@ -431,8 +436,9 @@ def channel_profiles(params: np.ndarray, coarse=(192, 64, 32), side: int = 8, sp
     fine variances include the fluctuations below the coarse filter width."""
     ref = channel_truth(coarse, side, spinup, mean_steps, fluc_steps, stations, seed, tau_c, centre_x)
     out = dict(stations=ref["stations"], coarse=list(coarse), side=side, centre_x=centre_x, tau_c=tau_c,
-               tau_f=fine_tau(tau_c), re=3 * 0.05 * side / (tau_c - 0.5), steps=[spinup, mean_steps, fluc_steps])
-    errs, profiles = channel_errors(params, ref, models)
+               tau_f=fine_tau(tau_c), re=3 * 0.05 * side / (tau_c - 0.5), steps=[spinup, mean_steps, fluc_steps],
+               sgs_every=sgs_every)
+    errs, profiles = channel_errors(params, ref, models, sgs_every)
     out.update(errs)
     profiles["truth"] = ref["truth"]
     return out, profiles
@@ -500,6 +506,7 @@ def channel_main(argv) -> int:
     ap.add_argument("--steps", default="4000,4000,4000", help="spin-up, mean, fluctuation coarse steps")
     ap.add_argument("--tau", type=float, default=TAU_C, help="coarse tau0")
     ap.add_argument("--centre-x", type=int, default=None, help="cylinder centre x (coarse node; default nx/6)")
+    ap.add_argument("--sgs-every", type=int, default=1, help="the closure's refresh interval (SGS every)")
     ap.add_argument("--seed", type=int, default=12345)
     ap.add_argument("--report", default=None, help="JSON report path")
     ap.add_argument("--profiles", default=None, help=".npz of the profiles")
@@ -508,7 +515,8 @@ def channel_main(argv) -> int:
     coarse = tuple(int(v) for v in a.coarse.split("x"))
     sp, ms, fs = (int(v) for v in a.steps.split(","))
     t0 = time.perf_counter()
-    out, prof = channel_profiles(P, coarse, a.side, sp, ms, fs, seed=a.seed, tau_c=a.tau, centre_x=a.centre_x)
+    out, prof = channel_profiles(P, coarse, a.side, sp, ms, fs, seed=a.seed, tau_c=a.tau, centre_x=a.centre_x,
+                                 sgs_every=a.sgs_every)
     out["seconds"] = time.perf_counter() - t0
     out["weights"] = a.weights
     print(json.dumps(out))

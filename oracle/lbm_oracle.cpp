@@ -658,7 +658,14 @@ void step_impl(const orc_params* p, const uint8_t* mask, const T* fA, T* fB, dou
                     if (p->mlp) {
                         double g[Q];
                         for (int q = 0; q < Q; ++q) g[q] = double(f[q]);
-                        orc_collide_mlp(p->mlp, 1.0 / double(p->omega), g, 1, nullptr);
+                        const double tau0 = 1.0 / double(p->omega);
+                        if (p->mlp_every <= 1 || !p->mlp_nu || p->t % p->mlp_every == 0) {
+                            double nu = 0;
+                            orc_collide_mlp(p->mlp, tau0, g, 1, &nu);
+                            if (p->mlp_nu) p->mlp_nu[c] = nu;
+                        } else {
+                            orc_collide_d(0, 0, 1.0 / (tau0 + 3.0 * p->mlp_nu[c]), 0, 0, g, 1);
+                        }
                         for (int q = 0; q < Q; ++q) f[q] = T(g[q]);
                     } else {
                         /* DI3:1358: the body force acts only up to DYNY1 */

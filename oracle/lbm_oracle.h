@@ -97,6 +97,12 @@ typedef struct {
     /* dynamic inlet (DI3:1358): no body force for y > dyn_y1; a large value
      * switches the cut off */
     int dyn_y1;
+    /* the closure refreshed every mlp_every steps: on steps t with
+     * t % mlp_every == 0 the MLP's nu_t of each node goes to mlp_nu[node]
+     * (compact index), the other steps relax at tau0 + 3 mlp_nu[node];
+     * mlp_every <= 1 or mlp_nu null: the MLP on every step */
+    int mlp_every;
+    double* mlp_nu;
 } orc_params;
 
 typedef struct {

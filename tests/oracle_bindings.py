@@ -38,7 +38,7 @@ class Params(ctypes.Structure):
                 ("exp_y0", ctypes.c_int), ("exp_nx", ctypes.c_int), ("exp_ny", ctypes.c_int),
                 ("noise_amp", _F), ("noise_seed", ctypes.c_uint32), ("pull_clamp", ctypes.c_int),
                 ("lid_quirk", ctypes.c_int), ("halfway", ctypes.c_int), ("mlp", ctypes.c_void_p),
-                ("dyn_y1", ctypes.c_int)]
+                ("dyn_y1", ctypes.c_int), ("mlp_every", ctypes.c_int), ("mlp_nu", ctypes.c_void_p)]
 
 
 class Refine(ctypes.Structure):
@@ -89,7 +89,7 @@ class OracleRun:
 
     def __init__(self, nx, ny, nz, mask, omega, *, model=0, les=0, cs=0.02, dpdy=0.0, u_in=0.05, init_kind=0,
                  init_u=0.05, lid_u=(0, 0, 0), lid_face=5, startf=0, refine=None, noise_amp=0.0, seed=12345,
-                 stats=None, f0=None, pull_clamp=0, lid_quirk=0, halfway=0, mlp=None, cf_time=False):
+                 stats=None, f0=None, pull_clamp=0, lid_quirk=0, halfway=0, mlp=None, cf_time=False, mlp_every=1):
         o = oracle()
         self.p = Params(nx=nx, ny=ny, nz=nz, model=model, les=les, omega=omega, cs=cs, dpdy=dpdy, u_in=u_in,
                         rho_out=1.0, lid_face=lid_face, stats_weight=1.0, noise_amp=noise_amp, noise_seed=seed,
@@ -97,6 +97,9 @@ class OracleRun:
         if mlp is not None:
             self._mlp = np.ascontiguousarray(mlp, np.float32)
             self.p.mlp = self._mlp.ctypes.data
+            if mlp_every > 1:
+                self._nu = np.zeros(nx * ny * nz)
+                self.p.mlp_every, self.p.mlp_nu = mlp_every, self._nu.ctypes.data
         self.p.lid_u[:] = list(lid_u)
         if stats:
             self.p.stats_on, self.p.start_av, self.p.start_fluc = 1, stats[0], stats[1]

@@ -80,6 +80,9 @@ def test_make_inputs_is_a_fixed_point(product):
     n = product.normalize_inputs(t)
     assert product.normalize_inputs(n) == n
     assert "omega \t: 1.92308" in n  # tau0 = 0.52
+    t2 = product.make_inputs(64, 24, 6, geometry="channel_square", sgs="mlp", sgs_every=8)
+    n2 = product.normalize_inputs(t2)
+    assert "SGS every: \t8\n" in n2 and product.normalize_inputs(n2) == n2
 
 
 @pytest.mark.parametrize("text,code,msg", [
@@ -88,6 +91,7 @@ def test_make_inputs_is_a_fixed_point(product):
     ("Base domain size \t64x24\n", 3, "cannot read"),
     ("Base domain size \t64x24x6\nRE: \tabc\n", 3, "cannot read"),
     ("Base domain size \t64x24x6\nWhat: \t1\n", 3, "unknown key"),
+    ("Base domain size \t64x24x6\nSGS every: \t0\n", 3, "cannot read"),
 ])
 def test_malformed_records_are_rejected(product, text, code, msg):
     with pytest.raises(product.LbmError) as e:
