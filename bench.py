@@ -567,10 +567,12 @@ def main():
         mss, kmss, _, _, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, sgs="mlp")
         sgsr = (mss, kmss)
         # the same closure evaluated every SGS_REFRESH steps, its eddy
-        # viscosity reused per node in between
-        msr, _, _, _, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, sgs="mlp",
+        # viscosity reused per node in between, timed over whole refresh
+        # periods (every window of k steps holds one refresh)
+        nref = SGS_REFRESH * max(1, -(-args.steps // SGS_REFRESH))
+        msr, _, _, _, _, _ = time_precision("fp32", nref, args.warmup, world, dist, False, local, sgs="mlp",
                                             sgs_every=SGS_REFRESH)
-        sgsr = (mss, kmss, msr)
+        sgsr = (mss, kmss, msr, nref)
     if args.precision == "all":
         # the reference's own wall treatment (full-way, on-node bounce-back)
         msf, kmsf, _, _, _, _ = time_precision("fp32", args.steps, args.warmup, world, dist, False, local, "fullway")
@@ -642,9 +644,10 @@ def main():
                                    frac=gbs / pk["hbm_gbs"],
                                    tensor_tflops=CELLS * SGS_FLOP_PER_CELL / (sgsr[1] * 1e-3) / 1e12,
                                    kernel="k_stream_collide_mlp<fp32>", weights=str(SGS_WEIGHTS.relative_to(ROOT)))
-        vr = world * CELLS * args.steps / (worst(sgsr[2]) * 1e-3) / 1e6
+        vr = world * CELLS * sgsr[3] / (worst(sgsr[2]) * 1e-3) / 1e6
         line[f"learned_sgs_every{SGS_REFRESH}"] = dict(
-            value=vr, ratio_vs_smagorinsky=vr / mlups, cost=1 - vr / mlups, ms_per_step=worst(sgsr[2]) / args.steps,
+            value=vr, ratio_vs_smagorinsky=vr / mlups, cost=1 - vr / mlups, ms_per_step=worst(sgsr[2]) / sgsr[3],
+            steps=sgsr[3],
             note=f"SGS every: {SGS_REFRESH} -- the closure's kernel on the steps t % {SGS_REFRESH} == 0, its "
                  "per-node eddy viscosity reused by the plain stream-collide in between")
     if args.precision == "all":
