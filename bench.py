@@ -22,8 +22,9 @@ OpenMP restatement of the channel step, about 10 s of it), and
 staged and built by oracle/ref_recipe.py; a lid cavity) at the same shape.
 `--impl reference` times the channel step on the host cores alone (the
 reference arm), with CPU_3D's figure beside it.  The default line also
-carries the two-level refinement (`c3_refinement`) and the closure's
-training ensemble (`c5_ensemble`) on their own configurations; `--workload`
+carries the two-level refinement (`c3_refinement`), the closure's
+training ensemble (`c5_ensemble`) and the FP16 / BF16 precision study at
+768x256x256 over 2000 steps (`c4_precision`) on their own configurations; `--workload`
 prints one of those rows, the precision study (`c4`) or the closure
 deployment (`sgs`) alone.
 """
@@ -656,6 +657,8 @@ def main():
         # and the closure's training ensemble
         line["c3_refinement"] = workload_c3(min(args.steps, 500), max(args.warmup, 3))
         line["c5_ensemble"] = workload_ensemble(min(args.steps, 64), max(args.warmup, 3))
+        # the precision study at its configured 2000 steps, errors at the end
+        line["c4_precision"] = workload_c4(2000, every=2000)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
         prog = cpu_reference_program()
