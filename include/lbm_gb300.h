@@ -274,7 +274,10 @@ int lbm_tc_selftest(int kc, const uint16_t* A, const uint16_t* B, float* D);
 /* weights of the learned closure for a handle whose record selects
  * "SGS: mlp" (the record may instead name a float32 file in "SGS weights:");
  * the stream-collide then takes its eddy viscosity from the MLP on the
- * tensor cores instead of the Smagorinsky model.  n = lbm_mlp_param_count() */
+ * tensor cores instead of the Smagorinsky model ("SGS every: k" evaluates it
+ * on the steps t % k == 0 and on the first step after weights, populations
+ * or a checkpoint were set, and reuses each node's value in between).
+ * n = lbm_mlp_param_count() */
 int lbm_set_sgs_mlp(lbm_handle* h, const float* params, int n);
 
 /* Checkpoint and restart (no counterpart in the reference, which always

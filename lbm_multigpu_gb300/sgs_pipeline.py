@@ -362,8 +362,8 @@ def channel_truth(coarse=(192, 64, 32), side: int = 8, spinup: int = 4000, mean_
 
 
 def zero_closure(params) -> np.ndarray:
-    """the closure's weights with the output bias at -30: nu_t = 1e-4
-    softplus(-30), zero to FP32 precision"""
+    """the closure's weights with the output bias at -30: the coefficient
+    1e-4 softplus(-30), and so nu_t, zero to FP32 precision"""
     z = np.array(params if params is not None and len(params) else np.zeros(library().lbm_mlp_param_count()),
                  np.float32)
     z[-1] = -30.0

@@ -118,7 +118,8 @@ void orc_sgs_features(const double* p, double tau0, double* x) {
     x[15] = 1;
 }
 
-/* nu_t of n samples X[n][16] */
+/* the network's coefficient o of n samples X[n][16] (the collision's eddy
+ * viscosity is o * x12 / tau0) */
 void orc_mlp_forward(const float* params, const float* X, int n, double* nu) {
     Fwd a;
     for (int i = 0; i < n; ++i) {

@@ -256,6 +256,33 @@ def test_closure_refresh_graphs_are_bit_exact(product):
     np.testing.assert_array_equal(out[0][1], out[1][1])
 
 
+def test_closure_refresh_checkpoint_continuation(product, tmp_path):
+    """a checkpoint of a run with SGS every: 4 holds the closure's weights;
+    the restored solver evaluates the closure on its first step, so
+    continuing from a checkpoint taken on a refresh step (t = 20) equals the
+    uninterrupted run bit for bit, populations and forces"""
+    lbm = product
+    lib = lbm.library()
+    P = _params(lib, 21) * 3
+    text = lbm.make_inputs(64, 24, 6, obst1=(20.5, 11.5, 0.0), r1=4.0, re=60.0, umax=0.05, tmax=40, les=1,
+                           cs=0.01, geometry="channel_square", sgs="mlp", sgs_every=4, bounceback="halfway",
+                           inlet_noise=0.01)
+    with lbm.Solver(text) as s:
+        s.set_sgs_mlp(P)
+        s.step(40)
+        want_f, want_force = s.populations(), s.forces()
+    ck = tmp_path / "closure.ckpt"
+    with lbm.Solver(text) as s:
+        s.set_sgs_mlp(P)
+        s.step(20)
+        s.save_state(str(ck))
+    with lbm.Solver.from_state(str(ck)) as s:
+        assert s.time() == 20
+        s.step(20)
+        np.testing.assert_array_equal(s.populations(), want_f)
+        np.testing.assert_array_equal(s.forces(), want_force)
+
+
 def test_closure_requires_weights(product):
     lbm = product
     text = lbm.make_inputs(64, 24, 6, obst1=(20.5, 11.5, 0.0), r1=4.0, re=60.0, umax=0.05, tmax=10, les=1,
