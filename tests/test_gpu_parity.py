@@ -815,6 +815,24 @@ def _run_layout(lbm, text, steps, levels=1):
     return out
 
 
+def test_ragged_width_channel_vs_oracle(product):
+    """a width that is not a multiple of 32 (70: the last 32-node block of
+    every row holds 26 padding lanes) in the default blocked layout, with
+    half-way walls and inlet noise, against the oracle after 30 steps"""
+    lbm = product
+    steps, nx = 30, 70
+    text = lbm.make_inputs(nx, 24, 6, obst1=(20.5, 11.5, 0.0), r1=4.0, re=60.0, umax=0.05, tmax=steps, les=1,
+                           cs=0.01, geometry="channel_square", bounceback="halfway", inlet_noise=0.01, seed=9)
+    with lbm.Solver(text) as s:
+        s.step(steps)
+        f, mask, om = s.populations(), s.mask(), s.params()["omega"]
+    o = OracleRun(nx, 24, 6, mask, om, model=0, les=1, cs=0.01, u_in=0.05, init_u=0.05, noise_amp=0.01, seed=9,
+                  halfway=1)
+    o.step(steps)
+    err, drho = _compare(f, o.fa, mask)
+    assert err < RTOL and drho < 1e-5, (err, drho)
+
+
 @pytest.mark.parametrize("precision", ["fp32", "fp16"])
 def test_mapped_host_buffers_match_pageable(product, precision):
     """page-locked host buffers are read and written by the layout kernels
