@@ -312,23 +312,22 @@ __device__ __forceinline__ void load19(const Level& L, const S* f, long long c, 
 }
 
 /* second-order correction of the interpolated momentum from the 8 corner
- * strain rates and momenta (LR7:2101-2144, 2270-2316); corner i = x + 2y + 4z */
-__device__ __forceinline__ void second_order(const float mc[8][9], const float S[8][6], float a[9]) {
-#pragma unroll
-    for (int j = 0; j < 9; ++j) a[j] = 0.f;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        const float sx = (i & 1) ? 1.f : -1.f, sy = (i & 2) ? 1.f : -1.f, sz = (i & 4) ? 1.f : -1.f;
-        a[0] += sx * S[i][0];
-        a[1] += sy * S[i][3] - sx * sy * mc[i][2];
-        a[2] += sz * S[i][5] - sx * sz * mc[i][3];
-        a[3] += sx * S[i][3] - sx * sy * mc[i][1];
-        a[4] += sy * S[i][1];
-        a[5] += sz * S[i][4] - sy * sz * mc[i][3];
-        a[6] += sx * S[i][5] - sx * sz * mc[i][1];
-        a[7] += sy * S[i][4] - sy * sz * mc[i][2];
-        a[8] += sz * S[i][2];
-    }
+ * strain rates and momenta (LR7:2101-2144, 2270-2316); corner i = x + 2y + 4z.
+ * Accumulated one corner at a time as the corners are read (a starts at 0),
+ * so that no thread holds all eight corners' moments at once */
+__device__ __forceinline__ void second_order_add(float a[9], int i, const float mc[9], const float S[6]) {
+    const float sx = (i & 1) ? 1.f : -1.f, sy = (i & 2) ? 1.f : -1.f, sz = (i & 4) ? 1.f : -1.f;
+    a[0] += sx * S[0];
+    a[1] += sy * S[3] - sx * sy * mc[2];
+    a[2] += sz * S[5] - sx * sz * mc[3];
+    a[3] += sx * S[3] - sx * sy * mc[1];
+    a[4] += sy * S[1];
+    a[5] += sz * S[4] - sy * sz * mc[3];
+    a[6] += sx * S[5] - sx * sz * mc[1];
+    a[7] += sy * S[4] - sy * sz * mc[2];
+    a[8] += sz * S[2];
+}
+__device__ __forceinline__ void second_order_scale(float a[9]) {
 #pragma unroll
     for (int j = 0; j < 9; ++j) a[j] *= (j % 4 == 0) ? -0.03125f : -0.0625f;
 }
@@ -398,30 +397,32 @@ __device__ __forceinline__ void interp_cf_node(const RefineParams& r, const Leve
         fz = (k % L) * r.lrfactor + r.lrfactor * 0.5f;
     }
     const long long ne = (long long)r.enx * r.eny * r.cnz;
-    float mc[8][9], Sc[8][6];
+    /* trilinear moments and the second-order terms, one corner at a time */
+    float mom[9], a[9];
+#pragma unroll
+    for (int m = 0; m < 9; ++m) mom[m] = a[m] = 0.f;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         int zc = zb + ((c >> 2) & 1);
         zc = zc < 0 ? zc + r.cnz : (zc >= r.cnz ? zc - r.cnz : zc);
         const long long ce = ((long long)zc * r.eny + (ym + ((c >> 1) & 1))) * r.enx + (xm + (c & 1));
+        float mc[9], Sc[6];
 #pragma unroll
-        for (int m = 0; m < 9; ++m) mc[c][m] = __ldg(mom_c + m * ne + ce);
+        for (int m = 0; m < 9; ++m) mc[m] = __ldg(mom_c + m * ne + ce);
         if (mom_prev) {
 #pragma unroll
-            for (int m = 0; m < 9; ++m) mc[c][m] = (1.f - theta) * __ldg(mom_prev + m * ne + ce) + theta * mc[c][m];
+            for (int m = 0; m < 9; ++m) mc[m] = (1.f - theta) * __ldg(mom_prev + m * ne + ce) + theta * mc[m];
         }
-        strain_rate<float>(mc[c], Sc[c]);
-    }
-    float mom[9];
+        const float wx = (c & 1) ? fx : 1.f - fx, wy = (c & 2) ? fy : 1.f - fy, wz = (c & 4) ? fz : 1.f - fz;
 #pragma unroll
-    for (int m = 0; m < 9; ++m)
-        mom[m] = mc[0][m] * (1.f - fx) * (1.f - fy) * (1.f - fz) + mc[1][m] * fx * (1.f - fy) * (1.f - fz) +
-                 mc[2][m] * (1.f - fx) * fy * (1.f - fz) + mc[3][m] * fx * fy * (1.f - fz) +
-                 mc[4][m] * (1.f - fx) * (1.f - fy) * fz + mc[5][m] * fx * (1.f - fy) * fz +
-                 mc[6][m] * (1.f - fx) * fy * fz + mc[7][m] * fx * fy * fz;
+        for (int m = 0; m < 9; ++m) mom[m] += mc[m] * wx * wy * wz;
+        if (r.order == 2) {
+            strain_rate<float>(mc, Sc);
+            second_order_add(a, c, mc, Sc);
+        }
+    }
     if (r.order == 2) {
-        float a[9];
-        second_order(mc, Sc, a);
+        second_order_scale(a);
         const float wx = 1.f - (4.f * fx * fx - 4.f * fx + 1.f);
         const float wy = 1.f - (4.f * fy * fy - 4.f * fy + 1.f);
         const float wz = 1.f - (4.f * fz * fz - 4.f * fz + 1.f);
@@ -480,27 +481,30 @@ __device__ __forceinline__ void interp_fc_node(const RefineParams& r, const Leve
         k0 = kh;
         k1 = kl;
     }
-    float mc[8][9], Sc[8][6];
+    /* the children's mean moments and the second-order terms, one child at
+     * a time */
+    float sum[9], a[9];
+#pragma unroll
+    for (int m = 0; m < 9; ++m) sum[m] = a[m] = 0.f;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         const int kk = (c & 4) ? k1 : k0;
         const long long cf = kk * F.plane + (long long)(ym + ((c >> 1) & 1)) * F.pitch + (xm + (c & 1));
-        float g[19];
+        float g[19], mc[9], Sc[6];
         load19<S>(F, f_f, cf, g);
-        physical_moments<float>(g, mc[c]);
-        strain_rate<float>(mc[c], Sc[c]);
+        physical_moments<float>(g, mc);
+#pragma unroll
+        for (int m = 0; m < 9; ++m) sum[m] += mc[m];
+        if (r.order == 2) {
+            strain_rate<float>(mc, Sc);
+            second_order_add(a, c, mc, Sc);
+        }
     }
     float mom[9];
 #pragma unroll
-    for (int m = 0; m < 9; ++m) {
-        float s = 0.f;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) s += mc[c][m];
-        mom[m] = 0.125f * s;
-    }
+    for (int m = 0; m < 9; ++m) mom[m] = 0.125f * sum[m];
     if (r.order == 2) {
-        float a[9];
-        second_order(mc, Sc, a);
+        second_order_scale(a);
         mom[1] += a[0] + a[1] + a[2];
         mom[2] += a[3] + a[4] + a[5];
         mom[3] += a[6] + a[7] + a[8];
