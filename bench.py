@@ -23,7 +23,8 @@ staged and built by oracle/ref_recipe.py; a lid cavity) at the same shape.
 `--impl reference` times the channel step on the host cores alone (the
 reference arm), with CPU_3D's figure beside it.  The default line also
 carries the two-level refinement (`c3_refinement`), the closure's
-training ensemble (`c5_ensemble`) and the FP16 / BF16 precision study at
+training ensemble (`c5_ensemble`), the closure's data generation and
+training (`c5_training`) and the FP16 / BF16 precision study at
 768x256x256 over 2000 steps (`c4_precision`) on their own configurations; `--workload`
 prints one of those rows, the precision study (`c4`) or the closure
 deployment (`sgs`) alone.
@@ -501,6 +502,31 @@ def workload_ensemble(steps: int, warmup: int) -> dict:
                 roofline=dict(bound="hbm", achieved=gbs, peak=pk["hbm_gbs"], unit="GB/s", frac=gbs / pk["hbm_gbs"]))
 
 
+def workload_training(train_steps: int = 1000) -> dict:
+    """C5 training: the 16-member ensemble at 2x resolution advanced and
+    box-filtered into samples (lbm_multigpu_gb300.sgs_pipeline.generate),
+    then train_steps Adam steps of the fused forward/backward kernels on
+    them (batch 16384, the closure's coefficient targets)"""
+    import torch
+
+    from lbm_multigpu_gb300 import sgs_pipeline as sp
+
+    sizes = sp.ensemble_sizes(2024, 16)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    X, T, gen = sp.generate(sizes, 2024)
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t0
+    T = sp.coefficient_targets(X, T)
+    P, hist, t_train = sp.train(X, T, steps=train_steps)
+    return dict(workload="C5 training: 16-box ensemble (" + ",".join(map(str, sizes)) + ") at 2x, 6 snapshots, "
+                         f"{train_steps} Adam steps of batch 16384",
+                samples=int(X.shape[0]), ensemble_fine_steps=gen["fine_steps"], ensemble_mlups=gen["mlups"],
+                generate_s=t_gen, train_steps=train_steps, train_s=t_train,
+                train_samples_per_s=train_steps * 16384 / t_train, loss_first=float(hist[:10].mean()),
+                loss_last=float(hist[-10:].mean()))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -659,6 +685,7 @@ def main():
         line["c5_ensemble"] = workload_ensemble(min(args.steps, 64), max(args.warmup, 3))
         # the precision study at its configured 2000 steps, errors at the end
         line["c4_precision"] = workload_c4(2000, every=2000)
+        line["c5_training"] = workload_training()
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
         prog = cpu_reference_program()
