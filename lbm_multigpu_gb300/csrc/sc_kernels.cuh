@@ -178,20 +178,6 @@ constexpr int FEAT_DEVMRT = 16;
  * (StepParams::nu) instead of the LES setting */
 constexpr int FEAT_NUBUF = 32;
 
-/* nodes per thread along z in k_stream_collide (the x/y index work of a
- * thread is done once for all of them) */
-#ifndef LBM_SC_ZN
-#define LBM_SC_ZN 1
-#endif
-constexpr int SC_ZN = LBM_SC_ZN;
-/* with two nodes per thread: load both before updating either */
-#ifndef LBM_SC_PIPE
-#define LBM_SC_PIPE 0
-#endif
-/* a straight-line path for warps whose nodes are all plain fluid */
-#ifndef LBM_SC_FAST
-#define LBM_SC_FAST 0
-#endif
 /* FP16 / BF16 nodes collide their stored deviations (no offsets on the way
  * in and out) */
 #ifndef LBM_SC_DEV
@@ -347,15 +333,6 @@ __device__ __forceinline__ void sc_finish(const Level& L, const StepParams& p, c
     const unsigned xp = (x == L.nx - 1) ? (cl ? x : 0) : x + 1;
     const unsigned ym = (y == 0) ? (cl ? 0 : L.ny - 1) : y - 1;
     const unsigned yp = (y == L.ny - 1) ? (cl ? y : 0) : y + 1;
-#if LBM_SC_FAST
-    const bool plain = type == FLUID && !(HALFWAY && (mbyte & NEAR_SOLID));
-    if (__all_sync(__activemask(), plain)) {
-        sc_collide_store<S, LAY, (FEAT & FEAT_DEVMRT) != 0, (FEAT & FEAT_NUBUF) != 0>(L, p, fB, stats, mom_export, n,
-                                                                                      f, c, x, y, z);
-        if (p.exp_nx > 0) sc_export<S>(L, p, mom_export, f, x, y, z);
-        return;
-    }
-#endif
     if (HALFWAY && (mbyte & NEAR_SOLID)) {
         /* a population that would come from a solid node is the node's own
          * post-collision population of the opposite direction, reflected
@@ -443,25 +420,7 @@ __global__ void __launch_bounds__(SC_BX* SC_BY, sc_min_blocks<FEAT>()) k_stream_
     const int x = blockIdx.x * SC_BX + threadIdx.x;
     const int y = blockIdx.y * SC_BY + threadIdx.y;
     if (x >= L.nx || y >= L.ny) return;
-    if constexpr (SC_ZN == 1) {
-        sc_node<S, FEAT, LAY>(L, p, fA, fB, mask, stats, mom_export, links, x, y, int(blockIdx.z));
-    } else if constexpr (SC_ZN == 2 && LBM_SC_PIPE) {
-        /* two nodes of a z column: the pulls of both in flight before either
-         * is updated (the second is the first again past the last plane, and
-         * is then not updated) */
-        const int z0 = blockIdx.z * 2, z1 = min(z0 + 1, L.nz - 1);
-        const ScNode<LAY> a = sc_setup<FEAT, LAY>(L, mask, x, y, z0);
-        const ScNode<LAY> b = sc_setup<FEAT, LAY>(L, mask, x, y, z1);
-        typename Fmt<S>::T fa[19], fb[19];
-        sc_load<S, LAY>(L, fA, a, fa);
-        sc_load<S, LAY>(L, fA, b, fb);
-        sc_finish<S, FEAT, LAY>(L, p, fA, fB, stats, mom_export, links, a, fa);
-        if (z1 != z0) sc_finish<S, FEAT, LAY>(L, p, fA, fB, stats, mom_export, links, b, fb);
-    } else {
-        const int z0 = blockIdx.z * SC_ZN, z1 = min(z0 + SC_ZN, L.nz);
-#pragma unroll 1
-        for (int z = z0; z < z1; ++z) sc_node<S, FEAT, LAY>(L, p, fA, fB, mask, stats, mom_export, links, x, y, z);
-    }
+    sc_node<S, FEAT, LAY>(L, p, fA, fB, mask, stats, mom_export, links, x, y, int(blockIdx.z));
 }
 
 /* The stream-collide step with the learned subgrid closure in place of the
@@ -476,10 +435,6 @@ constexpr int MLP_BY = 4; /* tile 32 x 4: one M = 128 MMA per layer */
 /* resident blocks per SM the closure kernel is compiled for */
 #ifndef LBM_MLP_MINB
 #define LBM_MLP_MINB 7
-#endif
-/* issue the next tile's pulls before this tile's tensor-core round trips */
-#ifndef LBM_MLP_PREFETCH
-#define LBM_MLP_PREFETCH 0
 #endif
 template <class S, bool HALFWAY, int LAY>
 __global__ void __launch_bounds__(SC_BX* MLP_BY, LBM_MLP_MINB) k_stream_collide_mlp(const Level L, const StepParams p,
@@ -514,19 +469,6 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, LBM_MLP_MINB) k_stream_collide_
         const unsigned zm = (z == 0) ? L.nz - 1 : z - 1, zp = (z == L.nz - 1) ? 0 : z + 1;
         return NodeIdx<LAY>(L, xm, unsigned(x), xp, ym, unsigned(y), yp, zm, unsigned(z), zp);
     };
-    /* the 19 pulls of tile g, issued one tile ahead: they are in flight
-     * while the current tile runs its three tensor-core round trips */
-    float fn[19];
-    auto prefetch = [&](int g) {
-        int x, y, z;
-        node_of(g, x, y, z);
-        if (x < L.nx && y < L.ny) {
-            const NodeIdx<LAY> nn = node_idx(x, y, z);
-#pragma unroll
-            for (int q = 0; q < 19; ++q) fn[q] = F::ld(nn.pull(fA, q), L.off[q]);
-        }
-    };
-    if (LBM_MLP_PREFETCH && int(blockIdx.x) < ntiles) prefetch(blockIdx.x);
     for (int g = blockIdx.x; g < ntiles; g += gridDim.x) {
         int x, y, z;
         node_of(g, x, y, z);
@@ -541,13 +483,8 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, LBM_MLP_MINB) k_stream_collide_
             c = unsigned(z) * plane + unsigned(y) * pitch + unsigned(x);
             const int mbyte = mask[c];
             type = mbyte & TYPE_MASK;
-            if (LBM_MLP_PREFETCH) {
 #pragma unroll
-                for (int q = 0; q < 19; ++q) f[q] = fn[q];
-            } else {
-#pragma unroll
-                for (int q = 0; q < 19; ++q) f[q] = F::ld(n.pull(fA, q), L.off[q]);
-            }
+            for (int q = 0; q < 19; ++q) f[q] = F::ld(n.pull(fA, q), L.off[q]);
             if (HALFWAY && (mbyte & NEAR_SOLID)) {
                 const uint32_t lk = links[c];
 #pragma unroll
@@ -589,7 +526,6 @@ __global__ void __launch_bounds__(SC_BX* MLP_BY, LBM_MLP_MINB) k_stream_collide_
 #pragma unroll
         for (int k = 0; k < 6; ++k) p6[k] *= sc;
         sgs::features_fast(p6, tau0, inv_t0, xf);
-        if (LBM_MLP_PREFETCH && g + int(gridDim.x) < ntiles) prefetch(g + int(gridDim.x));
         /* across the tensor-core round trips only rho, j and the five
          * stresses stay live; the products are formed again afterwards */
         float keep[10] = {mo.rho, mo.jx, mo.jy, mo.jz, mo.n9, mo.n11, mo.n13, mo.n14, mo.n15,
@@ -648,7 +584,7 @@ template <int LAY>
 inline cudaError_t launch_sc_layout(const Level& L, const StepParams& p, const void* fA, void* fB,
                                     const uint8_t* mask, float* stats, float* mom_export, cudaStream_t s,
                                     const uint32_t* links) {
-    const dim3 block(SC_BX, SC_BY), grid(L.pitch / SC_BX, (L.ny + SC_BY - 1) / SC_BY, (L.nz + SC_ZN - 1) / SC_ZN);
+    const dim3 block(SC_BX, SC_BY), grid(L.pitch / SC_BX, (L.ny + SC_BY - 1) / SC_BY, L.nz);
     const bool reduced = L.storage == STORE_F16 || L.storage == STORE_BF16;
     const int feat = (p.halfway ? FEAT_HALFWAY : 0) | (p.has_lid ? FEAT_LID : 0) | (p.pull_clamp ? FEAT_CLAMP : 0) |
                      (p.has_xbc ? FEAT_XBC : 0) |

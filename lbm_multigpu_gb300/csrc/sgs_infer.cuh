@@ -8,10 +8,9 @@
  *   tcgen05.ld -> ReLU + bf16 pack (one cvt per pair) -> shared memory
  *   layer 2:  tcgen05.mma  Z2[ROWS][64] = H1[ROWS][64] W2^T, 4 K-steps
  *             (b2 rides in column HC against the constant unit h1[HC] = 1)
- *   tcgen05.ld -> y = b3 + w3 . ReLU(z2) in FP32 on the CUDA cores
- *             (LBM_INFER_L3CC; else ReLU + bf16 pack -> shared memory and
- *             layer 3 as tcgen05.mma Y[ROWS][16] = H2[ROWS][64] W3^T with
- *             row 0 of W3 = w3, column 0 read back)
+ *   tcgen05.ld -> y = b3 + w3 . ReLU(z2) in FP32 on the CUDA cores (one
+ *             tensor-core round trip fewer than an N = 16 output MMA,
+ *             measured faster)
  *   -> softplus -> the coefficient o (nu_t = o * strain_gain in the caller)
  *
  * Thread t of the block owns row t: MMA h = t / 128 covers rows 128 h ..
@@ -50,21 +49,11 @@ template <int ROWS> struct InferSmem;
  * can serve (512 columns) fit on one SM */
 template <int ROWS> inline size_t infer_dyn_smem();
 
-/* the output layer (64 -> 1) on the CUDA cores from the layer-2
- * accumulators in registers (one tensor-core round trip fewer), or as an
- * N = 16 MMA */
-#ifndef LBM_INFER_L3CC
-#define LBM_INFER_L3CC 1
-#endif
-
 template <int ROWS> struct InferSmem {
     alignas(1024) unsigned char w1[W1_BYTES];
     alignas(1024) unsigned char w2[W2_BYTES];
-#if !LBM_INFER_L3CC
-    alignas(1024) unsigned char w3[W3_BYTES];
-#endif
     /* the layer-1 A operand (features, ROWS x 16 bf16) at the start, then
-     * h1, then h2 (h1 is written only after the layer-1 MMA has read x) */
+     * h1 over it (written only after the layer-1 MMA has read x) */
     alignas(1024) unsigned char a2[ROWS * NH * 2];
     alignas(16) float w3f[NH];
     float b3;
@@ -112,10 +101,6 @@ template <int ROWS> __device__ __forceinline__ void infer_setup(InferSmem<ROWS>&
     for (int i = t; i < int(W1_BYTES / 16); i += ROWS) reinterpret_cast<uint4*>(s.w1)[i] = src[i];
     for (int i = t; i < int(W2_BYTES / 16); i += ROWS)
         reinterpret_cast<uint4*>(s.w2)[i] = src[BLOB_W2 / 16 + i];
-#if !LBM_INFER_L3CC
-    for (int i = t; i < int(W3_BYTES / 16); i += ROWS)
-        reinterpret_cast<uint4*>(s.w3)[i] = src[BLOB_W3 / 16 + i];
-#endif
     /* w3 = row 0 of the blob's output-layer B operand, as FP32 */
     if (t < NH) {
         const __nv_bfloat16 w = *reinterpret_cast<const __nv_bfloat16*>(blob + BLOB_W3 + tc::core_off(0, t, W2_LBO,
@@ -233,9 +218,8 @@ template <int ROWS> __device__ __forceinline__ float infer_nu(InferSmem<ROWS>& s
                                                                    pack_bf16(x[12], x[13]), pack_bf16(x[14], x[15])));
     infer_publish();
     if (s.failed) return -1.f;
-    /* the completions of a call have parities ph, ph ^ 1 (and ph again with
-     * the output layer on the tensor core); the barrier above orders this
-     * read after the previous call's update */
+    /* the two completions of a call have parities ph, ph ^ 1, so every
+     * call starts at the parity set up by infer_setup */
     const uint32_t ph = s.phase;
     const uint32_t id = tc::idesc_bf16_f32(128, NH);
     if (t == 0) {
@@ -256,7 +240,6 @@ template <int ROWS> __device__ __forceinline__ float infer_nu(InferSmem<ROWS>& s
         tc::mma_commit(&s.mbar);
     }
     ok = infer_mma_wait(s, ph ^ 1u) && ok;
-#if LBM_INFER_L3CC
     /* output layer: y = b3 + w3 . relu(z2) in FP32, from the layer-2
      * accumulators (two completions per call: parities ph, ph ^ 1) */
     float y = s.b3;
@@ -277,24 +260,6 @@ template <int ROWS> __device__ __forceinline__ float infer_nu(InferSmem<ROWS>& s
         }
     }
     /* two completions per call leave the parity of the next one at ph */
-#else
-    /* layer 2 epilogue: relu -> h2 over h1 (the layer-2 MMA has finished
-     * reading it) */
-    infer_epilogue<ROWS>(s, ta, t);
-    infer_publish();
-    if (s.failed) return -1.f;
-    if (t == 0) {
-        infer_mma_k64<ROWS>(s.tmem, tc::smem_u32(s.a2), s.w3, tc::idesc_bf16_f32(128, N3));
-        tc::mma_commit(&s.mbar);
-    }
-    ok = infer_mma_wait(s, ph) && ok;
-    uint32_t r0;
-    tc::tmem_ld1(ta, &r0);
-    tc::tmem_wait_ld();
-    tc::tmem_fence_regs<1>(&r0);
-    const float y = __uint_as_float(r0) + s.b3;
-    if (t == 0) s.phase = ph ^ 1u; /* every thread read it before the second infer_publish */
-#endif
     if (!ok) {
         if ((t & 31) == 0) atomicExch(err, 2);
         return 0.f;
