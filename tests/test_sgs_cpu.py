@@ -237,6 +237,35 @@ def test_coefficient_targets_invert_the_strain_gain():
         np.testing.assert_allclose(nu[i], y[0] * x[12] / 0.52, rtol=1e-6)
 
 
+def test_oracle_refresh_schedule():
+    """orc_params.mlp_every: on a refresh step (t % k == 0) the oracle's
+    step equals the every-step closure's and stores each node's nu_t
+    (non-negative, finite); on the steps between it relaxes with the stored
+    values, so the two schedules part after the first step"""
+    from oracle_bindings import OracleRun
+
+    rng = np.random.default_rng(12)
+    nx, ny, nz = 12, 8, 4
+    mask = np.zeros((nz, ny, nx), np.uint8)
+    mask[:, 0, :] = mask[:, -1, :] = 1
+    P = _params(7, 0.2)
+    P[-1] = 10.0
+    runs = [OracleRun(nx, ny, nz, mask, 1 / 0.52, model=0, les=0, init_kind=0, init_u=0.0, mlp=P, mlp_every=k)
+            for k in (1, 4)]
+    f0 = runs[0].fa * (1 + 0.01 * rng.standard_normal(runs[0].fa.shape)).astype(np.float32)  # a stressed state
+    for o in runs:
+        o.fa[:] = f0
+        o.fb[:] = f0
+    for o in runs:
+        o.step(1)
+    np.testing.assert_array_equal(runs[0].fa, runs[1].fa)
+    nu = runs[1]._nu.reshape(nz, ny, nx)[:, 1:-1, :]
+    assert np.isfinite(nu).all() and (nu >= 0).all() and nu.max() > 0
+    for o in runs:
+        o.step(2)
+    assert np.abs(runs[0].fa - runs[1].fa).max() > 0
+
+
 def _bf16(a):
     """round FP32 to bf16 (nearest even) and back to FP32"""
     u = np.asarray(a, np.float32).view(np.uint32).astype(np.uint64)
