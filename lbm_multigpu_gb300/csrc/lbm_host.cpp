@@ -1133,10 +1133,12 @@ int lbm_create(const char* inputs_text, lbm_handle** out) {
             return fail(LBM_ERR_CONFIG, "refinement patch does not fit in the base grid");
         if (c.lrx < 2 * lev + 2 || c.lry < 2 * lev + 2) return fail(LBM_ERR_CONFIG, "refinement patch too small");
     }
-    if (c.sgs_mlp && (c.refinement || c.geometry == "cavity" || c.geometry == "duct" || c.faces_set || c.pull_clamp ||
-                      storage == STORE_F64))
-        return fail(LBM_ERR_CONFIG, "SGS mlp runs on channel, dyninlet and periodic levels without refinement or "
-                                    "FACES, FP32/FP16/BF16");
+    /* the closure's collision carries no body force (the dynamic inlet's
+     * DPDY drive) */
+    if (c.sgs_mlp && (c.refinement || c.geometry == "cavity" || c.geometry == "duct" || c.geometry == "dyninlet" ||
+                      c.faces_set || c.pull_clamp || c.dpdy != 0.f || storage == STORE_F64))
+        return fail(LBM_ERR_CONFIG, "SGS mlp runs on channel and periodic levels without refinement, FACES or a "
+                                    "body force (DPDY), FP32/FP16/BF16");
     std::vector<float> sgs_params;
     if (!c.sgs_weights.empty()) {
         std::ifstream in(c.sgs_weights, std::ios::binary);

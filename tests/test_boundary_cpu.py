@@ -99,6 +99,19 @@ def test_malformed_records_are_rejected(product, text, code, msg):
     assert e.value.code == code and msg in str(e.value)
 
 
+@pytest.mark.parametrize("kw", [dict(geometry="dyninlet"), dict(geometry="channel_square", dpdy=-2e-6),
+                                dict(geometry="cavity"), dict(geometry="channel_square", precision="fp64")])
+def test_closure_configurations_are_rejected(product, kw):
+    """the learned closure's collision carries no body force and runs on
+    channel and periodic levels in FP32/FP16/BF16: other records are
+    refused before any device work (LBM_ERR_CONFIG)"""
+    t = product.make_inputs(64, 24, 6, obst1=(20.5, 11.5, 0.0), r1=4.0, re=60.0, umax=0.05, tmax=10, les=1,
+                            sgs="mlp", **kw)
+    with pytest.raises(product.LbmError) as e:
+        product.Solver(t)
+    assert e.value.code == 4 and "SGS mlp" in str(e.value)
+
+
 def test_masks_of_every_geometry(product):
     for geom, expect in (("channel_square", {0, 1, 2, 3, 4}), ("channel_circle", {0, 1, 2, 3, 4}),
                          ("channel", {0, 1, 3, 4}), ("cavity", {0, 1, 7}), ("periodic", {0})):
