@@ -220,7 +220,10 @@ int parse_inputs(const char* text, Config& c) {
         else if (key == "KP") F(c.kp);
         /* extension keys */
         else if (key == "GEOMETRY") c.geometry = val;
-        else if (key == "PRECISION") c.precision = val;
+        else if (key == "PRECISION") {
+            ok = (val == "fp32" || val == "fp16" || val == "bf16" || val == "fp64");
+            c.precision = val;
+        }
         else if (key == "LAYOUT") {
             ok = (val == "soa" || val == "blocked" || val == "auto");
             c.pop_layout = val;

@@ -92,6 +92,8 @@ def test_make_inputs_is_a_fixed_point(product):
     ("Base domain size \t64x24x6\nRE: \tabc\n", 3, "cannot read"),
     ("Base domain size \t64x24x6\nWhat: \t1\n", 3, "unknown key"),
     ("Base domain size \t64x24x6\nSGS every: \t0\n", 3, "cannot read"),
+    ("Base domain size \t64x24x6\nLAYOUT: \tweird\n", 3, "cannot read"),
+    ("Base domain size \t64x24x6\nPRECISION: \tfp8\n", 3, "cannot read"),
 ])
 def test_malformed_records_are_rejected(product, text, code, msg):
     with pytest.raises(product.LbmError) as e:
